@@ -1,0 +1,57 @@
+"""Collect the reference's own golden fixtures for the per-frequency path.
+
+Run once in a checkout that has the HAMS-MREL reference next to it:
+
+    python tests/golden/make_golden.py /path/to/HAMS-MREL
+
+It copies, unchanged, the input decks and the expected HAMS/WAMIT-format
+outputs of three reference cases into tests/golden/<case>/:
+
+  config1   test/data/config1            3 bodies x 234 panels, h = 70 m,
+                                         3 frequencies x 3 headings, IRSP = 0
+                                         (the reference's integration test)
+  example5  examples/example5_single_body  234 hull + 383 lid panels, h = 70 m,
+                                         10 frequencies x 36 headings, IRSP = 1
+  example3  examples/example3_multi_bodies_gen_mod
+                                         2 bodies with lids and generalized
+                                         modes, IRSP = 1
+
+The GPU machine has no copy of the reference, so the tests read only these
+committed files.
+"""
+import os
+import shutil
+import sys
+
+CASES = {
+    "config1": ("test/data/config1/input", "test/data/config1/expected_output",
+                ["OAMASS%d.txt", "ODAMPING%d.txt", "OEXFOR%d.txt"]),
+    "example5": ("examples/example5_single_body/Input", "examples/example5_single_body/Output",
+                 ["Hams_format/OAMASS%d.txt", "Hams_format/ODAMPING%d.txt", "Hams_format/OEXFOR%d.txt",
+                  "Wamit_format/AmssDamp.1", "Wamit_format/ExcForce.3"]),
+    "example3": ("examples/example3_multi_bodies_gen_mod/Input",
+                 "examples/example3_multi_bodies_gen_mod/Output",
+                 ["Hams_format/OAMASS%d.txt", "Hams_format/ODAMPING%d.txt", "Hams_format/OEXFOR%d.txt",
+                  "Wamit_format/AmssDamp.1", "Wamit_format/ExcForce.3"]),
+}
+
+
+def main(ref_root: str) -> None:
+    here = os.path.dirname(os.path.abspath(__file__))
+    for case, (inp, out, patterns) in CASES.items():
+        dst_in = os.path.join(here, case, "input")
+        dst_out = os.path.join(here, case, "expected")
+        os.makedirs(dst_in, exist_ok=True)
+        os.makedirs(dst_out, exist_ok=True)
+        for name in sorted(os.listdir(os.path.join(ref_root, inp))):
+            shutil.copy(os.path.join(ref_root, inp, name), os.path.join(dst_in, name))
+        for pat in patterns:
+            names = [pat % k for k in range(1, 7)] if "%d" in pat else [pat]
+            for name in names:
+                src = os.path.join(ref_root, out, name)
+                if os.path.exists(src):
+                    shutil.copy(src, os.path.join(dst_out, os.path.basename(name)))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
