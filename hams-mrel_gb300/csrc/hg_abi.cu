@@ -1,0 +1,659 @@
+// C-ABI of the GB300 per-frequency BEM library (declared in include/hamsgpu.h).
+//
+// One context holds the device copy of the mesh, the per-frequency
+// matrices, the LU factors and the solution columns.  Each entry point maps
+// onto one group of the reference's Fortran subroutines (see hamsgpu.h).
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/hamsgpu.h"
+#include "hg_common.cuh"
+#include "hg_green.cuh"
+#include "hg_kernels.cuh"
+#include "hg_linalg.cuh"
+
+using hg::FinState;
+
+namespace {
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t cap = 0;  // elements
+  cudaError_t ensure(size_t count) {
+    if (count <= cap && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc((void**)&p, (count ? count : 1) * sizeof(T));
+    if (e == cudaSuccess) cap = count;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+}  // namespace
+
+struct hg_ctx {
+  hg_opts o;
+  cudaStream_t st = nullptr;
+  std::string err;
+  // mesh
+  int n = 0, nl = 0, tn = 0, tnf = 0, ntnd = 0, nbody = 0;  // tn: rows of the current solve, tnf: n + nl
+  bool mesh_set = false;
+  std::vector<int> bstart, bend;
+  DevBuf<double> nodes, xyz_p, ds, pnsz, dxyz, rec, fx, betas;
+  DevBuf<int> ncon, ncn, body_of, body_start, body_end, ipiv, status, info;
+  // frequency
+  double v = 0, wk = 0, w1 = 0, h = -1, nm0 = 0;
+  int nk = 0;
+  bool freq_set = false;
+  DevBuf<double> wvn;
+  // matrices
+  DevBuf<double2> A, S, C, A64, B, X, R, R2, W, part, exfc;
+  DevBuf<float2> Af, Sf, Cf, Bf;
+  DevBuf<double> amas, bdmp;
+  int irsp = 0;
+  bool factored = false;
+  bool keep = false;
+  // last solve
+  int nbeta = 0;
+  std::vector<double> betas_h;
+  bool rad_done = false, dif_done = false;
+  int sweeps = 0;
+  double resid = 0.0;
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  float stage_ms[4] = {0, 0, 0, 0};
+};
+
+namespace {
+
+int fail(hg_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  c->err = buf;
+  return code;
+}
+
+#define CK(call)                                                                                    \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess)                                                                          \
+      return fail(c, HG_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                  __LINE__);                                                                        \
+  } while (0)
+
+int check_status(hg_ctx* c) {
+  int st = 0;
+  CK(cudaMemcpyAsync(&st, c->status.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (st != 0) {
+    CK(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->st));
+    return fail(c, HG_ERR_DEVICE, "device status 0x%x (1: series cap, 2: quadrature stack, 4: wait timeout, 64: bad node id)",
+                st);
+  }
+  return 0;
+}
+
+FinState fin_state(const hg_ctx* c) {
+  FinState fs;
+  fs.v = c->v;
+  fs.wk = c->wk;
+  fs.h = c->h;
+  fs.nm0 = c->nm0;
+  fs.wvn = c->wvn.p;
+  fs.nk = c->nk;
+  fs.status = c->status.p;
+  return fs;
+}
+
+bool mixed(const hg_ctx* c) { return c->o.precision == HG_PREC_MIXED; }
+
+int ncols_total(const hg_ctx* c) { return 6 * c->nbody + c->nbeta; }
+
+// Ensure the B/X/R buffers hold 6*nbody + nbeta columns.
+int ensure_rhs(hg_ctx* c, int nbeta) {
+  const int nc = 6 * c->nbody + nbeta;
+  CK(c->B.ensure((size_t)c->tn * nc));
+  CK(c->X.ensure((size_t)c->n * nc));
+  CK(c->W.ensure((size_t)c->n * (nbeta > 0 ? nbeta : 1)));
+  CK(c->part.ensure(hg::rhs_work_bytes(c->n, c->tn, c->nbody, nbeta) / sizeof(double2) + 1));
+  CK(c->betas.ensure(nbeta > 0 ? nbeta : 1));
+  if (mixed(c)) {
+    CK(c->R.ensure((size_t)c->tn * nc));
+    CK(c->R2.ensure((size_t)c->n * nc));
+    CK(c->Bf.ensure((size_t)c->n * nc));
+  } else if (c->irsp == 1) {
+    CK(c->R2.ensure((size_t)c->n * nc));
+  }
+  return 0;
+}
+
+// Column norms of a complex128 block: out[k] = max over rows |re|+|im|.
+__global__ void k_colmax(int rows, const double2* __restrict__ M, long ld, double* __restrict__ out) {
+  const int col = blockIdx.x;
+  double m = 0.0;
+  for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+    const double2 v = M[r + (long)col * ld];
+    m = fmax(m, fabs(v.x) + fabs(v.y));
+  }
+  for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, off));
+  __shared__ double sm[32];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = fmax(t, sm[w]);
+    out[col] = t;
+  }
+}
+
+// Solve M X[:, c0:c1] = rhs for the current factorisation.  rhs is B (tn
+// rows) for irsp = 0, or the normal-equation right-hand side A^T B for irsp = 1.
+int solve_cols(hg_ctx* c, int c0, int c1) {
+  const int n = c->n, tn = c->tn, nc = c1 - c0;
+  if (nc <= 0) return 0;
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0), mone = make_double2(-1, 0);
+  double2* Bc = c->B.p + (size_t)c0 * tn;
+  double2* Xc = c->X.p + (size_t)c0 * n;
+  if (!mixed(c)) {
+    if (c->irsp == 1) {
+      CK(hg::gemm<double>(c->st, true, n, nc, tn, one, c->A.p, tn, Bc, tn, zero, Xc, n));
+      CK(hg::getrs<double>(c->st, n, nc, c->C.p, n, c->ipiv.p, Xc, n));
+    } else {
+      CK(cudaMemcpy2DAsync(Xc, (size_t)n * sizeof(double2), Bc, (size_t)tn * sizeof(double2), (size_t)n * sizeof(double2),
+                           nc, cudaMemcpyDeviceToDevice, c->st));
+      CK(hg::getrs<double>(c->st, n, nc, c->A.p, tn, c->ipiv.p, Xc, n));
+    }
+    c->sweeps = 0;
+    c->resid = 0.0;
+    return 0;
+  }
+  // ---- mixed form: complex64 LU + FP64 iterative refinement ----
+  const float2* LU = (c->irsp == 1) ? c->Cf.p : c->Af.p;
+  const long ldlu = (c->irsp == 1) ? n : tn;
+  double2* Rh = c->R2.p + (size_t)c0 * n;  // n x nc right-hand side of the square system
+  float2* Bf = c->Bf.p + (size_t)c0 * n;
+  if (c->irsp == 1) CK(hg::gemm<double>(c->st, true, n, nc, tn, one, c->A64.p, tn, Bc, tn, zero, Rh, n));
+  else CK(cudaMemcpy2DAsync(Rh, (size_t)n * sizeof(double2), Bc, (size_t)tn * sizeof(double2), (size_t)n * sizeof(double2),
+                            nc, cudaMemcpyDeviceToDevice, c->st));
+  // norms of the square-system right-hand side
+  DevBuf<double> nb;
+  CK(nb.ensure(2 * (size_t)nc));
+  k_colmax<<<nc, 256, 0, c->st>>>(n, Rh, n, nb.p);
+  std::vector<double> bnorm(nc), rnorm(nc);
+  CK(cudaMemcpyAsync(bnorm.data(), nb.p, nc * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  // x0 = M^{-1} b in complex64
+  CK(hg::convert_z2c_2d(c->st, n, nc, Rh, n, Bf, n));
+  CK(hg::getrs<float>(c->st, n, nc, LU, ldlu, c->ipiv.p, Bf, n));
+  CK(cudaMemsetAsync(Xc, 0, (size_t)n * nc * sizeof(double2), c->st));
+  CK(hg::add_c2z_2d(c->st, n, nc, Bf, n, Xc, n));
+  int sweep = 0;
+  double worst = 0.0;
+  for (;;) {
+    // r = b - M x in FP64 (M = A, or A^T A applied as A^T (B - A x))
+    if (c->irsp == 1) {
+      double2* R1 = c->R.p + (size_t)c0 * tn;
+      CK(cudaMemcpy2DAsync(R1, (size_t)tn * sizeof(double2), Bc, (size_t)tn * sizeof(double2), (size_t)tn * sizeof(double2),
+                           nc, cudaMemcpyDeviceToDevice, c->st));
+      CK(hg::gemm<double>(c->st, false, tn, nc, n, mone, c->A64.p, tn, Xc, n, one, R1, tn));
+      CK(hg::gemm<double>(c->st, true, n, nc, tn, one, c->A64.p, tn, R1, tn, zero, Rh, n));
+    } else {
+      CK(cudaMemcpy2DAsync(Rh, (size_t)n * sizeof(double2), Bc, (size_t)tn * sizeof(double2), (size_t)n * sizeof(double2),
+                           nc, cudaMemcpyDeviceToDevice, c->st));
+      CK(hg::gemm<double>(c->st, false, n, nc, n, mone, c->A64.p, tn, Xc, n, one, Rh, n));
+    }
+    k_colmax<<<nc, 256, 0, c->st>>>(n, Rh, n, nb.p + nc);
+    CK(cudaMemcpyAsync(rnorm.data(), nb.p + nc, nc * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    worst = 0.0;
+    for (int k = 0; k < nc; ++k) worst = std::fmax(worst, bnorm[k] > 0 ? rnorm[k] / bnorm[k] : rnorm[k]);
+    if (worst <= c->o.refine_tol || sweep >= c->o.max_refine) break;
+    // x += M^{-1} r (complex64 correction)
+    CK(hg::convert_z2c_2d(c->st, n, nc, Rh, n, Bf, n));
+    CK(hg::getrs<float>(c->st, n, nc, LU, ldlu, c->ipiv.p, Bf, n));
+    CK(hg::add_c2z_2d(c->st, n, nc, Bf, n, Xc, n));
+    ++sweep;
+  }
+  nb.release();
+  c->sweeps = sweep;
+  c->resid = worst;
+  return 0;
+}
+
+int build_rhs(hg_ctx* c, int nbeta, const double* betas_h, bool modes) {
+  int r = ensure_rhs(c, nbeta);
+  if (r) return r;
+  if (nbeta > 0) {
+    CK(cudaMemcpyAsync(c->betas.p, betas_h, nbeta * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(hg::launch_incident(c->st, c->n, c->xyz_p.p, c->dxyz.p, nbeta, c->betas.p, c->v, c->wk, c->w1, c->h, c->W.p));
+  }
+  if (mixed(c))
+    CK(hg::launch_rhs<float2>(c->st, c->n, c->tn, c->Sf.p, c->tn, c->dxyz.p, c->body_of.p, c->nbody, nbeta, c->W.p,
+                              c->part.p, c->B.p, c->tn));
+  else
+    CK(hg::launch_rhs<double2>(c->st, c->n, c->tn, c->S.p, c->tn, c->dxyz.p, c->body_of.p, c->nbody, nbeta, c->W.p,
+                               c->part.p, c->B.p, c->tn));
+  (void)modes;
+  return 0;
+}
+
+int copy_out(hg_ctx* c, int c0, int nc, double* host, int ldm) {
+  if (!host || nc <= 0) return 0;
+  CK(cudaMemcpy2DAsync(host, (size_t)ldm * sizeof(double2), c->X.p + (size_t)c0 * c->n, (size_t)c->n * sizeof(double2),
+                       (size_t)c->n * sizeof(double2), nc, cudaMemcpyDeviceToHost, c->st));
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void hg_default_opts(hg_opts* o) {
+  if (!o) return;
+  o->device = 0;
+  o->precision = HG_PREC_FP64;
+  o->grn_kind = 8;
+  o->max_refine = 10;
+  o->refine_tol = 1e-12;
+  o->rho = 1000.0;
+  o->g = 9.80665;
+}
+
+int hg_create(hg_ctx** out, const hg_opts* opts) {
+  if (!out) return -1;
+  *out = nullptr;
+  hg_ctx* c = new (std::nothrow) hg_ctx();
+  if (!c) return HG_ERR_ALLOC;
+  hg_default_opts(&c->o);
+  if (opts) c->o = *opts;
+  if (c->o.precision != HG_PREC_FP64 && c->o.precision != HG_PREC_MIXED) { delete c; return -2; }
+  if (c->o.grn_kind != 4 && c->o.grn_kind != 8) { delete c; return -2; }
+  cudaError_t e = cudaSetDevice(c->o.device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+  for (int k = 0; k < 5 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
+  if (e == cudaSuccess) e = c->status.ensure(1);
+  if (e == cudaSuccess) e = c->info.ensure(1);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->status.p, 0, sizeof(int), c->st);
+  if (e != cudaSuccess) {
+    hg_destroy(c);
+    return HG_ERR_CUDA;
+  }
+  *out = c;
+  return 0;
+}
+
+void hg_destroy(hg_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->o.device);
+  if (c->st) cudaStreamSynchronize(c->st);
+  DevBuf<double>* dbs[] = {&c->nodes, &c->xyz_p, &c->ds, &c->pnsz, &c->dxyz, &c->rec, &c->fx, &c->betas,
+                           &c->wvn, &c->amas, &c->bdmp};
+  for (auto* b : dbs) b->release();
+  DevBuf<int>* ibs[] = {&c->ncon, &c->ncn, &c->body_of, &c->body_start, &c->body_end, &c->ipiv, &c->status, &c->info};
+  for (auto* b : ibs) b->release();
+  DevBuf<double2>* zbs[] = {&c->A, &c->S, &c->C, &c->A64, &c->B, &c->X, &c->R, &c->R2, &c->W, &c->part, &c->exfc};
+  for (auto* b : zbs) b->release();
+  DevBuf<float2>* cbs[] = {&c->Af, &c->Sf, &c->Cf, &c->Bf};
+  for (auto* b : cbs) b->release();
+  for (int k = 0; k < 5; ++k)
+    if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+}
+
+const char* hg_last_error(const hg_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int hg_set_mesh(hg_ctx* c, int n, int ntnd, const double* nodes, const int* ncon, const int* ncn, const double* xyz_p,
+                const double* ds, const double* pnsz, const double* dxyz_p, int nl, const double* lid_xyz_p, int nbody,
+                const int* body_ranges) {
+  if (!c) return -1;
+  if (n <= 0) return fail(c, -2, "n must be positive");
+  if (ntnd <= 0) return fail(c, -3, "ntnd must be positive");
+  if (!nodes) return fail(c, -4, "nodes is NULL");
+  if (!ncon) return fail(c, -5, "ncon is NULL");
+  if (!ncn) return fail(c, -6, "ncn is NULL");
+  if (!xyz_p) return fail(c, -7, "xyz_p is NULL");
+  if (!ds) return fail(c, -8, "ds is NULL");
+  if (!pnsz) return fail(c, -9, "pnsz is NULL");
+  if (!dxyz_p) return fail(c, -10, "dxyz_p is NULL");
+  if (nl < 0 || (nl > 0 && !lid_xyz_p)) return fail(c, -11, "bad lid arrays");
+  if (nbody <= 0) return fail(c, -13, "nbody must be positive");
+  if (!body_ranges) return fail(c, -14, "body_ranges is NULL");
+  for (int e = 0; e < n; ++e) {
+    if (ncn[e] != 3 && ncn[e] != 4) return fail(c, -6, "panel %d has %d vertices (3 or 4 expected)", e + 1, ncn[e]);
+    for (int k = 0; k < ncn[e]; ++k) {
+      const int id = ncon[e + (size_t)k * n];
+      if (id < 1 || id > ntnd) return fail(c, -5, "panel %d vertex %d: node id %d out of 1..%d", e + 1, k + 1, id, ntnd);
+    }
+  }
+  std::vector<int> body_of(n, -1), bs(nbody), be(nbody);
+  int prev = 0;
+  for (int b = 0; b < nbody; ++b) {
+    const int s = body_ranges[2 * b] - 1, t = body_ranges[2 * b + 1];
+    if (s != prev || t < s || t > n) return fail(c, -14, "body %d range [%d,%d] is not contiguous in 1..%d", b + 1, s + 1, t, n);
+    bs[b] = s;
+    be[b] = t;
+    for (int e = s; e < t; ++e) body_of[e] = b;
+    prev = t;
+  }
+  if (prev != n) return fail(c, -14, "body ranges cover %d of %d panels", prev, n);
+  cudaSetDevice(c->o.device);
+  c->n = n; c->nl = nl; c->tn = n + nl; c->tnf = n + nl; c->ntnd = ntnd; c->nbody = nbody;
+  c->bstart = bs; c->bend = be;
+  CK(c->nodes.ensure((size_t)ntnd * 3));
+  CK(c->ncon.ensure((size_t)n * 4));
+  CK(c->ncn.ensure(n));
+  CK(c->xyz_p.ensure((size_t)n * 3));
+  CK(c->ds.ensure(n));
+  CK(c->pnsz.ensure(n));
+  CK(c->dxyz.ensure((size_t)n * 6));
+  CK(c->rec.ensure((size_t)n * PR_SIZE));
+  CK(c->fx.ensure((size_t)c->tnf * 3));
+  CK(c->body_of.ensure(n));
+  CK(c->body_start.ensure(nbody));
+  CK(c->body_end.ensure(nbody));
+  CK(cudaMemcpyAsync(c->nodes.p, nodes, (size_t)ntnd * 3 * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->ncon.p, ncon, (size_t)n * 4 * sizeof(int), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->ncn.p, ncn, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->xyz_p.p, xyz_p, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->ds.p, ds, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->pnsz.p, pnsz, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->dxyz.p, dxyz_p, (size_t)n * 6 * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->body_of.p, body_of.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->body_start.p, bs.data(), nbody * sizeof(int), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->body_end.p, be.data(), nbody * sizeof(int), cudaMemcpyHostToDevice, c->st));
+  // field points: hull centroids then lid centroids, column-major tn x 3
+  for (int k = 0; k < 3; ++k) {
+    CK(cudaMemcpyAsync(c->fx.p + (size_t)k * c->tnf, xyz_p + (size_t)k * n, (size_t)n * sizeof(double),
+                       cudaMemcpyHostToDevice, c->st));
+    if (nl > 0)
+      CK(cudaMemcpyAsync(c->fx.p + (size_t)k * c->tnf + n, lid_xyz_p + (size_t)k * nl, (size_t)nl * sizeof(double),
+                         cudaMemcpyHostToDevice, c->st));
+  }
+  CK(hg::launch_prep_panels(c->st, n, ntnd, c->nodes.p, c->ncon.p, c->ncn.p, c->xyz_p.p, c->ds.p, c->pnsz.p, c->dxyz.p,
+                            c->rec.p, c->status.p));
+  CK(cudaStreamSynchronize(c->st));
+  int r = check_status(c);
+  if (r) return r;
+  c->mesh_set = true;
+  c->factored = false;
+  c->rad_done = c->dif_done = false;
+  return 0;
+}
+
+int hg_set_frequency(hg_ctx* c, double v, double wk, double w1, double h, const double* wvn, int nk) {
+  if (!c) return -1;
+  if (!std::isfinite(v)) return fail(c, -2, "v is not finite");
+  if (h > 0.0) {
+    if (!wvn) return fail(c, -6, "finite depth needs the dispersion roots");
+    if (nk < 20) return fail(c, -7, "finite depth needs at least 20 dispersion roots (got %d)", nk);
+    if (!(wk > 0.0) && !(fabs(v) < (double)1.e-8f) && !(fabs(v + 1.0) < (double)1.e-8f))
+      return fail(c, -3, "wave number must be positive");
+  }
+  c->v = v; c->wk = wk; c->w1 = w1; c->h = h; c->nk = (h > 0.0) ? nk : 0;
+  if (h > 0.0) {
+    CK(c->wvn.ensure(nk));
+    CK(cudaMemcpyAsync(c->wvn.p, wvn, nk * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    c->nm0 = h / 2.0 * (1.0 + std::sinh(2.0 * wk * h) / (2.0 * wk * h));
+  }
+  c->freq_set = true;
+  c->factored = false;
+  c->rad_done = c->dif_done = false;
+  return 0;
+}
+
+int hg_keep_matrices(hg_ctx* c, int keep) {
+  if (!c) return -1;
+  c->keep = keep != 0;
+  return 0;
+}
+
+int hg_fill_factor(hg_ctx* c, int irsp) {
+  if (!c) return -1;
+  if (irsp != 0 && irsp != 1) return fail(c, -2, "irsp must be 0 or 1");
+  if (!c->mesh_set || !c->freq_set) return fail(c, HG_ERR_STATE, "hg_set_mesh and hg_set_frequency must come first");
+  if (irsp == 1 && c->nl == 0) return fail(c, -2, "irsp = 1 needs lid panels in hg_set_mesh");
+  cudaSetDevice(c->o.device);
+  c->irsp = irsp;
+  const int n = c->n, tn = (irsp == 1) ? c->tnf : c->n;
+  c->tn = tn;  // rows used by this solve (lid rows only with irsp = 1)
+  const FinState fs = fin_state(c);
+  const bool deep = c->h < 0.0;
+  CK(cudaEventRecord(c->ev[0], c->st));
+  CK(c->ipiv.ensure(n));
+  if (!mixed(c)) {
+    CK(c->A.ensure((size_t)tn * n));
+    CK(c->S.ensure((size_t)tn * n));
+    CK(hg::launch_green_fill<double2>(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, deep, c->o.grn_kind, c->A.p, c->S.p, tn,
+                                      c->status.p));
+    if (c->keep && irsp == 0) {
+      CK(c->A64.ensure((size_t)tn * n));
+      CK(cudaMemcpyAsync(c->A64.p, c->A.p, (size_t)tn * n * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
+    }
+    CK(cudaEventRecord(c->ev[1], c->st));
+    if (irsp == 1) {
+      CK(c->C.ensure((size_t)n * n));
+      CK(hg::gemm<double>(c->st, true, n, n, tn, make_double2(1, 0), c->A.p, tn, c->A.p, tn, make_double2(0, 0), c->C.p,
+                          n));
+      CK(hg::getrf<double>(c->st, n, c->C.p, n, c->ipiv.p, c->info.p, nullptr));
+    } else {
+      CK(hg::getrf<double>(c->st, n, c->A.p, tn, c->ipiv.p, c->info.p, nullptr));
+    }
+  } else {
+    CK(c->Af.ensure((size_t)tn * n));
+    CK(c->Sf.ensure((size_t)tn * n));
+    CK(c->A64.ensure((size_t)tn * n));
+    CK(hg::launch_green_fill<float2>(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, deep, c->o.grn_kind, c->Af.p, c->Sf.p, tn,
+                                     c->status.p));
+    CK(hg::convert_c2z(c->st, (long)tn * n, c->Af.p, c->A64.p));
+    CK(cudaEventRecord(c->ev[1], c->st));
+    if (irsp == 1) {
+      CK(c->Cf.ensure((size_t)n * n));
+      CK(hg::gemm<float>(c->st, true, n, n, tn, make_float2(1, 0), c->Af.p, tn, c->Af.p, tn, make_float2(0, 0), c->Cf.p,
+                         n));
+      CK(hg::getrf<float>(c->st, n, c->Cf.p, n, c->ipiv.p, c->info.p, nullptr));
+    } else {
+      CK(hg::getrf<float>(c->st, n, c->Af.p, tn, c->ipiv.p, c->info.p, nullptr));
+    }
+  }
+  CK(cudaEventRecord(c->ev[2], c->st));
+  int info = 0;
+  CK(cudaMemcpyAsync(&info, c->info.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  int r = check_status(c);
+  if (r) return r;
+  CK(cudaEventElapsedTime(&c->stage_ms[0], c->ev[0], c->ev[1]));
+  CK(cudaEventElapsedTime(&c->stage_ms[1], c->ev[1], c->ev[2]));
+  c->factored = (info == 0);
+  c->rad_done = c->dif_done = false;
+  if (info != 0) return fail(c, info, "zero pivot at row %d", info);
+  return 0;
+}
+
+int hg_solve_radiation(hg_ctx* c, double* mxpot, int ldm) {
+  if (!c) return -1;
+  if (!c->factored) return fail(c, HG_ERR_STATE, "hg_fill_factor must succeed first");
+  if (mxpot && ldm < c->n) return fail(c, -3, "ldm %d < n %d", ldm, c->n);
+  c->nbeta = 0;
+  int r = build_rhs(c, 0, nullptr, true);
+  if (r) return r;
+  r = solve_cols(c, 0, 6 * c->nbody);
+  if (r) return r;
+  r = copy_out(c, 0, 6 * c->nbody, mxpot, ldm);
+  if (r) return r;
+  CK(cudaStreamSynchronize(c->st));
+  c->rad_done = true;
+  c->dif_done = false;
+  return 0;
+}
+
+int hg_solve_all_headings(hg_ctx* c, const double* betas, int nbeta, double* mxpot_dif, int ldm) {
+  if (!c) return -1;
+  if (!c->factored) return fail(c, HG_ERR_STATE, "hg_fill_factor must succeed first");
+  if (nbeta <= 0 || !betas) return fail(c, -3, "need at least one heading");
+  if (mxpot_dif && ldm < c->n) return fail(c, -5, "ldm %d < n %d", ldm, c->n);
+  // keep the radiation columns: move them aside if B/X must grow
+  const int nr = 6 * c->nbody;
+  std::vector<double2> keepx;
+  if (c->rad_done && (size_t)c->n * (nr + nbeta) > c->X.cap) {
+    keepx.resize((size_t)c->n * nr);
+    CK(cudaMemcpyAsync(keepx.data(), c->X.p, keepx.size() * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  }
+  c->nbeta = nbeta;
+  c->betas_h.assign(betas, betas + nbeta);
+  int r = build_rhs(c, nbeta, betas, false);
+  if (r) return r;
+  if (!keepx.empty())
+    CK(cudaMemcpyAsync(c->X.p, keepx.data(), keepx.size() * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+  r = solve_cols(c, nr, nr + nbeta);
+  if (r) return r;
+  r = copy_out(c, nr, nbeta, mxpot_dif, ldm);
+  if (r) return r;
+  CK(cudaStreamSynchronize(c->st));
+  c->dif_done = true;
+  return 0;
+}
+
+int hg_solve_diffraction(hg_ctx* c, double beta, double* mxpot_col) {
+  if (!c) return -1;
+  return hg_solve_all_headings(c, &beta, 1, mxpot_col, c->n);
+}
+
+int hg_forces(hg_ctx* c, int isol, double* amas, double* bdmp, double* exfc) {
+  if (!c) return -1;
+  if (!c->rad_done) return fail(c, HG_ERR_STATE, "hg_solve_radiation must run first");
+  if (isol != 1 && isol != 2) return fail(c, -2, "isol must be 1 or 2");
+  const int nd = 6 * c->nbody, nbeta = c->dif_done ? c->nbeta : 0;
+  CK(c->amas.ensure((size_t)nd * nd));
+  CK(c->bdmp.ensure((size_t)nd * nd));
+  CK(c->exfc.ensure((size_t)(nbeta > 0 ? nbeta : 1) * nd));
+  CK(hg::launch_forces(c->st, c->n, c->X.p, c->n, c->xyz_p.p, c->ds.p, c->dxyz.p, c->body_start.p, c->body_end.p,
+                       c->nbody, nbeta, c->betas.p, c->v, c->wk, c->w1, c->h, isol, c->o.rho, c->o.g, c->amas.p,
+                       c->bdmp.p, c->exfc.p));
+  // device layout is row-major [row][col]; the ABI returns column-major
+  std::vector<double> a((size_t)nd * nd), b((size_t)nd * nd);
+  std::vector<double2> f((size_t)(nbeta > 0 ? nbeta : 1) * nd);
+  CK(cudaMemcpyAsync(a.data(), c->amas.p, a.size() * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(b.data(), c->bdmp.p, b.size() * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  if (nbeta > 0) CK(cudaMemcpyAsync(f.data(), c->exfc.p, (size_t)nbeta * nd * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  for (int i = 0; i < nd; ++i)
+    for (int j = 0; j < nd; ++j) {
+      if (amas) amas[i + (size_t)j * nd] = a[(size_t)i * nd + j];
+      if (bdmp) bdmp[i + (size_t)j * nd] = b[(size_t)i * nd + j];
+    }
+  if (exfc)
+    for (int k = 0; k < nbeta; ++k)
+      for (int d = 0; d < nd; ++d) {
+        exfc[2 * (k + (size_t)d * nbeta)] = f[(size_t)k * nd + d].x;
+        exfc[2 * (k + (size_t)d * nbeta) + 1] = f[(size_t)k * nd + d].y;
+      }
+  return 0;
+}
+
+int hg_solve_frequency(hg_ctx* c, double v, double wk, double w1, double h, const double* wvn, int nk, int irsp,
+                       const double* betas, int nbeta, int isol, double* amas, double* bdmp, double* exfc,
+                       double* mxpot, int ldm) {
+  if (!c) return -1;
+  if (nbeta < 0) return fail(c, -9, "nbeta must be >= 0");
+  if (nbeta > 0 && !betas) return fail(c, -8, "betas is NULL");
+  if (mxpot && ldm < c->n) return fail(c, -15, "ldm %d < n %d", ldm, c->n);
+  int r = hg_set_frequency(c, v, wk, w1, h, wvn, nk);
+  if (r) return r;
+  r = hg_fill_factor(c, irsp);
+  if (r) return r;
+  CK(cudaEventRecord(c->ev[2], c->st));
+  c->nbeta = nbeta;
+  c->betas_h.assign(betas, betas + nbeta);
+  r = build_rhs(c, nbeta, betas, true);
+  if (r) return r;
+  r = solve_cols(c, 0, 6 * c->nbody + nbeta);
+  if (r) return r;
+  CK(cudaEventRecord(c->ev[3], c->st));
+  c->rad_done = true;
+  c->dif_done = nbeta > 0;
+  r = hg_forces(c, isol, amas, bdmp, exfc);
+  if (r) return r;
+  r = copy_out(c, 0, 6 * c->nbody + nbeta, mxpot, ldm);
+  if (r) return r;
+  CK(cudaEventRecord(c->ev[4], c->st));
+  CK(cudaStreamSynchronize(c->st));
+  CK(cudaEventElapsedTime(&c->stage_ms[2], c->ev[2], c->ev[3]));
+  CK(cudaEventElapsedTime(&c->stage_ms[3], c->ev[3], c->ev[4]));
+  return check_status(c);
+}
+
+int hg_get_matrix(hg_ctx* c, int which, double* out, int ld) {
+  if (!c) return -1;
+  if (which != 0 && which != 1) return fail(c, -2, "which must be 0 (A) or 1 (S)");
+  if (!out) return fail(c, -3, "out is NULL");
+  if (ld < c->tn) return fail(c, -4, "ld %d < rows %d", ld, c->tn);
+  const int tn = c->tn, n = c->n;
+  const double2* src = nullptr;
+  DevBuf<double2> tmp;
+  if (!mixed(c)) {
+    if (which == 1) src = c->S.p;
+    else if (c->irsp == 1) src = c->A.p;
+    else if (c->keep) src = c->A64.p;
+    else return fail(c, HG_ERR_STATE, "the influence matrix was factorised in place; call hg_keep_matrices(ctx, 1) first");
+  } else {
+    if (which == 0) src = c->A64.p;
+    else {
+      CK(tmp.ensure((size_t)tn * n));
+      CK(hg::convert_c2z(c->st, (long)tn * n, c->Sf.p, tmp.p));
+      src = tmp.p;
+    }
+  }
+  CK(cudaMemcpy2DAsync(out, (size_t)ld * sizeof(double2), src, (size_t)tn * sizeof(double2), (size_t)tn * sizeof(double2), n,
+                       cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  tmp.release();
+  return 0;
+}
+
+int hg_green_points(hg_ctx* c, int npts, const double* pts, const int* flags, double* out) {
+  if (!c) return -1;
+  if (npts <= 0) return fail(c, -2, "npts must be positive");
+  if (!pts || !flags || !out) return fail(c, -3, "NULL array");
+  if (!c->freq_set) return fail(c, HG_ERR_STATE, "hg_set_frequency must come first");
+  DevBuf<double> dp, dout;
+  DevBuf<int> df;
+  CK(dp.ensure((size_t)6 * npts));
+  CK(dout.ensure((size_t)8 * npts));
+  CK(df.ensure(npts));
+  CK(cudaMemcpyAsync(dp.p, pts, (size_t)6 * npts * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(df.p, flags, (size_t)npts * sizeof(int), cudaMemcpyHostToDevice, c->st));
+  CK(hg::launch_green_points(c->st, npts, dp.p, df.p, fin_state(c), c->h < 0.0, dout.p));
+  CK(cudaMemcpyAsync(out, dout.p, (size_t)8 * npts * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  dp.release(); dout.release(); df.release();
+  return check_status(c);
+}
+
+int hg_refine_info(const hg_ctx* c, int* sweeps, double* residual) {
+  if (!c) return -1;
+  if (sweeps) *sweeps = c->sweeps;
+  if (residual) *residual = c->resid;
+  return 0;
+}
+
+int hg_stage_times(const hg_ctx* c, float* ms4) {
+  if (!c || !ms4) return -1;
+  for (int k = 0; k < 4; ++k) ms4[k] = c->stage_ms[k];
+  return 0;
+}
+
+}  // extern "C"

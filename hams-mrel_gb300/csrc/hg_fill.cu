@@ -1,0 +1,428 @@
+// Green-function influence-matrix fill (CALGREEN* + ASSB_LEFT* +
+// BODINT_LEFT, CalGreenFunc.f90:49-252 / AssbMatx.f90:53-116), the
+// single-layer matrix that feeds the right-hand sides (RBC_RIGHT /
+// DBC_RIGHT DUM, BodyIntgr.f90:83-173), the right-hand-side products
+// (ASSB_RBC*, ASSB_DBC*) and the force integration (RFORCE*/EFORCE*,
+// PotentWavForce.f90:44-221).
+//
+// Layout: field rows 0..n-1 are hull panels, n..tn-1 lid panels (IRSP=1);
+// source columns are hull panels.  A and S are column-major tn x n with
+// lda = tn, one complex entry per (field, source) pair.
+#include "hg_common.cuh"
+#include "hg_green.cuh"
+#include "hg_kernels.cuh"
+#include "hg_tma.cuh"
+
+namespace hg {
+
+// ---------------------------------------------------------------------------
+// Source-panel records (Newman frame of SingularIntgr.f90:150-179 / :372-427)
+// ---------------------------------------------------------------------------
+__global__ void k_prep_panels(int n, int ntnd, const double* __restrict__ nodes /* ntnd x 3, col-major */,
+                              const int* __restrict__ ncon /* n x 4, col-major, 1-based */,
+                              const int* __restrict__ ncn, const double* __restrict__ xyz_p /* n x 3 */,
+                              const double* __restrict__ ds, const double* __restrict__ pnsz,
+                              const double* __restrict__ dxyz_p /* n x 6 */, double* __restrict__ rec,
+                              int* status) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  double* p = rec + (size_t)j * PR_SIZE;
+  for (int k = 0; k < PR_SIZE; ++k) p[k] = 0.0;
+  const int nv = ncn[j];
+  double xv[4][3];
+  for (int c = 0; c < 4; ++c) {
+    int id = (c < nv) ? ncon[j + (size_t)c * n] : ncon[j];
+    if (id < 1 || id > ntnd) { hg_set_status(status, 64); id = 1; }
+    for (int k = 0; k < 3; ++k) xv[c][k] = nodes[(id - 1) + (size_t)k * ntnd];
+  }
+  for (int k = 0; k < 3; ++k) {
+    p[PR_XQ + k] = xyz_p[j + (size_t)k * n];
+    p[PR_N + k] = dxyz_p[j + (size_t)k * n];
+  }
+  p[PR_DS] = ds[j];
+  p[PR_FLAGD] = 50.0 * pnsz[j];
+  p[PR_NCN] = (double)nv;
+  double po[3], ui[3], uj[3], uk[3], ksi[4], eta[4];
+  if (nv == 3) {
+    double p12[3], p13[3], po3[3], po1[3], po2[3];
+    for (int k = 0; k < 3; ++k) { p12[k] = xv[1][k] - xv[0][k]; p13[k] = xv[2][k] - xv[0][k]; }
+    const double alfa = (p12[0] * p13[0] + p12[1] * p13[1] + p12[2] * p13[2]) /
+                        (p12[0] * p12[0] + p12[1] * p12[1] + p12[2] * p12[2]);
+    for (int k = 0; k < 3; ++k) po[k] = xv[0][k] + alfa * p12[k];
+    for (int k = 0; k < 3; ++k) po3[k] = xv[2][k] - po[k];
+    const double n12 = sqrt(p12[0] * p12[0] + p12[1] * p12[1] + p12[2] * p12[2]);
+    const double n3 = sqrt(po3[0] * po3[0] + po3[1] * po3[1] + po3[2] * po3[2]);
+    for (int k = 0; k < 3; ++k) { ui[k] = p12[k] / n12; uj[k] = po3[k] / n3; }
+    uk[0] = ui[1] * uj[2] - ui[2] * uj[1];
+    uk[1] = ui[2] * uj[0] - ui[0] * uj[2];
+    uk[2] = ui[0] * uj[1] - ui[1] * uj[0];
+    for (int k = 0; k < 3; ++k) { po1[k] = xv[0][k] - po[k]; po2[k] = xv[1][k] - po[k]; }
+    ksi[0] = -copysign(1.0, alfa) * sqrt(po1[0] * po1[0] + po1[1] * po1[1] + po1[2] * po1[2]);
+    eta[0] = 0.0;
+    ksi[1] = 0.0;
+    eta[1] = n3;
+    ksi[2] = sqrt(po2[0] * po2[0] + po2[1] * po2[1] + po2[2] * po2[2]);
+    eta[2] = 0.0;
+    ksi[3] = 0.0; eta[3] = 0.0;
+  } else {
+    double pov[4][3], un[3];
+    for (int k = 0; k < 3; ++k) po[k] = (xv[0][k] + xv[1][k] + xv[2][k] + xv[3][k]) / 4.0;
+    for (int c = 0; c < 4; ++c)
+      for (int k = 0; k < 3; ++k) pov[c][k] = xv[c][k] - po[k];
+    un[0] = pov[0][1] * pov[1][2] - pov[0][2] * pov[1][1];
+    un[1] = pov[0][2] * pov[1][0] - pov[0][0] * pov[1][2];
+    un[2] = pov[0][0] * pov[1][1] - pov[0][1] * pov[1][0];
+    double nn = sqrt(pov[0][0] * pov[0][0] + pov[0][1] * pov[0][1] + pov[0][2] * pov[0][2]);
+    for (int k = 0; k < 3; ++k) ui[k] = pov[0][k] / nn;
+    nn = sqrt(un[0] * un[0] + un[1] * un[1] + un[2] * un[2]);
+    for (int k = 0; k < 3; ++k) uk[k] = un[k] / nn;
+    uj[0] = uk[1] * ui[2] - uk[2] * ui[1];
+    uj[1] = uk[2] * ui[0] - uk[0] * ui[2];
+    uj[2] = uk[0] * ui[1] - uk[1] * ui[0];
+    for (int c = 0; c < 4; ++c) {
+      const double d = uk[0] * pov[c][0] + uk[1] * pov[c][1] + uk[2] * pov[c][2];
+      double pon[3];
+      for (int k = 0; k < 3; ++k) pon[k] = pov[c][k] - d * uk[k];
+      ksi[c] = ui[0] * pon[0] + ui[1] * pon[1] + ui[2] * pon[2];
+      eta[c] = uj[0] * pon[0] + uj[1] * pon[1] + uj[2] * pon[2];
+    }
+  }
+  for (int k = 0; k < 3; ++k) {
+    p[PR_PO + k] = po[k]; p[PR_UI + k] = ui[k]; p[PR_UJ + k] = uj[k]; p[PR_UK + k] = uk[k];
+  }
+  for (int e = 0; e < 4; ++e) { p[PR_KSI + e] = ksi[e]; p[PR_ETA + e] = eta[e]; }
+  for (int e = 0; e < nv; ++e) {
+    const int nx = (e + 1 == nv) ? 0 : e + 1;
+    const double a = ksi[nx] - ksi[e], b = eta[nx] - eta[e];
+    p[PR_L + e] = sqrt(a * a + b * b);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pair kernel.  CTA = FILL_ROWS field rows x FILL_COLS source columns.  The
+// source records of the tile are brought into shared memory with one bulk
+// async copy; each thread owns one field row and walks the tile's columns,
+// so every warp store of A/S is 32 consecutive complex entries of one column.
+// ---------------------------------------------------------------------------
+constexpr int FILL_ROWS = 128;
+constexpr int FILL_COLS = 16;
+
+template <bool DEEP, typename OUT>
+__global__ void __launch_bounds__(FILL_ROWS)
+k_green_fill(const double* __restrict__ rec, const double* __restrict__ fx /* ldf x 3 col-major */, int ldf, int n, int tn,
+             FinState fs, int grn_kind, OUT* __restrict__ A, OUT* __restrict__ S, long lda, int* status) {
+  __shared__ alignas(128) double tile[FILL_COLS * PR_SIZE];
+  __shared__ alignas(8) uint64_t bar;
+  const int col0 = blockIdx.y * FILL_COLS;
+  const int ncol = min(FILL_COLS, n - col0);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_expect_tx(&bar, (uint32_t)(ncol * PR_SIZE * sizeof(double)));
+    bulk_g2s(tile, rec + (size_t)col0 * PR_SIZE, (uint32_t)(ncol * PR_SIZE * sizeof(double)), &bar);
+  }
+  __syncthreads();
+  if (!mbar_wait_bounded(&bar, 0, 1L << 24)) {
+    hg_set_status(status, HG_DEV_WAIT_TIMEOUT);
+    mbar_wait_bounded(&bar, 0, 1L << 24);  // drain the copy before shared memory goes away
+    return;
+  }
+  const int i = blockIdx.x * FILL_ROWS + threadIdx.x;
+  if (i >= tn) return;
+  const double xp = fx[i], yp = fx[i + ldf], zp = fx[i + 2 * (size_t)ldf];
+  for (int jj = 0; jj < ncol; ++jj) {
+    const double* pr = tile + jj * PR_SIZE;
+    const int j = col0 + jj;
+    const double xq = pr[PR_XQ], yq = pr[PR_XQ + 1], zq = pr[PR_XQ + 2];
+    const double dist = sqrt((xp - xq) * (xp - xq) + (yp - yq) * (yp - yq) + (zp - zq) * (zp - zq));
+    const int flag = (dist <= pr[PR_FLAGD]) ? 1 : 0;
+    double sij = 0.0, d0 = 0.0, d1 = 0.0, d2 = 0.0;
+    if (flag) newman_pair(pr, xp, yp, zp, sij, d0, d1, d2);
+    double2 g[4];
+    if (DEEP) inf_green(xq, yq, zq, xp, yp, zp, fs.v, flag, g);
+    else fin_green(fs, xq, yq, zq, xp, yp, zp, flag, g);
+    if (grn_kind == 4) {
+      sij = (float)sij; d0 = (float)d0; d1 = (float)d1; d2 = (float)d2;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) g[k] = make_double2((float)g[k].x, (float)g[k].y);
+    }
+    const double ear = pr[PR_DS], n0 = pr[PR_N], n1 = pr[PR_N + 1], n2 = pr[PR_N + 2];
+    double ar, ai, sr, si;
+    if (flag) {
+      ar = (d0 + g[1].x * ear) * n0 + (d1 + g[2].x * ear) * n1 + (d2 + g[3].x * ear) * n2;
+      ai = (g[1].y * ear) * n0 + (g[2].y * ear) * n1 + (g[3].y * ear) * n2;
+      sr = sij + g[0].x * ear;
+    } else {
+      ar = (g[1].x * n0 + g[2].x * n1 + g[3].x * n2) * ear;
+      ai = (g[1].y * n0 + g[2].y * n1 + g[3].y * n2) * ear;
+      sr = g[0].x * ear;
+    }
+    si = g[0].y * ear;
+    if (i == j) ar += 2.0 * HG_PI;
+    store_c(A + i + (long)j * lda, ar, ai);
+    store_c(S + i + (long)j * lda, sr, si);
+  }
+}
+
+template <typename OUT>
+cudaError_t launch_green_fill(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
+                              const FinState& fs, bool deep, int grn_kind, OUT* A, OUT* S, long lda, int* status) {
+  dim3 grid((tn + FILL_ROWS - 1) / FILL_ROWS, (n + FILL_COLS - 1) / FILL_COLS);
+  if (deep) k_green_fill<true, OUT><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, status);
+  else k_green_fill<false, OUT><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, status);
+  return cudaGetLastError();
+}
+template cudaError_t launch_green_fill<double2>(cudaStream_t, const double*, const double*, int, int, int,
+                                                const FinState&, bool, int, double2*, double2*, long, int*);
+template cudaError_t launch_green_fill<float2>(cudaStream_t, const double*, const double*, int, int, int,
+                                               const FinState&, bool, int, float2*, float2*, long, int*);
+
+cudaError_t launch_prep_panels(cudaStream_t st, int n, int ntnd, const double* nodes, const int* ncon, const int* ncn,
+                               const double* xyz_p, const double* ds, const double* pnsz, const double* dxyz_p,
+                               double* rec, int* status) {
+  k_prep_panels<<<(n + 127) / 128, 128, 0, st>>>(n, ntnd, nodes, ncon, ncn, xyz_p, ds, pnsz, dxyz_p, rec, status);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Incident-wave weights of the diffraction RHS: w[j, b] = -(grad phi_I(x_j; beta_b) . n_j),
+// DINP (PatclVelct.f90:83-123) at the source centroid, XW = 0, AMP = 1.
+// ---------------------------------------------------------------------------
+__global__ void k_incident(int n, const double* __restrict__ xyz_p, const double* __restrict__ dxyz_p, int nbeta,
+                           const double* __restrict__ betas, double v, double wk, double w1, double h,
+                           double2* __restrict__ w) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+  if (j >= n || b >= nbeta) return;
+  double w0, wk0;
+  if (fabs(v) < SPD(1.e-8)) { w0 = SPD(1.e-20); wk0 = SPD(1.e-20); }
+  else if (fabs(v + 1.0) < SPD(1.e-8)) { w0 = SPD(1.e+20); wk0 = SPD(1.e+20); }
+  else { w0 = w1; wk0 = wk; }
+  const double x = xyz_p[j], y = xyz_p[j + n], z = xyz_p[j + 2 * (size_t)n];
+  double sb, cb;
+  sincos(betas[b], &sb, &cb);
+  const double wkx = wk0 * (x * cb + y * sb);
+  double s, c;
+  sincos(wkx, &s, &c);
+  double th, tv;
+  if (h < 0.0) { th = exp(wk0 * z); tv = th; }
+  else { const double sh = sinh(wk0 * h); th = cosh(wk0 * (z + h)) / sh; tv = sinh(wk0 * (z + h)) / sh; }
+  // DPOX = w0 th e^{i wkx} cos(beta) / i ; DPOZ = -i w0 tv e^{i wkx} / i = -w0 tv e^{i wkx}
+  const double n1 = dxyz_p[j], n2 = dxyz_p[j + n], n3 = dxyz_p[j + 2 * (size_t)n];
+  const double hx = w0 * th * (cb * n1 + sb * n2);
+  // (c + i s)/i = s - i c
+  const double dre = hx * s - w0 * tv * n3 * c;
+  const double dim = -hx * c - w0 * tv * n3 * s;
+  w[j + (size_t)b * n] = make_double2(-dre, -dim);
+}
+
+cudaError_t launch_incident(cudaStream_t st, int n, const double* xyz_p, const double* dxyz_p, int nbeta,
+                            const double* betas, double v, double wk, double w1, double h, double2* w) {
+  if (nbeta <= 0) return cudaSuccess;
+  k_incident<<<dim3((n + 127) / 128, nbeta), 128, 0, st>>>(n, xyz_p, dxyz_p, nbeta, betas, v, wk, w1, h, w);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Right-hand sides from the single-layer matrix S (tn x n):
+//   B[:, 6b+md] = sum_{j in body b} S[:, j] n_j,md        (ASSB_RBC_MULTI)
+//   B[:, 6NB+k] = sum_j S[:, j] w[j, k]                   (ASSB_DBC)
+// Grid: (row blocks, source chunks, heading groups).  Each thread owns one
+// row and writes its chunk's partial sums; k_rhs_reduce adds the chunks.
+// ---------------------------------------------------------------------------
+constexpr int RHS_ROWS = 128;
+constexpr int RHS_CHUNK = 256;
+constexpr int RHS_HG = 8;
+
+template <typename IN>
+__global__ void __launch_bounds__(RHS_ROWS)
+k_rhs_partial(int n, int tn, const IN* __restrict__ S, long lds, const double* __restrict__ dxyz_p,
+              const int* __restrict__ body_of, int nbody, int nbeta, const double2* __restrict__ w,
+              double2* __restrict__ part /* [nchunk][ncols][tn] */) {
+  const int i = blockIdx.x * RHS_ROWS + threadIdx.x;
+  const int chunk = blockIdx.y, hg0 = blockIdx.z * RHS_HG;
+  const int j0 = chunk * RHS_CHUNK, j1 = min(n, j0 + RHS_CHUNK);
+  const int ncols = 6 * nbody + nbeta;
+  if (i >= tn) return;
+  double2* pc = part + (size_t)chunk * ncols * tn;
+  const bool do_modes = (blockIdx.z == 0);
+  const int nh = max(0, min(RHS_HG, nbeta - hg0));
+  double mr[6] = {0, 0, 0, 0, 0, 0}, mi[6] = {0, 0, 0, 0, 0, 0};
+  double hr[RHS_HG], hi[RHS_HG];
+#pragma unroll
+  for (int k = 0; k < RHS_HG; ++k) { hr[k] = 0; hi[k] = 0; }
+  int cur = (j0 < j1) ? body_of[j0] : 0;
+  for (int j = j0; j < j1; ++j) {
+    const IN sv = S[i + (long)j * lds];
+    const double sr = sv.x, si = sv.y;
+    if (do_modes) {
+      const int b = body_of[j];
+      if (b != cur) {
+#pragma unroll
+        for (int md = 0; md < 6; ++md) {
+          pc[(size_t)(6 * cur + md) * tn + i] = make_double2(mr[md], mi[md]);
+          mr[md] = 0; mi[md] = 0;
+        }
+        cur = b;
+      }
+#pragma unroll
+      for (int md = 0; md < 6; ++md) {
+        const double nv = dxyz_p[j + (size_t)md * n];
+        mr[md] += sr * nv;
+        mi[md] += si * nv;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < RHS_HG; ++k) {
+      if (k < nh) {
+        const double2 ww = w[j + (size_t)(hg0 + k) * n];
+        hr[k] += sr * ww.x - si * ww.y;
+        hi[k] += sr * ww.y + si * ww.x;
+      }
+    }
+  }
+  if (do_modes && j0 < j1) {
+#pragma unroll
+    for (int md = 0; md < 6; ++md) pc[(size_t)(6 * cur + md) * tn + i] = make_double2(mr[md], mi[md]);
+  }
+#pragma unroll
+  for (int k = 0; k < RHS_HG; ++k)
+    if (k < nh) pc[(size_t)(6 * nbody + hg0 + k) * tn + i] = make_double2(hr[k], hi[k]);
+}
+
+__global__ void k_rhs_reduce(int tn, int ncols, int nchunk, const double2* __restrict__ part, double2* __restrict__ B,
+                             long ldb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+  if (i >= tn) return;
+  double r = 0, im = 0;
+  for (int k = 0; k < nchunk; ++k) {
+    const double2 v = part[((size_t)k * ncols + c) * tn + i];
+    r += v.x;
+    im += v.y;
+  }
+  B[i + (long)c * ldb] = make_double2(r, im);
+}
+
+size_t rhs_work_bytes(int n, int tn, int nbody, int nbeta) {
+  const int nchunk = (n + RHS_CHUNK - 1) / RHS_CHUNK;
+  return (size_t)nchunk * (6 * nbody + nbeta) * tn * sizeof(double2);
+}
+
+template <typename IN>
+cudaError_t launch_rhs(cudaStream_t st, int n, int tn, const IN* S, long lds, const double* dxyz_p, const int* body_of,
+                       int nbody, int nbeta, const double2* w, double2* part, double2* B, long ldb) {
+  const int nchunk = (n + RHS_CHUNK - 1) / RHS_CHUNK;
+  const int ncols = 6 * nbody + nbeta;
+  cudaError_t e = cudaMemsetAsync(part, 0, rhs_work_bytes(n, tn, nbody, nbeta), st);
+  if (e != cudaSuccess) return e;
+  const int ngroups = max(1, (nbeta + RHS_HG - 1) / RHS_HG);
+  k_rhs_partial<IN><<<dim3((tn + RHS_ROWS - 1) / RHS_ROWS, nchunk, ngroups), RHS_ROWS, 0, st>>>(
+      n, tn, S, lds, dxyz_p, body_of, nbody, nbeta, w, part);
+  k_rhs_reduce<<<dim3((tn + 255) / 256, ncols), 256, 0, st>>>(tn, ncols, nchunk, part, B, ldb);
+  return cudaGetLastError();
+}
+template cudaError_t launch_rhs<double2>(cudaStream_t, int, int, const double2*, long, const double*, const int*, int,
+                                         int, const double2*, double2*, double2*, long);
+template cudaError_t launch_rhs<float2>(cudaStream_t, int, int, const float2*, long, const double*, const int*, int,
+                                        int, const double2*, double2*, double2*, long);
+
+// ---------------------------------------------------------------------------
+// Forces.  One CTA per (body m, potential column c): six direction sums over
+// body m's panels, then
+//   c < 6NB : AMAS[6m+k][c] = sum Im(i rho phi ds n_k) ,  BDMP = -sum Re(i rho w phi ds n_k)
+//   c >= 6NB: EXFC[c-6NB][6m+k] = i w rho sum (phi [+ phi_I]) ds n_k
+// (RFORCE_MULTI / EFORCE_MULTI, PotentWavForceMulti.f90:45-226)
+// ---------------------------------------------------------------------------
+__global__ void k_forces(int n, const double2* __restrict__ X, long ldx, const double* __restrict__ xyz_p,
+                         const double* __restrict__ ds, const double* __restrict__ dxyz_p,
+                         const int* __restrict__ body_start, const int* __restrict__ body_end, int nbody, int nbeta,
+                         const double* __restrict__ betas, double v, double wk, double w1, double h, int isol,
+                         double rho, double g, double* __restrict__ amas, double* __restrict__ bdmp,
+                         double2* __restrict__ exfc) {
+  const int m = blockIdx.x, c = blockIdx.y;
+  const int nd = 6 * nbody;
+  const bool rad = c < nd;
+  const int i0 = body_start[m], i1 = body_end[m];
+  double sr[6] = {0, 0, 0, 0, 0, 0}, si[6] = {0, 0, 0, 0, 0, 0};
+  double w0 = w1, wk0 = wk;
+  if (fabs(v) < SPD(1.e-8)) { w0 = SPD(1.e-20); wk0 = SPD(1.e-20); }
+  else if (fabs(v + 1.0) < SPD(1.e-8)) { w0 = SPD(1.e+20); wk0 = SPD(1.e+20); }
+  double sb = 0, cb = 1;
+  if (!rad) sincos(betas[c - nd], &sb, &cb);
+  for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    double2 p = X[i + (long)c * ldx];
+    if (!rad && isol == 1) {
+      // VINP (PatclVelct.f90:42-76), deep if H < 0 or H > 500
+      const double x = xyz_p[i], y = xyz_p[i + n], z = xyz_p[i + 2 * (size_t)n];
+      const double wkx = wk0 * (x * cb + y * sb);
+      double s, co;
+      sincos(wkx, &s, &co);
+      double amp;
+      if (h < 0.0 || h > 500.0) amp = -g / w0 * exp(wk0 * z);        // VINP = -i g/w0 e^{kz} e^{i kx} / i
+      else amp = (-w0 / (wk0 * sinh(wk0 * h))) * cosh(wk0 * (z + h));  // VINP = i dum cosh e^{ikx} / i
+      p.x += amp * co;
+      p.y += amp * s;
+    }
+    const double a = ds[i];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const double nk = dxyz_p[i + (size_t)k * n];
+      sr[k] += p.x * a * nk;
+      si[k] += p.y * a * nk;
+    }
+  }
+  __shared__ double red[2][6][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    for (int off = 16; off > 0; off >>= 1) {
+      sr[k] += __shfl_down_sync(0xffffffffu, sr[k], off);
+      si[k] += __shfl_down_sync(0xffffffffu, si[k], off);
+    }
+    if (lane == 0) { red[0][k][warp] = sr[k]; red[1][k][warp] = si[k]; }
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    const int k = threadIdx.x;
+    double tr = 0, ti = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { tr += red[0][k][w]; ti += red[1][k][w]; }
+    if (rad) {
+      // i rho (tr + i ti) = rho (-ti + i tr)
+      amas[(size_t)(6 * m + k) * nd + c] = rho * tr;
+      bdmp[(size_t)(6 * m + k) * nd + c] = rho * w1 * ti;
+    } else {
+      // i w rho (tr + i ti) = w rho (-ti + i tr)
+      exfc[(size_t)(c - nd) * nd + 6 * m + k] = make_double2(-w1 * rho * ti, w1 * rho * tr);
+    }
+  }
+}
+
+cudaError_t launch_forces(cudaStream_t st, int n, const double2* X, long ldx, const double* xyz_p, const double* ds,
+                          const double* dxyz_p, const int* body_start, const int* body_end, int nbody, int nbeta,
+                          const double* betas, double v, double wk, double w1, double h, int isol, double rho,
+                          double g, double* amas, double* bdmp, double2* exfc) {
+  k_forces<<<dim3(nbody, 6 * nbody + nbeta), 256, 0, st>>>(n, X, ldx, xyz_p, ds, dxyz_p, body_start, body_end, nbody,
+                                                           nbeta, betas, v, wk, w1, h, isol, rho, g, amas, bdmp, exfc);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Green function at arbitrary points (kernel-level parity tests of every
+// finite-depth region): pts[k] = (xq,yq,zq,xp,yp,zp), out[k] = 4 complex.
+// ---------------------------------------------------------------------------
+__global__ void k_green_points(int npts, const double* __restrict__ pts, const int* __restrict__ flags, FinState fs,
+                               int deep, double* __restrict__ out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= npts) return;
+  const double* p = pts + 6 * (size_t)k;
+  double2 g[4];
+  if (deep) inf_green(p[0], p[1], p[2], p[3], p[4], p[5], fs.v, flags[k], g);
+  else fin_green(fs, p[0], p[1], p[2], p[3], p[4], p[5], flags[k], g);
+  for (int q = 0; q < 4; ++q) { out[8 * (size_t)k + 2 * q] = g[q].x; out[8 * (size_t)k + 2 * q + 1] = g[q].y; }
+}
+
+cudaError_t launch_green_points(cudaStream_t st, int npts, const double* pts, const int* flags, const FinState& fs,
+                                bool deep, double* out) {
+  k_green_points<<<(npts + 63) / 64, 64, 0, st>>>(npts, pts, flags, fs, deep ? 1 : 0, out);
+  return cudaGetLastError();
+}
+
+}  // namespace hg

@@ -1,0 +1,38 @@
+// Host-callable launchers of the fill / right-hand-side / force kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include "hg_common.cuh"
+
+namespace hg {
+
+struct FinState;
+
+__device__ __forceinline__ void store_c(double2* p, double re, double im) { *p = make_double2(re, im); }
+__device__ __forceinline__ void store_c(float2* p, double re, double im) { *p = make_float2((float)re, (float)im); }
+
+cudaError_t launch_prep_panels(cudaStream_t st, int n, int ntnd, const double* nodes, const int* ncon, const int* ncn,
+                               const double* xyz_p, const double* ds, const double* pnsz, const double* dxyz_p,
+                               double* rec, int* status);
+
+template <typename OUT>
+cudaError_t launch_green_fill(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
+                              const FinState& fs, bool deep, int grn_kind, OUT* A, OUT* S, long lda, int* status);
+
+cudaError_t launch_incident(cudaStream_t st, int n, const double* xyz_p, const double* dxyz_p, int nbeta,
+                            const double* betas, double v, double wk, double w1, double h, double2* w);
+
+size_t rhs_work_bytes(int n, int tn, int nbody, int nbeta);
+
+template <typename IN>
+cudaError_t launch_rhs(cudaStream_t st, int n, int tn, const IN* S, long lds, const double* dxyz_p, const int* body_of,
+                       int nbody, int nbeta, const double2* w, double2* part, double2* B, long ldb);
+
+cudaError_t launch_forces(cudaStream_t st, int n, const double2* X, long ldx, const double* xyz_p, const double* ds,
+                          const double* dxyz_p, const int* body_start, const int* body_end, int nbody, int nbeta,
+                          const double* betas, double v, double wk, double w1, double h, int isol, double rho,
+                          double g, double* amas, double* bdmp, double2* exfc);
+
+cudaError_t launch_green_points(cudaStream_t st, int npts, const double* pts, const int* flags, const FinState& fs,
+                                bool deep, double* out);
+
+}  // namespace hg

@@ -1,0 +1,403 @@
+// Blocked complex LU with partial pivoting and triangular solves.
+//
+// getrf: right-looking, panel width NB.  Per panel: a one-CTA panel
+// factorisation (pivot = max |re|+|im| as LAPACK's IZAMAX, row swaps,
+// reciprocal scaling, rank-1 updates), the row interchanges applied to the
+// columns outside the panel, a unit-lower triangular solve for the U12 block
+// and the trailing update A22 -= L21 U12, the only O(n^3) step.
+#include <climits>
+#include "hg_linalg.cuh"
+
+namespace hg {
+
+template <typename R> struct ops;
+template <> struct ops<double> {
+  typedef double2 T;
+  static __device__ __forceinline__ T mk(double a, double b) { return make_double2(a, b); }
+};
+template <> struct ops<float> {
+  typedef float2 T;
+  static __device__ __forceinline__ T mk(float a, float b) { return make_float2(a, b); }
+};
+
+template <typename T> __device__ __forceinline__ T cmul(T a, T b) {
+  T r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+template <typename T> __device__ __forceinline__ T csub(T a, T b) { T r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename T> __device__ __forceinline__ T crecip(T a) {
+  // 1/a with Smith's scaling
+  T r;
+  if (fabs((double)a.x) >= fabs((double)a.y)) {
+    auto q = a.y / a.x, d = a.x + a.y * q;
+    r.x = 1 / d; r.y = -q / d;
+  } else {
+    auto q = a.x / a.y, d = a.y + a.x * q;
+    r.x = q / d; r.y = -1 / d;
+  }
+  return r;
+}
+template <typename T> __device__ __forceinline__ T cdiv_(T a, T b) { return cmul(a, crecip(b)); }
+
+// ------------------------------------------------------------------------
+// GEMM
+// ------------------------------------------------------------------------
+template <typename R, int BM, int BN, int BK, int TM, int TN, bool TA>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN))
+k_gemm(int m, int n, int k, typename cx<R>::T alpha, const typename cx<R>::T* __restrict__ A, long lda,
+       const typename cx<R>::T* __restrict__ B, long ldb, typename cx<R>::T beta,
+       typename cx<R>::T* __restrict__ C, long ldc) {
+  typedef typename cx<R>::T T;
+  constexpr int TX = BM / TM, TY = BN / TN, NT = TX * TY;
+  __shared__ R as_re[BK][BM], as_im[BK][BM], bs_re[BK][BN], bs_im[BK][BN];
+  const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  R acr[TM][TN], aci[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) { acr[i][j] = 0; aci[i][j] = 0; }
+
+  for (int kk = 0; kk < k; kk += BK) {
+#pragma unroll
+    for (int e = tid; e < BM * BK; e += NT) {
+      int i, l;
+      if (!TA) { i = e % BM; l = e / BM; } else { l = e % BK; i = e / BK; }
+      const int gm = m0 + i, gk = kk + l;
+      T v;
+      v.x = 0; v.y = 0;
+      if (gm < m && gk < k) v = TA ? A[gk + (long)gm * lda] : A[gm + (long)gk * lda];
+      as_re[l][i] = v.x; as_im[l][i] = v.y;
+    }
+#pragma unroll
+    for (int e = tid; e < BN * BK; e += NT) {
+      const int l = e % BK, j = e / BK, gk = kk + l, gn = n0 + j;
+      T v;
+      v.x = 0; v.y = 0;
+      if (gn < n && gk < k) v = B[gk + (long)gn * ldb];
+      bs_re[l][j] = v.x; bs_im[l][j] = v.y;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int l = 0; l < BK; ++l) {
+      R ar[TM], ai[TM], br[TN], bi[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) { ar[i] = as_re[l][tx + i * TX]; ai[i] = as_im[l][tx + i * TX]; }
+#pragma unroll
+      for (int j = 0; j < TN; ++j) { br[j] = bs_re[l][ty + j * TY]; bi[j] = bs_im[l][ty + j * TY]; }
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) {
+          acr[i][j] = fma(ar[i], br[j], acr[i][j]);
+          acr[i][j] = fma(-ai[i], bi[j], acr[i][j]);
+          aci[i][j] = fma(ar[i], bi[j], aci[i][j]);
+          aci[i][j] = fma(ai[i], br[j], aci[i][j]);
+        }
+    }
+    __syncthreads();
+  }
+  const bool zb = (beta.x == 0 && beta.y == 0);
+#pragma unroll
+  for (int j = 0; j < TN; ++j) {
+    const int gn = n0 + ty + j * TY;
+    if (gn >= n) continue;
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+      const int gm = m0 + tx + i * TX;
+      if (gm >= m) continue;
+      T r;
+      r.x = alpha.x * acr[i][j] - alpha.y * aci[i][j];
+      r.y = alpha.x * aci[i][j] + alpha.y * acr[i][j];
+      T* c = C + gm + (long)gn * ldc;
+      if (!zb) {
+        const T o = *c;
+        r.x += beta.x * o.x - beta.y * o.y;
+        r.y += beta.x * o.y + beta.y * o.x;
+      }
+      *c = r;
+    }
+  }
+}
+
+template <typename R, int BM, int BN, int BK, int TM, int TN>
+static cudaError_t launch_gemm(cudaStream_t st, bool transa, int m, int n, int k, typename cx<R>::T alpha,
+                               const typename cx<R>::T* A, long lda, const typename cx<R>::T* B, long ldb,
+                               typename cx<R>::T beta, typename cx<R>::T* C, long ldc) {
+  if (m <= 0 || n <= 0) return cudaSuccess;
+  dim3 grid((m + BM - 1) / BM, (n + BN - 1) / BN);
+  const int nt = (BM / TM) * (BN / TN);
+  if (transa) k_gemm<R, BM, BN, BK, TM, TN, true><<<grid, nt, 0, st>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  else k_gemm<R, BM, BN, BK, TM, TN, false><<<grid, nt, 0, st>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  return cudaGetLastError();
+}
+
+template <>
+cudaError_t gemm<double>(cudaStream_t st, bool transa, int m, int n, int k, double2 alpha, const double2* A,
+                         long lda, const double2* B, long ldb, double2 beta, double2* C, long ldc) {
+  if (n <= 32) return launch_gemm<double, 64, 32, 8, 4, 2>(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  return launch_gemm<double, 64, 64, 8, 4, 4>(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+template <>
+cudaError_t gemm<float>(cudaStream_t st, bool transa, int m, int n, int k, float2 alpha, const float2* A,
+                        long lda, const float2* B, long ldb, float2 beta, float2* C, long ldc) {
+  if (n <= 64) return launch_gemm<float, 64, 32, 8, 4, 2>(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  return launch_gemm<float, 128, 128, 8, 8, 8>(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+
+// ------------------------------------------------------------------------
+// Panel factorisation: one CTA, rows [0, m) x columns [0, jb) of P.
+// ------------------------------------------------------------------------
+constexpr int kNB = 32;
+constexpr int kPanelThreads = 1024;
+
+template <typename R>
+__global__ void __launch_bounds__(kPanelThreads)
+k_getf2(typename cx<R>::T* P, long lda, int m, int jb, int* ipiv, int k0, int* info) {
+  typedef typename cx<R>::T T;
+  __shared__ R s_v[32];
+  __shared__ int s_i[32];
+  __shared__ T s_row[kNB];
+  __shared__ int s_p;
+  __shared__ R s_max;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int jj = 0; jj < jb; ++jj) {
+    R best = -1;
+    int bidx = INT_MAX;
+    for (int r = jj + tid; r < m; r += kPanelThreads) {
+      const T a = P[r + (long)jj * lda];
+      const R v = fabs(a.x) + fabs(a.y);
+      if (v > best) { best = v; bidx = r; }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const R ov = __shfl_down_sync(0xffffffffu, best, off);
+      const int oi = __shfl_down_sync(0xffffffffu, bidx, off);
+      if (ov > best || (ov == best && oi < bidx)) { best = ov; bidx = oi; }
+    }
+    if (lane == 0) { s_v[warp] = best; s_i[warp] = bidx; }
+    __syncthreads();
+    if (warp == 0) {
+      best = (lane < kPanelThreads / 32) ? s_v[lane] : (R)-1;
+      bidx = (lane < kPanelThreads / 32) ? s_i[lane] : INT_MAX;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const R ov = __shfl_down_sync(0xffffffffu, best, off);
+        const int oi = __shfl_down_sync(0xffffffffu, bidx, off);
+        if (ov > best || (ov == best && oi < bidx)) { best = ov; bidx = oi; }
+      }
+      if (lane == 0) {
+        if (bidx == INT_MAX) bidx = jj;
+        s_p = bidx;
+        s_max = best;
+        ipiv[k0 + jj] = k0 + bidx + 1;
+        if (!(best > 0) && *info == 0) *info = k0 + jj + 1;
+      }
+    }
+    __syncthreads();
+    const int p = s_p;
+    if (s_max > 0) {
+      if (p != jj && tid < jb) {
+        const T t = P[jj + (long)tid * lda];
+        P[jj + (long)tid * lda] = P[p + (long)tid * lda];
+        P[p + (long)tid * lda] = t;
+      }
+      __syncthreads();
+      if (tid < jb) s_row[tid] = P[jj + (long)tid * lda];
+      __syncthreads();
+      const T rp = crecip(s_row[jj]);
+      for (int r = jj + 1 + tid; r < m; r += kPanelThreads) {
+        const T l = cmul(P[r + (long)jj * lda], rp);
+        P[r + (long)jj * lda] = l;
+        for (int c = jj + 1; c < jb; ++c) {
+          T* a = P + r + (long)c * lda;
+          *a = csub(*a, cmul(l, s_row[c]));
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Apply the pivots ipiv[r0..r1) (1-based global rows) to every column of A
+// outside [skip0, skip1).
+template <typename T>
+__global__ void k_laswp(T* A, long lda, int ncols, const int* ipiv, int r0, int r1, int skip0, int skip1) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncols || (c >= skip0 && c < skip1)) return;
+  T* col = A + (long)c * lda;
+  for (int r = r0; r < r1; ++r) {
+    const int p = ipiv[r] - 1;
+    if (p != r) {
+      const T t = col[r];
+      col[r] = col[p];
+      col[p] = t;
+    }
+  }
+}
+
+// X = L^{-1} X for the unit-lower jb x jb block L (lda) and ncols columns of X (ldx).
+template <typename T>
+__global__ void k_trsm_lower_unit(const T* L, long lda, int jb, T* X, long ldx, int ncols) {
+  __shared__ T sl[kNB][kNB + 1];
+  for (int e = threadIdx.x; e < jb * jb; e += blockDim.x) {
+    const int r = e % jb, c = e / jb;
+    sl[r][c] = L[r + (long)c * lda];
+  }
+  __syncthreads();
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncols) return;
+  T x[kNB];
+  T* xc = X + (long)col * ldx;
+#pragma unroll
+  for (int r = 0; r < kNB; ++r)
+    if (r < jb) x[r] = xc[r];
+#pragma unroll
+  for (int r = 0; r < kNB; ++r) {
+    if (r >= jb) break;
+#pragma unroll
+    for (int c = 0; c < kNB; ++c)
+      if (c < r) x[r] = csub(x[r], cmul(sl[r][c], x[c]));
+  }
+#pragma unroll
+  for (int r = 0; r < kNB; ++r)
+    if (r < jb) xc[r] = x[r];
+}
+
+// X = U^{-1} X for the non-unit upper jb x jb block U.
+template <typename T>
+__global__ void k_trsm_upper(const T* U, long lda, int jb, T* X, long ldx, int ncols) {
+  __shared__ T su[kNB][kNB + 1];
+  __shared__ T sd[kNB];
+  for (int e = threadIdx.x; e < jb * jb; e += blockDim.x) {
+    const int r = e % jb, c = e / jb;
+    su[r][c] = U[r + (long)c * lda];
+  }
+  __syncthreads();
+  if (threadIdx.x < jb) sd[threadIdx.x] = crecip(su[threadIdx.x][threadIdx.x]);
+  __syncthreads();
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncols) return;
+  T x[kNB];
+  T* xc = X + (long)col * ldx;
+#pragma unroll
+  for (int r = 0; r < kNB; ++r)
+    if (r < jb) x[r] = xc[r];
+#pragma unroll
+  for (int rr = kNB - 1; rr >= 0; --rr) {
+    if (rr >= jb) continue;
+#pragma unroll
+    for (int c = 0; c < kNB; ++c)
+      if (c > rr && c < jb) x[rr] = csub(x[rr], cmul(su[rr][c], x[c]));
+    x[rr] = cmul(x[rr], sd[rr]);
+  }
+#pragma unroll
+  for (int r = 0; r < kNB; ++r)
+    if (r < jb) xc[r] = x[r];
+}
+
+size_t lu_work_bytes(int) { return 0; }
+
+template <typename R>
+cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* ipiv, int* info, void*) {
+  typedef typename cx<R>::T T;
+  cudaError_t e = cudaMemsetAsync(info, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  T mone, one;
+  mone.x = -1; mone.y = 0; one.x = 1; one.y = 0;
+  for (int k = 0; k < n; k += kNB) {
+    const int jb = (n - k < kNB) ? n - k : kNB;
+    k_getf2<R><<<1, kPanelThreads, 0, st>>>(A + k + (long)k * lda, lda, n - k, jb, ipiv, k, info);
+    k_laswp<T><<<(n + 127) / 128, 128, 0, st>>>(A, lda, n, ipiv, k, k + jb, k, k + jb);
+    const int rest = n - k - jb;
+    if (rest > 0) {
+      k_trsm_lower_unit<T><<<(rest + 127) / 128, 128, 0, st>>>(A + k + (long)k * lda, lda, jb,
+                                                                 A + k + (long)(k + jb) * lda, lda, rest);
+      e = gemm<R>(st, false, rest, rest, jb, mone, A + (k + jb) + (long)k * lda, lda, A + k + (long)(k + jb) * lda,
+                  lda, one, A + (k + jb) + (long)(k + jb) * lda, lda);
+      if (e != cudaSuccess) return e;
+    }
+  }
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t getrs(cudaStream_t st, int n, int nrhs, const typename cx<R>::T* LU, long lda, const int* ipiv,
+                  typename cx<R>::T* B, long ldb) {
+  typedef typename cx<R>::T T;
+  T mone, one;
+  mone.x = -1; mone.y = 0; one.x = 1; one.y = 0;
+  k_laswp<T><<<(nrhs + 127) / 128, 128, 0, st>>>(B, ldb, nrhs, ipiv, 0, n, 0, 0);
+  for (int k = 0; k < n; k += kNB) {
+    const int jb = (n - k < kNB) ? n - k : kNB;
+    k_trsm_lower_unit<T><<<(nrhs + 127) / 128, 128, 0, st>>>(LU + k + (long)k * lda, lda, jb, B + k, ldb, nrhs);
+    const int rest = n - k - jb;
+    if (rest > 0) {
+      cudaError_t e = gemm<R>(st, false, rest, nrhs, jb, mone, LU + (k + jb) + (long)k * lda, lda, B + k, ldb, one,
+                              B + k + jb, ldb);
+      if (e != cudaSuccess) return e;
+    }
+  }
+  const int last = ((n - 1) / kNB) * kNB;
+  for (int k = last; k >= 0; k -= kNB) {
+    const int jb = (n - k < kNB) ? n - k : kNB;
+    k_trsm_upper<T><<<(nrhs + 127) / 128, 128, 0, st>>>(LU + k + (long)k * lda, lda, jb, B + k, ldb, nrhs);
+    if (k > 0) {
+      cudaError_t e = gemm<R>(st, false, k, nrhs, jb, mone, LU + (long)k * lda, lda, B + k, ldb, one, B, ldb);
+      if (e != cudaSuccess) return e;
+    }
+  }
+  return cudaGetLastError();
+}
+
+template cudaError_t getrf<double>(cudaStream_t, int, double2*, long, int*, int*, void*);
+template cudaError_t getrf<float>(cudaStream_t, int, float2*, long, int*, int*, void*);
+template cudaError_t getrs<double>(cudaStream_t, int, int, const double2*, long, const int*, double2*, long);
+template cudaError_t getrs<float>(cudaStream_t, int, int, const float2*, long, const int*, float2*, long);
+
+// ------------------------------------------------------------------------
+// conversions
+// ------------------------------------------------------------------------
+__global__ void k_z2c(long count, const double2* s, float2* d) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < count; i += (long)gridDim.x * blockDim.x)
+    d[i] = make_float2((float)s[i].x, (float)s[i].y);
+}
+__global__ void k_c2z(long count, const float2* s, double2* d) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < count; i += (long)gridDim.x * blockDim.x)
+    d[i] = make_double2(s[i].x, s[i].y);
+}
+__global__ void k_z2c_2d(int rows, int cols, const double2* s, long lds, float2* d, long ldd) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+  if (r < rows) {
+    const double2 v = s[r + (long)c * lds];
+    d[r + (long)c * ldd] = make_float2((float)v.x, (float)v.y);
+  }
+}
+__global__ void k_add_c2z_2d(int rows, int cols, const float2* s, long lds, double2* d, long ldd) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+  if (r < rows) {
+    const float2 v = s[r + (long)c * lds];
+    double2* o = d + r + (long)c * ldd;
+    o->x += v.x;
+    o->y += v.y;
+  }
+}
+cudaError_t convert_z2c(cudaStream_t st, long count, const double2* src, float2* dst) {
+  k_z2c<<<1216, 256, 0, st>>>(count, src, dst);
+  return cudaGetLastError();
+}
+cudaError_t convert_c2z(cudaStream_t st, long count, const float2* src, double2* dst) {
+  k_c2z<<<1216, 256, 0, st>>>(count, src, dst);
+  return cudaGetLastError();
+}
+cudaError_t convert_z2c_2d(cudaStream_t st, int rows, int cols, const double2* src, long lds, float2* dst, long ldd) {
+  if (rows <= 0 || cols <= 0) return cudaSuccess;
+  k_z2c_2d<<<dim3((rows + 255) / 256, cols), 256, 0, st>>>(rows, cols, src, lds, dst, ldd);
+  return cudaGetLastError();
+}
+cudaError_t add_c2z_2d(cudaStream_t st, int rows, int cols, const float2* src, long lds, double2* dst, long ldd) {
+  if (rows <= 0 || cols <= 0) return cudaSuccess;
+  k_add_c2z_2d<<<dim3((rows + 255) / 256, cols), 256, 0, st>>>(rows, cols, src, lds, dst, ldd);
+  return cudaGetLastError();
+}
+
+}  // namespace hg

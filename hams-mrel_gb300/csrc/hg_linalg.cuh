@@ -1,0 +1,45 @@
+// Dense complex linear algebra for the per-frequency solve: blocked
+// right-looking LU with partial pivoting (the ZGETRF/CGETRF of
+// AssbMatx.f90:111) and the triangular solves of ZGETRS (AssbMatx.f90:277),
+// in complex128 (plain form) and complex64 (mixed form).
+#pragma once
+#include <cuda_runtime.h>
+#include "hg_common.cuh"
+
+namespace hg {
+
+template <typename R> struct cx;
+template <> struct cx<double> { typedef double2 T; };
+template <> struct cx<float> { typedef float2 T; };
+
+// C = alpha * op(A) * B + beta * C, column-major, op(A) = A or A^T (no
+// conjugation: the irregular-frequency normal equations use A^T A,
+// AssbMatx_irr.f90:151-169).  M x N result, inner dimension K.
+template <typename R>
+cudaError_t gemm(cudaStream_t st, bool transa, int m, int n, int k, typename cx<R>::T alpha,
+                 const typename cx<R>::T* A, long lda, const typename cx<R>::T* B, long ldb,
+                 typename cx<R>::T beta, typename cx<R>::T* C, long ldc);
+
+// In-place LU with partial pivoting of the n x n matrix A (lda).  ipiv is a
+// device array of n 1-based pivot rows, LAPACK style.  info (device int) is
+// set to the first zero pivot (1-based) or left at 0.  work is a device
+// scratch of at least lu_work_bytes(n) bytes.
+template <typename R>
+cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* ipiv, int* info, void* work);
+
+// Solve A X = B with the factors of getrf; B is n x nrhs (ldb), overwritten.
+template <typename R>
+cudaError_t getrs(cudaStream_t st, int n, int nrhs, const typename cx<R>::T* LU, long lda, const int* ipiv,
+                  typename cx<R>::T* B, long ldb);
+
+size_t lu_work_bytes(int n);
+
+// Elementwise conversions between complex128 and complex64 buffers.
+cudaError_t convert_z2c(cudaStream_t st, long count, const double2* src, float2* dst);
+cudaError_t convert_c2z(cudaStream_t st, long count, const float2* src, double2* dst);
+// 2D (column-major) versions with leading dimensions.
+cudaError_t convert_z2c_2d(cudaStream_t st, int rows, int cols, const double2* src, long lds, float2* dst,
+                           long ldd);
+cudaError_t add_c2z_2d(cudaStream_t st, int rows, int cols, const float2* src, long lds, double2* dst, long ldd);
+
+}  // namespace hg

@@ -1,0 +1,251 @@
+"""ctypes binding of libhamsgpu.so (the C ABI declared in include/hamsgpu.h).
+
+This is the binding a Python caller (tests, bench.py, a serving loop) uses;
+the Fortran driver binds the same symbols through ISO_C_BINDING.  It loads
+only the in-tree CUDA library and raises if that library or a GPU is
+missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+HG_PREC_FP64 = 0
+HG_PREC_MIXED = 1
+
+# Every symbol include/hamsgpu.h declares (checked by the CPU test suite).
+EXPORTS = [
+    "hg_default_opts", "hg_create", "hg_destroy", "hg_last_error", "hg_set_mesh", "hg_set_frequency",
+    "hg_fill_factor", "hg_solve_radiation", "hg_solve_all_headings", "hg_solve_diffraction", "hg_forces",
+    "hg_solve_frequency", "hg_keep_matrices", "hg_get_matrix", "hg_green_points", "hg_refine_info",
+    "hg_stage_times", "hg_dispersion", "hg_wave_properties", "hg_panel_geometry",
+]
+
+
+class HgOpts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("precision", ctypes.c_int), ("grn_kind", ctypes.c_int),
+                ("max_refine", ctypes.c_int), ("refine_tol", ctypes.c_double), ("rho", ctypes.c_double),
+                ("g", ctypes.c_double)]
+
+
+_LIB = None
+
+
+def library_path() -> str:
+    return os.path.join(HERE, "_build", "libhamsgpu.so")
+
+
+def load(build_if_missing: bool = True):
+    """Load libhamsgpu.so (building it with nvcc first if needed)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if build_if_missing:
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("hams_build", os.path.join(HERE, "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        path = mod.build()
+    if not os.path.exists(path):
+        raise RuntimeError(f"libhamsgpu.so is not built ({path}); run build() first")
+    L = ctypes.CDLL(path)
+    P = ctypes.POINTER
+    c_int, c_double, c_void_p = ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+    L.hg_default_opts.argtypes = [P(HgOpts)]
+    L.hg_default_opts.restype = None
+    L.hg_create.argtypes = [P(c_void_p), P(HgOpts)]
+    L.hg_destroy.argtypes = [c_void_p]
+    L.hg_destroy.restype = None
+    L.hg_last_error.argtypes = [c_void_p]
+    L.hg_last_error.restype = ctypes.c_char_p
+    L.hg_set_mesh.argtypes = [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                              c_void_p, c_int, c_void_p, c_int, c_void_p]
+    L.hg_set_frequency.argtypes = [c_void_p, c_double, c_double, c_double, c_double, c_void_p, c_int]
+    L.hg_fill_factor.argtypes = [c_void_p, c_int]
+    L.hg_solve_radiation.argtypes = [c_void_p, c_void_p, c_int]
+    L.hg_solve_all_headings.argtypes = [c_void_p, c_void_p, c_int, c_void_p, c_int]
+    L.hg_solve_diffraction.argtypes = [c_void_p, c_double, c_void_p]
+    L.hg_forces.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p]
+    L.hg_solve_frequency.argtypes = [c_void_p, c_double, c_double, c_double, c_double, c_void_p, c_int, c_int,
+                                     c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int]
+    L.hg_keep_matrices.argtypes = [c_void_p, c_int]
+    L.hg_get_matrix.argtypes = [c_void_p, c_int, c_void_p, c_int]
+    L.hg_green_points.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p]
+    L.hg_refine_info.argtypes = [c_void_p, P(c_int), P(c_double)]
+    L.hg_stage_times.argtypes = [c_void_p, P(ctypes.c_float)]
+    L.hg_dispersion.argtypes = [c_double, c_double, c_int, c_void_p]
+    L.hg_wave_properties.argtypes = [c_int, c_double, c_double, c_int, P(c_double), P(c_double), P(c_double),
+                                     c_void_p]
+    L.hg_panel_geometry.argtypes = [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                    c_void_p, c_void_p]
+    _LIB = L
+    return L
+
+
+NK = 200
+
+
+def wave_properties(inft, value, h, nk=NK):
+    """CalWaveProperts through the library: returns (v, wk, w1, wvn or None)."""
+    L = load()
+    v, wk, w1 = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    wvn = np.zeros(nk) if h > 0 else None
+    rc = L.hg_wave_properties(int(inft), float(value), float(h), nk, ctypes.byref(v), ctypes.byref(wk),
+                              ctypes.byref(w1), _ptr(wvn))
+    if rc != 0:
+        raise HamsGpuError(rc, "hg_wave_properties failed")
+    return v.value, wk.value, w1.value, wvn
+
+
+def panel_geometry(nodes, ncon, ncn, xr):
+    """CalNormals geometry through the library; ncon 1-based (n,4)."""
+    L = load()
+    nodes_f = np.asfortranarray(nodes, dtype=np.float64)
+    ncon_f = np.asfortranarray(ncon, dtype=np.int32)
+    ncn_c = np.ascontiguousarray(ncn, dtype=np.int32)
+    n = len(ncn_c)
+    xyz = np.zeros((n, 3), order="F"); ds = np.zeros(n); pn = np.zeros(n); dx = np.zeros((n, 6), order="F")
+    xr_c = np.ascontiguousarray(xr, dtype=np.float64)
+    rc = L.hg_panel_geometry(n, len(nodes_f), _ptr(nodes_f), _ptr(ncon_f), _ptr(ncn_c), _ptr(xr_c), _ptr(xyz),
+                             _ptr(ds), _ptr(pn), _ptr(dx))
+    if rc != 0:
+        raise HamsGpuError(rc, "hg_panel_geometry failed")
+    return xyz, ds, pn, dx
+
+
+class HamsGpuError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"hamsgpu error {code}: {msg}")
+        self.code = code
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+class Solver:
+    """One library context (device buffers, stream, factorisation)."""
+
+    def __init__(self, precision: int = HG_PREC_FP64, device: int = 0, grn_kind: int = 8,
+                 max_refine: int = 10, refine_tol: float = 1e-12, rho: float = 1000.0, g: float = 9.80665):
+        self.L = load()
+        opts = HgOpts()
+        self.L.hg_default_opts(ctypes.byref(opts))
+        opts.device, opts.precision, opts.grn_kind = device, precision, grn_kind
+        opts.max_refine, opts.refine_tol, opts.rho, opts.g = max_refine, refine_tol, rho, g
+        h = ctypes.c_void_p()
+        rc = self.L.hg_create(ctypes.byref(h), ctypes.byref(opts))
+        if rc != 0:
+            raise HamsGpuError(rc, "hg_create failed (is a CUDA device present?)")
+        self.h = h
+        self.n = 0
+        self.nbody = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.hg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise HamsGpuError(rc, self.L.hg_last_error(self.h).decode())
+        return rc
+
+    def set_mesh(self, nodes, ncon, ncn, xyz_p, ds, pnsz, dxyz_p, body_ranges, lid_xyz_p=None):
+        """nodes (ntnd,3), ncon (n,4) 1-based, xyz_p (n,3), dxyz_p (n,6), body_ranges (nbody,2) 1-based."""
+        f = lambda a, t=np.float64: np.asfortranarray(a, dtype=t)  # noqa: E731
+        self._keep = [f(nodes), f(ncon, np.int32), np.ascontiguousarray(ncn, dtype=np.int32), f(xyz_p),
+                      np.ascontiguousarray(ds, dtype=np.float64), np.ascontiguousarray(pnsz, dtype=np.float64),
+                      f(dxyz_p)]
+        lid = None if lid_xyz_p is None or len(lid_xyz_p) == 0 else f(lid_xyz_p)
+        br = np.ascontiguousarray(np.asarray(body_ranges, dtype=np.int32).reshape(-1))
+        n = len(self._keep[2])
+        self._check(self.L.hg_set_mesh(self.h, n, len(self._keep[0]), *[_ptr(a) for a in self._keep],
+                                       0 if lid is None else len(lid), _ptr(lid), len(br) // 2, _ptr(br)))
+        self.n = n
+        self.nbody = len(br) // 2
+        self.nl = 0 if lid is None else len(lid)
+
+    def set_frequency(self, v, wk, w1, h, wvn=None):
+        w = None if wvn is None else np.ascontiguousarray(wvn, dtype=np.float64)
+        self._check(self.L.hg_set_frequency(self.h, v, wk, w1, h, _ptr(w), 0 if w is None else len(w)))
+
+    def fill_factor(self, irsp=0):
+        return self._check(self.L.hg_fill_factor(self.h, irsp))
+
+    def keep_matrices(self, keep=True):
+        self._check(self.L.hg_keep_matrices(self.h, 1 if keep else 0))
+
+    def get_matrix(self, which, rows):
+        out = np.zeros((rows, self.n), dtype=np.complex128, order="F")
+        self._check(self.L.hg_get_matrix(self.h, which, _ptr(out), rows))
+        return out
+
+    def solve_radiation(self):
+        out = np.zeros((self.n, 6 * self.nbody), dtype=np.complex128, order="F")
+        self._check(self.L.hg_solve_radiation(self.h, _ptr(out), self.n))
+        return out
+
+    def solve_all_headings(self, betas):
+        b = np.ascontiguousarray(betas, dtype=np.float64)
+        out = np.zeros((self.n, len(b)), dtype=np.complex128, order="F")
+        self._check(self.L.hg_solve_all_headings(self.h, _ptr(b), len(b), _ptr(out), self.n))
+        return out
+
+    def solve_diffraction(self, beta):
+        out = np.zeros(self.n, dtype=np.complex128)
+        self._check(self.L.hg_solve_diffraction(self.h, float(beta), _ptr(out)))
+        return out
+
+    def forces(self, nbeta, isol=1):
+        nd = 6 * self.nbody
+        amas = np.zeros((nd, nd), order="F"); bdmp = np.zeros((nd, nd), order="F")
+        exfc = np.zeros((max(nbeta, 1), nd), dtype=np.complex128, order="F")
+        self._check(self.L.hg_forces(self.h, isol, _ptr(amas), _ptr(bdmp), _ptr(exfc)))
+        return amas, bdmp, exfc[:nbeta]
+
+    def solve_frequency(self, v, wk, w1, h, wvn, betas, irsp=0, isol=1, want_potentials=True, out=None):
+        """One frequency-solve; returns (amas, bdmp, exfc, mxpot or None).
+
+        ``out`` may hold preallocated (pinned) arrays to avoid allocations."""
+        nd = 6 * self.nbody
+        b = np.ascontiguousarray(betas, dtype=np.float64)
+        nb = len(b)
+        if out is None:
+            out = {"amas": np.zeros((nd, nd), order="F"), "bdmp": np.zeros((nd, nd), order="F"),
+                   "exfc": np.zeros((max(nb, 1), nd), dtype=np.complex128, order="F"),
+                   "mxpot": np.zeros((self.n, nd + nb), dtype=np.complex128, order="F") if want_potentials else None}
+        w = None if wvn is None or h <= 0 else np.ascontiguousarray(wvn, dtype=np.float64)
+        mx = out.get("mxpot")
+        self._check(self.L.hg_solve_frequency(self.h, v, wk, w1, h, _ptr(w), 0 if w is None else len(w), irsp,
+                                              _ptr(b), nb, isol, _ptr(out["amas"]), _ptr(out["bdmp"]),
+                                              _ptr(out["exfc"]), _ptr(mx), self.n))
+        return out["amas"], out["bdmp"], out["exfc"][:nb], mx
+
+    def green_points(self, pts, flags):
+        p = np.ascontiguousarray(pts, dtype=np.float64)
+        fl = np.ascontiguousarray(flags, dtype=np.int32)
+        out = np.zeros((len(fl), 8))
+        self._check(self.L.hg_green_points(self.h, len(fl), _ptr(p), _ptr(fl), _ptr(out)))
+        return out[:, 0::2] + 1j * out[:, 1::2]
+
+    def refine_info(self):
+        s = ctypes.c_int(); r = ctypes.c_double()
+        self.L.hg_refine_info(self.h, ctypes.byref(s), ctypes.byref(r))
+        return s.value, r.value
+
+    def stage_times(self):
+        a = (ctypes.c_float * 4)()
+        self.L.hg_stage_times(self.h, a)
+        return list(a)

@@ -1,0 +1,163 @@
+/*
+ * hamsgpu: GB300 (sm_103a) library for the HAMS-MREL per-frequency
+ * boundary-integral path.  C ABI: plain pointers and sizes, no C++ or CUDA
+ * types, callable from Fortran through ISO_C_BINDING.
+ *
+ * Array conventions follow the Fortran caller: every 2-D array is
+ * column-major (Fortran order), node and panel indices inside NCON are
+ * 1-based, complex numbers are interleaved (re, im) doubles, i.e.
+ * COMPLEX*16.  The library owns every device buffer; host pointers passed
+ * in are only read or written during the call.
+ *
+ * Status codes follow LAPACK: 0 success, < 0 the -k-th argument is invalid,
+ * > 0 a zero pivot at that 1-based row of the LU.  CUDA failures and
+ * device-side status bits return HG_ERR_CUDA / HG_ERR_DEVICE with a message
+ * available from hg_last_error().  No call aborts the process.
+ *
+ * Threading: one context per host thread at a time; calls on a context are
+ * serialised by the caller and run on the context's own CUDA stream.
+ */
+#ifndef HAMSGPU_H
+#define HAMSGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HG_ERR_CUDA (-1000)
+#define HG_ERR_DEVICE (-1001)
+#define HG_ERR_STATE (-1002)
+#define HG_ERR_ALLOC (-1003)
+
+/* Precision of the solve. */
+#define HG_PREC_FP64 0   /* plain form: complex128 throughout */
+#define HG_PREC_MIXED 1  /* precision form: complex64 fill and LU, FP64 iterative refinement */
+
+typedef struct hg_ctx hg_ctx;
+
+typedef struct {
+    int device;          /* CUDA device ordinal */
+    int precision;       /* HG_PREC_FP64 or HG_PREC_MIXED */
+    int grn_kind;        /* 8: Green values kept in double; 4: rounded to single precision
+                            before assembly, as the reference's GRN_KIND=4 storage
+                            (src/WavDynMods.f90:47) */
+    int max_refine;      /* mixed form: maximum refinement sweeps (default 10) */
+    double refine_tol;   /* mixed form: stop when max_k ||A x_k - b_k|| / ||b_k|| <= tol (default 1e-12) */
+    double rho;          /* fluid density for the forces (reference Const_mod: 1000) */
+    double g;            /* gravity for VINP (reference Const_mod: 9.80665) */
+} hg_opts;
+
+/* Fill opts with the defaults above (device 0, FP64, GRN_KIND 8, rho 1000, g 9.80665). */
+void hg_default_opts(hg_opts *opts);
+
+/* Create / destroy a context.  opts may be NULL for the defaults. */
+int hg_create(hg_ctx **ctx, const hg_opts *opts);
+void hg_destroy(hg_ctx *ctx);
+const char *hg_last_error(const hg_ctx *ctx);
+
+/*
+ * Mesh, once per run after CalNormals / BuildCombinedArrays
+ * (src/ReadPanelMesh.f90:110-190, src/CalGreenFuncMulti.f90:53-106).
+ * Replaces the module-global geometry that CALGREEN reads
+ * (src/CalGreenFunc.f90:49-118): XYZ, NCON, NCN, XYZ_P, DS, PNSZ, DXYZ_P
+ * and, for IRSP=1, iXYZ_P.
+ *   n, ntnd          hull panels and nodes (global, body-major order)
+ *   nodes[ntnd*3]    XYZ(NTND,3)
+ *   ncon[n*4]        NCON(NELEM,4), 1-based node ids
+ *   ncn[n]           NCN, 3 or 4
+ *   xyz_p[n*3]       XYZ_P(NELEM,3) panel centroids
+ *   ds[n], pnsz[n]   areas and longest edges
+ *   dxyz_p[n*6]      DXYZ_P(NELEM,6) generalized normals
+ *   nl, lid_xyz_p    lid (waterplane) panel count and centroids iXYZ_P(iNELEM,3); nl = 0 without lids
+ *   nbody            number of bodies
+ *   body_ranges[2*nbody]  1-based first,last hull panel of each body (NELEM_TOTAL_RAD)
+ */
+int hg_set_mesh(hg_ctx *ctx, int n, int ntnd, const double *nodes, const int *ncon, const int *ncn,
+                const double *xyz_p, const double *ds, const double *pnsz, const double *dxyz_p,
+                int nl, const double *lid_xyz_p, int nbody, const int *body_ranges);
+
+/*
+ * Wave state of one frequency, after CalWaveProperts (src/ImplementSubs.f90:40-151):
+ * v = w^2/g (0 and -1 select the zero/infinite-frequency limits), wk = wave number,
+ * w1 = circular frequency, h = depth (< 0 deep water), wvn[nk] = DISPERSION roots
+ * (ignored in deep water; may be NULL then).
+ */
+int hg_set_frequency(hg_ctx *ctx, double v, double wk, double w1, double h, const double *wvn, int nk);
+
+/*
+ * CALGREEN / CALGREEN_IRR / CALGREEN_MULTI(_IRR) + ASSB_LEFT* including ZGETRF
+ * (src/AssbMatx.f90:53-116, src/AssbMatx_irr.f90:53-180): Green fill, influence
+ * matrix, for irsp = 1 the normal equations C = A^T A, and the LU.
+ * Returns 0, or the 1-based row of a zero pivot, or an error code.
+ */
+int hg_fill_factor(hg_ctx *ctx, int irsp);
+
+/*
+ * ASSB_RBC* + RADIATION_SOLVER* (src/AssbMatx.f90:123-181, :257-312): radiation
+ * potentials of all 6*nbody modes into mxpot (column-major, leading dimension
+ * ldm >= n, 6*nbody columns, COMPLEX*16).
+ */
+int hg_solve_radiation(hg_ctx *ctx, double *mxpot, int ldm);
+
+/*
+ * ASSB_DBC* + DIFFRACTION_SOLVER* for nbeta headings at once (radians):
+ * diffraction potentials into mxpot_dif (ldm >= n, nbeta columns).
+ * hg_solve_diffraction is the one-heading form of the reference interface.
+ */
+int hg_solve_all_headings(hg_ctx *ctx, const double *betas, int nbeta, double *mxpot_dif, int ldm);
+int hg_solve_diffraction(hg_ctx *ctx, double beta, double *mxpot_col);
+
+/*
+ * RFORCE_MULTI / EFORCE_MULTI (src/PotentWavForceMulti.f90:45-226) on the device
+ * from the last radiation and diffraction solves:
+ *   amas[6nb*6nb], bdmp[6nb*6nb]  column-major AMAS/BDMP (row = force DOF, column = mode)
+ *   exfc[nbeta*6nb]               COMPLEX*16, column-major (heading, DOF)
+ * isol = 1 adds the incident potential (ISOL of ControlFile.in).
+ */
+int hg_forces(hg_ctx *ctx, int isol, double *amas, double *bdmp, double *exfc);
+
+/*
+ * One frequency-solve in one call: set_frequency + fill_factor + radiation +
+ * all headings + forces.  mxpot may be NULL (no potential read-back); else it
+ * receives n x (6*nbody + nbeta) COMPLEX*16 with leading dimension ldm.
+ */
+int hg_solve_frequency(hg_ctx *ctx, double v, double wk, double w1, double h, const double *wvn, int nk,
+                       int irsp, const double *betas, int nbeta, int isol, double *amas, double *bdmp,
+                       double *exfc, double *mxpot, int ldm);
+
+/* Diagnostics for tests: copy the tn x n influence matrix (which = 0, before
+ * factorisation) or single-layer matrix (which = 1) of the last fill to host
+ * memory (COMPLEX*16, leading dimension ld >= tn).  Requires hg_fill_factor
+ * to have run with keep_matrices enabled by hg_keep_matrices(ctx, 1). */
+int hg_keep_matrices(hg_ctx *ctx, int keep);
+int hg_get_matrix(hg_ctx *ctx, int which, double *out, int ld);
+
+/* Green function of the current frequency at npts arbitrary point pairs:
+ * pts[6*k..] = (xq, yq, zq, xp, yp, zp) source and field, flags[k] in {0,1}
+ * (FLAG of INFGREEN3D / FINGREEN3D), out[8*k..] = GRN(1..4) as (re, im). */
+int hg_green_points(hg_ctx *ctx, int npts, const double *pts, const int *flags, double *out);
+
+/* Host-side helpers (no device work).
+ * hg_dispersion: DISPERSION (src/WavDynSubs.f90:40-126), nk roots for depth h > 0.
+ * hg_wave_properties: CalWaveProperts (src/ImplementSubs.f90:40-151) for one
+ *   frequency-list entry; inft as Input_frequency_type (1..5); h < 0 deep water.
+ * hg_panel_geometry: CalPanelCentre / CalPanelArea / CalPanelChartLength /
+ *   CalTransNormals / CalRotNormals (src/NormalProcess.f90) for n panels.
+ * Each returns 0 or a negative argument index (> 0: a root failed to converge). */
+int hg_dispersion(double w, double h, int nk, double *wvn);
+int hg_wave_properties(int inft, double value, double h, int nk, double *v, double *wk, double *w1,
+                       double *wvn);
+int hg_panel_geometry(int n, int ntnd, const double *nodes, const int *ncon, const int *ncn, const double *xr,
+                      double *xyz_p, double *ds, double *pnsz, double *dxyz_p);
+
+/* Refinement sweeps taken and final relative residual of the last mixed-form solve. */
+int hg_refine_info(const hg_ctx *ctx, int *sweeps, double *residual);
+
+/* Time (milliseconds, CUDA events on the context stream) of the stages of the
+ * last hg_solve_frequency: [0] fill, [1] LU, [2] solves and refinement, [3] forces. */
+int hg_stage_times(const hg_ctx *ctx, float *ms4);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
