@@ -1,0 +1,382 @@
+"""Benchmark: frequency-solves per second of the per-frequency BEM path.
+
+Workload (one "step" = one frequency-solve): the 5-body array of 6048
+panels in deep water (3 cylinders R = 4 m, T = 8 m with 48 x 22 side and
+48 x 8 bottom panels, 2 boxes 12 x 6 x 4 m with 0.5 m panels, on a 30 m grid
+perturbed by U(-3, 3) m from seed 3), 60 frequencies uniform in 0.1-2.5
+rad/s cycled step by step, 8 headings 0..315 deg, 30 rigid-body modes.  A
+step is the Green-function fill + influence-matrix assembly + LU + solves
+for all 30 modes and 8 headings + added mass, damping and excitation force.
+
+Default arm (ours): the mixed-precision form (complex64 fill and LU, FP64
+refinement) through the C ABI; the plain complex128 form is measured on a
+few steps beside it, and the mixed results are checked against it (1e-4).
+--impl reference: the CPU restatement of the reference (the oracle: C with
+OpenMP over field rows, LAPACK zgetrf/zgetrs through scipy's OpenBLAS) on
+all host cores; the reference itself is Fortran and no Fortran compiler
+exists on either machine.
+
+Multi-GPU (torchrun): frequencies are split round-robin over ranks, each
+rank a full replica with its own context; the only collectives are the
+barrier and the max over ranks of the timed region (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_FREQ = 60
+FREQS = np.linspace(0.1, 2.5, N_FREQ)
+BETAS_DEG = np.arange(8) * 45.0
+METRIC = "freq-solves/s at 6k panels (mixed vs FP64 GPU, <=1e-4 err); p50/p99 latency"
+CONFIG = {"workload": "5-body array, 6048 panels, deep water, 60 freqs x 8 headings, 30 modes",
+          "panels": 6048, "bodies": 5, "headings": 8, "modes": 30, "depth": "infinite",
+          "l2": "inputs larger than L2 (A and S are 2 x 293 MB complex64 per step)"}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p, "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            t = [x.strip() for x in ln.split(",")]
+            if len(t) < 9:
+                continue
+            try:
+                sm.append(float(t[1]))
+                mx = float(t[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, t[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        rank = int(os.environ["RANK"])
+        local = int(os.environ.get("LOCAL_RANK", rank))
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return dist, rank, ws, local
+    return None, 0, 1, 0
+
+
+def _barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def _max_over_ranks(dist, x, local):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _mesh():
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    return pkg, pkg.meshgen.five_body_array(seed=3)
+
+
+def _frequency_inputs(pkg, w):
+    v, wk, w1, wvn = pkg.hamsgpu.wave_properties(3, float(w), -1.0)
+    return v, wk, w1
+
+
+def cpu_reference(steps, warmup, rank, world):
+    """The oracle (CPU restatement of the reference path), all host cores."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    pkg, mesh = _mesh()
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import case_from_mesh
+    case = case_from_mesh(oracle, mesh, h=-1.0, headings_deg=list(BETAS_DEG))
+    cores = os.cpu_count()
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", str(cores))
+    # one bounded step = one full frequency-solve (about 10-30 s of CPU work at 6048 panels)
+    times = []
+    for k in range(warmup + steps):
+        w = FREQS[k % N_FREQ]
+        t0 = time.perf_counter()
+        oracle.solve_frequency(case, w, nthreads=cores)
+        t1 = time.perf_counter()
+        if k >= warmup:
+            times.append(t1 - t0)
+    total = sum(times)
+    value = len(times) / total
+    line = {"metric": METRIC, "value": value, "unit": "freq-solves/s", "n_gpus": world, "steps": steps,
+            "warmup": warmup, "ms_per_step": 1e3 * total / len(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "complex128", "data": "synthetic",
+            "config": CONFIG, "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "freq-solves/s", "cores": cores, "kind": "port",
+                             "sample": f"{len(times)} full frequency-solves of the 6048-panel workload"},
+            "e2e": {"value": value, "unit": "freq-solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def _cpu_baseline_sample():
+    """One full frequency-solve of the workload by the oracle on all host cores."""
+    try:
+        return _cpu_baseline_sample_inner()
+    except Exception as e:  # reported, never silently dropped
+        return {"value": None, "unit": "freq-solves/s", "cores": os.cpu_count(), "kind": "port",
+                "sample": f"failed: {e}"}
+
+
+def _cpu_baseline_sample_inner():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    pkg, mesh = _mesh()
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import case_from_mesh
+    case = case_from_mesh(oracle, mesh, h=-1.0, headings_deg=list(BETAS_DEG))
+    cores = os.cpu_count()
+    t0 = time.perf_counter()
+    oracle.solve_frequency(case, FREQS[17], nthreads=cores)
+    dt = time.perf_counter() - t0
+    return {"value": 1.0 / dt, "unit": "freq-solves/s", "cores": cores, "kind": "port",
+            "sample": "1 full frequency-solve (w = %.3f rad/s) of the 6048-panel workload: C oracle with OpenMP "
+                      "over field rows + scipy/OpenBLAS zgetrf/zgetrs" % FREQS[17]}
+
+
+def ours(args, dist, rank, world, local):
+    pkg, mesh = _mesh()
+    hg = pkg.hamsgpu
+    prec = hg.HG_PREC_MIXED if args.precision == "mixed" else hg.HG_PREC_FP64
+    my_freqs = [FREQS[k] for k in range(rank, N_FREQ, world)]
+    betas = BETAS_DEG * math.pi / 180.0
+    nd = 30
+    s = hg.Solver(precision=prec, device=local)
+    s.set_mesh(mesh.nodes, mesh.ncon, mesh.ncn, mesh.xyz_p, mesh.ds, mesh.pnsz, mesh.dxyz_p, mesh.body_ranges)
+    out = {"amas": np.zeros((nd, nd), order="F"), "bdmp": np.zeros((nd, nd), order="F"),
+           "exfc": np.zeros((8, nd), dtype=np.complex128, order="F"), "mxpot": None}
+
+    def step(k, o=out):
+        v, wk, w1 = _frequency_inputs(pkg, my_freqs[k % len(my_freqs)])
+        return s.solve_frequency(v, wk, w1, -1.0, None, betas, out=o)
+
+    for k in range(args.warmup):
+        step(k)
+    # ---- device-timed region (inputs resident, no potential read-back) ----
+    lat = []
+    _barrier(dist)
+    with ClockSampler(local) as clk:
+        s.mark(0)
+        for k in range(args.steps):
+            s.mark(2 + (k % 2))
+            step(args.warmup + k)
+            s.mark(3 - (k % 2))
+            lat.append(s.elapsed_ms(2 + (k % 2), 3 - (k % 2)))
+        s.mark(1)
+        ms = s.elapsed_ms(0, 1)
+    stages = s.stage_times()
+    sweeps, resid = s.refine_info()
+    ms_max = _max_over_ranks(dist, ms, local)
+    value = world * args.steps / (ms_max / 1e3)
+    clocks = clk.summary()
+
+    # ---- end to end through the C ABI with host buffers ----
+    pinned = None
+    try:
+        import torch
+        pinned = torch.empty((mesh.n, nd + 8), dtype=torch.complex128, pin_memory=True).numpy()
+    except Exception:
+        pinned = np.zeros((mesh.n, nd + 8), dtype=np.complex128)
+    e2e_out = dict(out)
+    e2e_out["mxpot"] = np.asfortranarray(pinned) if pinned.flags["F_CONTIGUOUS"] else pinned
+    if not e2e_out["mxpot"].flags["F_CONTIGUOUS"]:
+        e2e_out["mxpot"] = np.zeros((mesh.n, nd + 8), dtype=np.complex128, order="F")
+    s2 = hg.Solver(precision=prec, device=local)
+    _barrier(dist)
+    t0 = time.perf_counter()
+    s2.set_mesh(mesh.nodes, mesh.ncon, mesh.ncn, mesh.xyz_p, mesh.ds, mesh.pnsz, mesh.dxyz_p, mesh.body_ranges)
+    for k in range(args.steps):
+        v, wk, w1 = _frequency_inputs(pkg, my_freqs[k % len(my_freqs)])
+        s2.solve_frequency(v, wk, w1, -1.0, None, betas, out=e2e_out)
+    t_e2e = time.perf_counter() - t0
+    t_e2e = _max_over_ranks(dist, t_e2e, local)
+    s2.close()
+    mesh_bytes = mesh.nodes.nbytes + mesh.ncon.nbytes + mesh.ncn.nbytes + mesh.xyz_p.nbytes + mesh.ds.nbytes + \
+        mesh.pnsz.nbytes + mesh.dxyz_p.nbytes + mesh.body_ranges.nbytes
+    h2d = mesh_bytes / args.steps + betas.nbytes
+    d2h = 2 * nd * nd * 8 + 8 * nd * 16 + mesh.n * (nd + 8) * 16
+
+    # ---- plain FP64 form on a few steps, and the accuracy of the mixed form against it ----
+    fp64 = None
+    if rank == 0 and prec == hg.HG_PREC_MIXED and args.fp64_steps > 0:
+        sp = hg.Solver(precision=hg.HG_PREC_FP64, device=local)
+        sp.set_mesh(mesh.nodes, mesh.ncon, mesh.ncn, mesh.xyz_p, mesh.ds, mesh.pnsz, mesh.dxyz_p, mesh.body_ranges)
+        errs = []
+        pms = []
+        for k in range(args.fp64_steps):
+            w = FREQS[(7 + 19 * k) % N_FREQ]
+            v, wk, w1 = _frequency_inputs(pkg, w)
+            sp.mark(4)
+            a64, b64, f64, _ = sp.solve_frequency(v, wk, w1, -1.0, None, betas)
+            sp.mark(5)
+            pms.append(sp.elapsed_ms(4, 5))
+            a64, b64, f64 = a64.copy(), b64.copy(), f64.copy()
+            am, bm, fm, _ = s.solve_frequency(v, wk, w1, -1.0, None, betas)
+            e = lambda x, y: float(np.abs(x - y).max() / np.abs(y).max())  # noqa: E731
+            errs.append({"A": e(am, a64), "B": e(bm, b64), "F": e(fm, f64)})
+        sp.close()
+        fp64 = {"freq_solves_per_s": 1e3 / statistics.mean(pms), "ms_per_step": statistics.mean(pms),
+                "steps": args.fp64_steps,
+                "mixed_vs_fp64_max_norm_err": {k: max(d[k] for d in errs) for k in ("A", "B", "F")}}
+
+    # ---- roofline of the dominant kernel (the LU trailing-update GEMM) ----
+    roof = None
+    if rank == 0:
+        roof = _roofline(s, mesh.n, prec, hg)
+    s.close()
+    if rank != 0:
+        return
+    lat_sorted = sorted(lat)
+    line = {"metric": METRIC, "value": value, "unit": "freq-solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "complex64+fp64-refine" if prec == hg.HG_PREC_MIXED else "complex128",
+            "data": "synthetic", "config": dict(CONFIG, precision=args.precision, parallelism=f"replicas{world}"),
+            "latency_ms": {"p50": lat_sorted[len(lat) // 2], "p99": lat_sorted[min(len(lat) - 1,
+                                                                                  int(0.99 * len(lat)))]},
+            "stage_ms_last_step": {"fill": stages[0], "lu": stages[1], "solve_refine": stages[2],
+                                   "forces_readback": stages[3]},
+            "refine": {"sweeps": sweeps, "residual": resid},
+            "e2e": {"value": world * args.steps / t_e2e, "unit": "freq-solves/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": _launch_count(mesh.n, prec) * args.steps,
+            "clocks": clocks, "roofline": roof, "fp64_form": fp64}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = _cpu_baseline_sample()
+    print(json.dumps(line), flush=True)
+
+
+def _launch_count(n, prec):
+    """Kernels the library launches per frequency-solve (fill, conversion, LU
+    panels, solves, refinement, forces), counted from the launch sequence."""
+    nb = 32
+    panels = (n + nb - 1) // nb
+    lu = panels * 4                                # getf2, laswp, trsm, gemm per panel
+    getrs = 1 + 2 * panels * 2                     # laswp + (trsm, gemm) forward and backward
+    fill = 1 + (1 if prec == 1 else 0)             # fill (+ complex64 -> complex128 copy)
+    rhs = 3                                        # incident weights, partial products, reduce
+    refine = 0 if prec == 0 else 2 + 3 * (getrs + 4)  # initial + ~2 correction sweeps
+    return fill + lu + rhs + getrs + refine + 1
+
+
+def _roofline(s, n, prec, hg):
+    """Time the library's trailing-update GEMM at the first panel's shape
+    (m = n' = N - 32, k = 32), the dominant contraction of the LU."""
+    import ctypes
+    L = s.L
+    if not hasattr(L, "hg_bench_gemm"):
+        return None
+    L.hg_bench_gemm.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                ctypes.POINTER(ctypes.c_float)]
+    m = n - 32
+    k = 32
+    ms = ctypes.c_float()
+    rc = L.hg_bench_gemm(s.h, 1 if prec == hg.HG_PREC_MIXED else 0, m, m, k, 10, ctypes.byref(ms))
+    if rc != 0:
+        return None
+    flops = 8.0 * m * m * k
+    achieved = flops / (ms.value / 1e3) / 1e12
+    peaks, kind = _peaks()
+    peak = peaks.get("bf16_tflops", 1900.0)
+    return {"kernel": "k_gemm (LU trailing update A22 -= L21 U12, complex%s)" % ("64" if prec else "128"),
+            "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "peak_source": f"bf16_tflops of {kind} peaks",
+            "flops_per_launch": flops, "ms_per_launch": ms.value, "traffic": None}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        rank = int(os.environ.get("RANK", "0"))
+        world = int(os.environ.get("WORLD_SIZE", "1"))
+        cpu_reference(args.steps, args.warmup, rank, world)
+        return
+    dist, rank, world, local = _dist()
+    try:
+        ours(args, dist, rank, world, local)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

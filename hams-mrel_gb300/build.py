@@ -22,6 +22,10 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
            "-Xptxas", "-warn-spills"]
+# Per-file flags.  The finite-depth Green series must not be contracted into
+# fused multiply-adds: their epsilon-algorithm extrapolation amplifies
+# last-bit differences (see hg_fill_fin.cu).
+FILE_FLAGS = {"hg_fill_fin.cu": ["-fmad=false"]}
 
 
 def _nvcc() -> str:
@@ -56,7 +60,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-        cmd = [nvcc] + ARCH + flags + ["-I", INCLUDE, "-c", src, "-o", obj]
+        cmd = [nvcc] + ARCH + flags + FILE_FLAGS.get(os.path.basename(src), []) + ["-I", INCLUDE, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {os.path.basename(src)}:\n{r.stderr}")

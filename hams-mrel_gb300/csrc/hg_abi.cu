@@ -71,6 +71,7 @@ struct hg_ctx {
   int sweeps = 0;
   double resid = 0.0;
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t user_ev[16] = {};
   float stage_ms[4] = {0, 0, 0, 0};
 };
 
@@ -309,6 +310,8 @@ void hg_destroy(hg_ctx* c) {
   for (auto* b : cbs) b->release();
   for (int k = 0; k < 5; ++k)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+  for (int k = 0; k < 16; ++k)
+    if (c->user_ev[k]) cudaEventDestroy(c->user_ev[k]);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -647,6 +650,64 @@ int hg_refine_info(const hg_ctx* c, int* sweeps, double* residual) {
   if (!c) return -1;
   if (sweeps) *sweeps = c->sweeps;
   if (residual) *residual = c->resid;
+  return 0;
+}
+
+int hg_bench_gemm(hg_ctx* c, int precision, int m, int n, int k, int iters, float* ms_per_launch) {
+  if (!c) return -1;
+  if (precision != 0 && precision != 1) return fail(c, -2, "precision must be 0 or 1");
+  if (m <= 0 || n <= 0 || k <= 0) return fail(c, -3, "bad shape");
+  if (iters <= 0) return fail(c, -6, "iters must be positive");
+  if (!ms_per_launch) return fail(c, -7, "ms_per_launch is NULL");
+  cudaSetDevice(c->o.device);
+  const size_t es = precision ? sizeof(float2) : sizeof(double2);
+  void *a = nullptr, *b = nullptr, *cc = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaMalloc(&a, (size_t)m * k * es);
+  if (e == cudaSuccess) e = cudaMalloc(&b, (size_t)k * n * es);
+  if (e == cudaSuccess) e = cudaMalloc(&cc, (size_t)m * n * es);
+  if (e == cudaSuccess) e = cudaMemsetAsync(a, 0, (size_t)m * k * es, c->st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b, 0, (size_t)k * n * es, c->st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(cc, 0, (size_t)m * n * es, c->st);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  for (int it = -1; it < iters && e == cudaSuccess; ++it) {
+    if (it == 0) e = cudaEventRecord(e0, c->st);
+    if (e != cudaSuccess) break;
+    if (precision)
+      e = hg::gemm<float>(c->st, false, m, n, k, make_float2(-1, 0), (float2*)a, m, (float2*)b, k, make_float2(1, 0),
+                          (float2*)cc, m);
+    else
+      e = hg::gemm<double>(c->st, false, m, n, k, make_double2(-1, 0), (double2*)a, m, (double2*)b, k,
+                           make_double2(1, 0), (double2*)cc, m);
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(e1, c->st);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float ms = 0;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(a); cudaFree(b); cudaFree(cc);
+  if (e != cudaSuccess) return fail(c, HG_ERR_CUDA, "hg_bench_gemm: %s", cudaGetErrorString(e));
+  *ms_per_launch = ms / iters;
+  return 0;
+}
+
+int hg_mark(hg_ctx* c, int slot) {
+  if (!c) return -1;
+  if (slot < 0 || slot >= 16) return fail(c, -2, "slot must be in 0..15");
+  if (!c->user_ev[slot]) CK(cudaEventCreate(&c->user_ev[slot]));
+  CK(cudaEventRecord(c->user_ev[slot], c->st));
+  return 0;
+}
+
+int hg_elapsed(hg_ctx* c, int s0, int s1, float* ms) {
+  if (!c) return -1;
+  if (s0 < 0 || s0 >= 16 || !c->user_ev[s0]) return fail(c, -2, "slot %d was not marked", s0);
+  if (s1 < 0 || s1 >= 16 || !c->user_ev[s1]) return fail(c, -3, "slot %d was not marked", s1);
+  if (!ms) return fail(c, -4, "ms is NULL");
+  CK(cudaEventSynchronize(c->user_ev[s1]));
+  CK(cudaEventElapsedTime(ms, c->user_ev[s0], c->user_ev[s1]));
   return 0;
 }
 

@@ -82,6 +82,13 @@ struct HgStatus {
   int detail;
 };
 
-__device__ __forceinline__ void hg_set_status(int* status, int bit) {
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline void hg_set_status(int* status, int bit) {
+#ifdef __CUDA_ARCH__
   if (status) atomicOr(status, bit);
+#else
+  if (status) *status |= bit;
+#endif
 }

@@ -1,0 +1,30 @@
+// Finite-depth instantiations of the pair kernel.  This translation unit
+// is compiled with -fmad=false: the Wynn epsilon extrapolation of the
+// finite-depth series (Limes, src/FinGrnExtSubs.f90:370-503) divides by
+// differences of nearly converged partial sums, so a fused multiply-add
+// anywhere upstream changes its result far beyond one rounding; with
+// separately rounded products the series reproduce the reference's
+// arithmetic.
+#include "hg_fill_kernel.cuh"
+
+namespace hg {
+
+template <typename OUT>
+cudaError_t launch_green_fill_fin(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
+                                  const FinState& fs, int grn_kind, OUT* A, OUT* S, long lda, int* status) {
+  dim3 grid((tn + FILL_ROWS - 1) / FILL_ROWS, (n + FILL_COLS - 1) / FILL_COLS);
+  k_green_fill<false, OUT><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, status);
+  return cudaGetLastError();
+}
+template cudaError_t launch_green_fill_fin<double2>(cudaStream_t, const double*, const double*, int, int, int,
+                                                    const FinState&, int, double2*, double2*, long, int*);
+template cudaError_t launch_green_fill_fin<float2>(cudaStream_t, const double*, const double*, int, int, int,
+                                                   const FinState&, int, float2*, float2*, long, int*);
+
+cudaError_t launch_green_points_fin(cudaStream_t st, int npts, const double* pts, const int* flags, const FinState& fs,
+                                    double* out) {
+  k_green_points<false><<<(npts + 63) / 64, 64, 0, st>>>(npts, pts, flags, fs, out);
+  return cudaGetLastError();
+}
+
+}  // namespace hg

@@ -17,14 +17,26 @@
 #pragma once
 #include "hg_common.cuh"
 
+#ifdef __CUDACC__
+#define HGD __host__ __device__
+#else
+#define HGD
+#endif
+
 namespace hg {
+
+#ifdef __CUDA_ARCH__
+#define HGD_TABLE __device__ const
+#else
+#define HGD_TABLE static const
+#endif
 
 // ===================================================================
 // Newman (1986) closed-form integral of 1/r and grad(1/r) over a flat
 // panel, SingularIntgr.f90:44-244 (triangles) and :252-445 (quads).
 // pr = 36-double source-panel record (hg_common.cuh).
 // ===================================================================
-__device__ __forceinline__ void newman_pair(const double* __restrict__ pr, double xf0, double xf1,
+HGD inline void newman_pair(const double* __restrict__ pr, double xf0, double xf1,
                                             double xf2, double& sij, double& d0, double& d1,
                                             double& d2) {
   const double p0 = xf0 - pr[PR_PO], p1 = xf1 - pr[PR_PO + 1], p2 = xf2 - pr[PR_PO + 2];
@@ -75,42 +87,42 @@ __device__ __forceinline__ void newman_pair(const double* __restrict__ pr, doubl
 // ===================================================================
 // Deep water
 // ===================================================================
-__device__ __forceinline__ double poly_a(double t) {
+HGD inline double poly_a(double t) {
   double g = (21859.0 + -4838.6 * t) * t;
   g = (-41592.9 + g) * t; g = (42002.57 + g) * t; g = (-24314.21 + g) * t;
   g = (8418.94 + g) * t; g = (-1763.96 + g) * t; g = (215.896 + g) * t;
   g = (-13.328 + g) * t; return 1.21 + g;
 }
-__device__ __forceinline__ double poly_b(double t) {
+HGD inline double poly_b(double t) {
   double g = (-29030.24 + 7671.22 * t) * t;
   g = (44894.06 + g) * t; g = (-36618.81 + g) * t; g = (17137.74 + g) * t;
   g = (-4780.77 + g) * t; g = (796.534 + g) * t; g = (-67.92 + g) * t;
   g = (5.373 + g) * t; return 0.938 + g;
 }
-__device__ __forceinline__ double poly_c(double t) {
+HGD inline double poly_c(double t) {
   double g = (9136.4 + -3272.62 * t) * t;
   g = (-9844.35 + g) * t; g = (5155.67 + g) * t; g = (-1397.89 + g) * t;
   g = (209.653 + g) * t; g = (-9.747 + g) * t; return 1.268 + g;
 }
-__device__ __forceinline__ double poly_d(double t) {
+HGD inline double poly_d(double t) {
   double g = (128170.2 + -33744.6 * t) * t;
   g = (-205690.43 + g) * t; g = (181856.75 + g) * t; g = (-96293.05 + g) * t;
   g = (31127.39 + g) * t; g = (-6072.07 + g) * t; g = (667.16 + g) * t;
   g = (-40.97 + g) * t; return 0.632 + g;
 }
-__device__ __forceinline__ double poly_da(double t) {
+HGD inline double poly_da(double t) {
   double g = (-46688.0 + 12622.25 * t) * t;
   g = (68220.87 + g) * t; g = (-48811.41 + g) * t; g = (16370.75 + g) * t;
   g = (-1187.71 + g) * t; g = (-754.85 + g) * t; g = (249.69 + g) * t;
   g = (-24.53 + g) * t; return 2.948 + g;
 }
-__device__ __forceinline__ double poly_db(double t) {
+HGD inline double poly_db(double t) {
   double g = (-76209.82 + 19923.28 * t) * t;
   g = (118879.26 + g) * t; g = (-97014.11 + g) * t; g = (44270.15 + g) * t;
   g = (-11336.19 + g) * t; g = (1565.35 + g) * t; g = (-76.765 + g) * t;
   g = (2.894 + g) * t; return 1.11 + g;
 }
-__device__ __forceinline__ double poly_dc(double t) {
+HGD inline double poly_dc(double t) {
   double g = (3168.35 + -1590.27 * t) * t;
   g = (-2318.58 + g) * t; g = (847.8 + g) * t; g = (-148.24 + g) * t;
   return 14.19 + g;
@@ -118,7 +130,7 @@ __device__ __forceinline__ double poly_dc(double t) {
 
 // Havelock wave term GF and its horizontal derivative GFh at the
 // non-dimensional horizontal distance hh = v*R and depth vv = v*(z+zeta).
-__device__ __forceinline__ void havelock(double hh, double vv, double2& gf, double2& gfh) {
+HGD inline void havelock(double hh, double vv, double2& gf, double2& gfh) {
   const double gama = 0.5772156649;
   const double dd = sqrt(hh * hh + vv * vv);
   const double alpha = -vv / dd, beta = hh / dd, rho = dd / (1.0 + dd);
@@ -141,7 +153,7 @@ __device__ __forceinline__ void havelock(double hh, double vv, double2& gf, doub
     h1 = (1.909859286 + (-1.145914713 + (0.294656958 + (-0.042070508 + (0.003785727 -
           0.000207183 * yy) * yy) * yy) * yy) * yy) * yy;
   } else {
-    const double y = 3.0 / hh, y2 = y * y, isq = rsqrt(hh);
+    const double y = 3.0 / hh, y2 = y * y, isq = 1.0 / sqrt(hh);
     const double f0 = 0.79788454 + (-0.00553897 + (0.00099336 + (-0.00044346 + (0.00020445 -
                       0.00004959 * y2) * y2) * y2) * y2) * y2;
     const double t0 = hh - 0.25 * HG_PI + (-0.04166592 + (0.00239399 + (-0.00073984 + (0.00031099 -
@@ -172,7 +184,7 @@ __device__ __forceinline__ void havelock(double hh, double vv, double2& gf, doub
 }
 
 // INFGREEN3D (InfGreen_Appr.f90:104-186).  Source (xq,yq,zq), field (xp,yp,zp).
-__device__ __forceinline__ void inf_green(double xq, double yq, double zq, double xp, double yp,
+HGD inline void inf_green(double xq, double yq, double zq, double xp, double yp,
                                           double zp, double v, int flag, double2 g[4]) {
   const double xpq = xq - xp, ypq = yq - yp, zpq = zp + zq;
   const double rr = sqrt(xpq * xpq + ypq * ypq);
@@ -214,7 +226,18 @@ __device__ __forceinline__ void inf_green(double xq, double yq, double zq, doubl
 // ===================================================================
 // Finite depth: special functions (FinGrnExtSubs.f90)
 // ===================================================================
-__device__ inline double d_error(double x) {  // ERROR :62-93
+// x**k for an integer k by binary powering, the evaluation order a Fortran
+// compiler uses for an integer exponent.
+HGD inline double powi(double x, int m) {
+  unsigned n = (unsigned)m;
+  double y = (n % 2u) ? x : 1.0;
+  while (n >>= 1) {
+    x = x * x;
+    if (n % 2u) y = y * x;
+  }
+  return y;
+}
+HGD inline double d_error(double x) {  // ERROR :62-93
   const double x2 = x * x;
   if (fabs(x) < 3.5) {
     double er = 1.0, r = 1.0;
@@ -233,10 +256,10 @@ __device__ inline double d_error(double x) {  // ERROR :62-93
   double e = 1.0 - exp(-x2) / (fabs(x) * sqrt(HG_PI)) * er;
   return x < 0.0 ? -e : e;
 }
-__device__ __forceinline__ double d_erfcc(double x) { return 1.0 - d_error(x); }
-__device__ __forceinline__ double d_derfcc(double x) { return -2.0 / sqrt(HG_PI) * exp(-(x * x)); }
+HGD inline double d_erfcc(double x) { return 1.0 - d_error(x); }
+HGD inline double d_derfcc(double x) { return -2.0 / sqrt(HG_PI) * exp(-(x * x)); }
 
-__device__ inline double d_e1xa(double x) {  // E1XA :119-133
+HGD inline double d_e1xa(double x) {  // E1XA :119-133
   if (x == 0.0) return 1.0e+300;
   if (x <= 1.0)
     return -log(x) + ((((1.07857e-3 * x - 9.76004e-3) * x + 5.519968e-2) * x - 0.24991055) * x +
@@ -246,7 +269,7 @@ __device__ inline double d_e1xa(double x) {  // E1XA :119-133
   return exp(-x) / x * es1 / es2;
 }
 
-__device__ inline double d_eix(double x) {  // EIX :146-172
+HGD inline double d_eix(double x) {  // EIX :146-172
   if (x == 0.0) return -1.0e+300;
   if (x <= 40.0) {
     double ei = 1.0, r = 1.0;
@@ -266,7 +289,7 @@ __device__ inline double d_eix(double x) {  // EIX :146-172
 }
 
 // IK01A :538-640, returning K0 and K1.
-__device__ inline void d_ik01a(double x, double& bk0, double& bk1) {
+HGD inline void d_ik01a(double x, double& bk0, double& bk1) {
   if (x == 0.0) { bk0 = 1.0e+300; bk1 = 1.0e+300; return; }
   const double x2 = x * x;
   double bi0, bi1;
@@ -298,12 +321,14 @@ __device__ inline void d_ik01a(double x, double& bk0, double& bk1) {
     if (x >= 35.0) k0 = 9;
     if (x >= 50.0) k0 = 7;
     const double ca = exp(x) / sqrt(2.0 * HG_PI * x), xr = 1.0 / x;
-    double p = 1.0, s0 = 1.0, s1 = 1.0;
+    double s0 = 1.0, s1 = 1.0;
     for (int k = 1; k <= 12; ++k) {
       if (k > k0) break;
-      p *= xr;
-      s0 += A[k - 1] * p;
-      s1 += B[k - 1] * p;
+      s0 += A[k - 1] * powi(xr, k);
+    }
+    for (int k = 1; k <= 12; ++k) {
+      if (k > k0) break;
+      s1 += B[k - 1] * powi(xr, k);
     }
     bi0 = ca * s0;
     bi1 = ca * s1;
@@ -323,18 +348,15 @@ __device__ inline void d_ik01a(double x, double& bk0, double& bk1) {
     const double A1[8] = {0.125, 0.2109375, 1.0986328125, 1.1775970458984e01, 2.1461706161499e02,
                           5.9511522710323e03, 2.3347645606175e05, 1.2312234987631e07};
     const double xr2 = 1.0 / x2;
-    double p = 1.0, s = 1.0;
-    for (int k = 0; k < 8; ++k) {
-      p *= xr2;
-      s += A1[k] * p;
-    }
+    double s = 1.0;
+    for (int k = 0; k < 8; ++k) s += A1[k] * powi(xr2, k + 1);
     bk0 = 0.5 / x * s / bi0;
   }
   bk1 = (1.0 / x - bi1 * bk0) / bi0;
 }
 
 // JY01B :663-736
-__device__ inline void d_jy01b(double x, double& bj0, double& bj1, double& by0, double& by1) {
+HGD inline void d_jy01b(double x, double& bj0, double& bj1, double& by0, double& by1) {
   if (x == 0.0) { bj0 = 1.0; bj1 = 0.0; by0 = -1.0e+300; by1 = -1.0e+300; return; }
   if (x <= 4.0) {
     const double t = x / 4.0, t2 = t * t;
@@ -369,7 +391,7 @@ __device__ inline void d_jy01b(double x, double& bj0, double& bj1, double& by0, 
 
 // Wynn epsilon algorithm, Limes FinGrnExtSubs.f90:370-503.  s[0..n] is
 // overwritten; a[] is caller scratch of n+1 entries.
-__device__ inline double d_limes(int n, double* s, double* a) {
+HGD inline double d_limes(int n, double* s, double* a) {
   double a_max = 0.0, rl = s[n];
   for (int i = 0; i <= n; ++i) a[i] = 0.0;
   for (int k = 1;; ++k) {
@@ -390,7 +412,7 @@ __device__ inline double d_limes(int n, double* s, double* a) {
 }
 
 // Pidcock's image-source sums IMGS / DGSR / DGSZ (FinGreen3D.f90:908-1102).
-__device__ inline void d_imgs_all(double r, double zf, double zp, double h, double& gs, double& gr,
+HGD inline void d_imgs_all(double r, double zf, double zp, double h, double& gs, double& gr,
                                   double& gz) {
   // AMN(M,N), M = 0..4 (rows), N = 0..4
   const double AMN[5][5] = {{0.0, 0.05051418, 0.00230838, 0.00012934, 0.00000913},
@@ -403,18 +425,19 @@ __device__ inline void d_imgs_all(double r, double zf, double zp, double h, doub
   for (int l = -1; l <= 1; ++l) {
     const double za = t2 + 2.0 * l, zb = t3 + 2.0 * l;
     const double ra = sqrt(t1 * t1 + za * za), rb = sqrt(t1 * t1 + zb * zb);
-    const double ia = 1.0 / ra, ib = 1.0 / rb, ia3 = ia * ia * ia, ib3 = ib * ib * ib;
-    s1 += ia + ib;
-    s1r += t1 * ia3 + t1 * ib3;
-    s1z += za * ia3 + zb * ib3;
+    const double ra3 = ra * ra * ra, rb3 = rb * rb * rb;
+    s1 = s1 + 1.0 / ra + 1.0 / rb;
+    s1r = s1r + t1 / ra3 + t1 / rb3;
+    s1z = s1z + za / ra3 + zb / rb3;
   }
-  // powers t^(2m), t^(2m-1)
+  // real powers t^(2m), t^(2m-1) as in the reference (pow with a real exponent)
   double p1[5], p2[5], p3[5], q2[5], q3[5], pr1[5];
-  const double t12 = t1 * t1, t22 = t2 * t2, t32 = t3 * t3;
-  p1[0] = 1.0; p2[0] = 1.0; p3[0] = 1.0;
-  for (int k = 1; k < 5; ++k) { p1[k] = p1[k - 1] * t12; p2[k] = p2[k - 1] * t22; p3[k] = p3[k - 1] * t32; }
-  pr1[0] = 0.0; q2[0] = 0.0; q3[0] = 0.0;
-  for (int k = 1; k < 5; ++k) { pr1[k] = p1[k - 1] * t1; q2[k] = p2[k - 1] * t2; q3[k] = p3[k - 1] * t3; }
+  for (int k = 0; k < 5; ++k) {
+    p1[k] = pow(t1, 2.0 * k); p2[k] = pow(t2, 2.0 * k); p3[k] = pow(t3, 2.0 * k);
+    pr1[k] = k ? pow(t1, 2.0 * k - 1.0) : 0.0;
+    q2[k] = k ? pow(t2, 2.0 * k - 1.0) : 0.0;
+    q3[k] = k ? pow(t3, 2.0 * k - 1.0) : 0.0;
+  }
   double s2 = 0.0, s2r = 0.0, s2z = 0.0;
   for (int m = 0; m <= 4; ++m)
     for (int n = 0; n <= 4; ++n) {
@@ -429,7 +452,7 @@ __device__ inline void d_imgs_all(double r, double zf, double zp, double h, doub
 }
 
 // Subtraction of the Rankine pair shared by EIGEN / EIGENE / PIDCOCK.
-__device__ __forceinline__ void d_sub_rankine(double r, double zf, double zp, double& g0, double& g1,
+HGD inline void d_sub_rankine(double r, double zf, double zp, double& g0, double& g1,
                                               double& g2) {
   const double sr = sqrt(r * r + (zf - zp) * (zf - zp)), sr1 = sqrt(r * r + (zf + zp) * (zf + zp));
   g0 -= (1.0 / sr + 1.0 / sr1);
@@ -446,15 +469,18 @@ struct FinState {
 
 // Imaginary (propagating) part shared by the three series methods:
 // P0 (i J0 - Y0) etc. of EIGEN/EIGENE/PIDCOCK.
-__device__ __forceinline__ void d_prop_part(const FinState& s, double r, double zf, double zp, double g[6],
+HGD inline void d_prop_part(const FinState& s, double r, double zf, double zp, double g[6],
                                             bool pid) {
   const double wk = s.wk, h = s.h;
   const double p0 = HG_PI / s.nm0 * cosh(wk * (zf + h)) * cosh(wk * (zp + h));
-  const double dp0 = HG_PI / s.nm0 * sinh(wk * (zf + h)) * cosh(wk * (zp + h)) * wk;
+  // DP0 carries WK inside (PIDCOCK :601) or outside (EIGEN :317, EIGENE :442);
+  // kept in the reference's order so the rounding matches.
+  const double dp0 = pid ? wk * HG_PI / s.nm0 * sinh(wk * (zf + h)) * cosh(wk * (zp + h))
+                         : wk * (HG_PI / s.nm0 * sinh(wk * (zf + h)) * cosh(wk * (zp + h)));
   double j0, j1, y0, y1;
   d_jy01b(wk * r, j0, j1, y0, y1);
   g[0] = -p0 * y0;  g[1] = p0 * j0;
-  g[2] = wk * p0 * y1; g[3] = -wk * p0 * j1;
+  g[2] = wk * p0 * y1; g[3] = -(wk * p0) * j1;
   g[4] = -dp0 * y0; g[5] = dp0 * j0;
   if (pid) {
     g[0] += 2.0 / h * (0.5772156649015328 + log(r / 4.0 / h));
@@ -463,7 +489,7 @@ __device__ __forceinline__ void d_prop_part(const FinState& s, double r, double 
 }
 
 // EIGEN (R/h >= 0.5), FinGreen3D.f90:281-362.  g = [re0, im0, re1, im1, re2, im2]
-__device__ inline void d_eigen(const FinState& s, double r, double zf, double zp, double g[6]) {
+HGD inline void d_eigen(const FinState& s, double r, double zf, double zp, double g[6]) {
   d_prop_part(s, r, zf, zp, g, false);
   const double h = s.h;
   for (int i = 2; i <= 10; ++i) {
@@ -482,7 +508,7 @@ __device__ inline void d_eigen(const FinState& s, double r, double zf, double zp
 }
 
 // EIGENE (0.05 <= R/h < 0.5), :413-506, and PIDCOCK (0.0005 <= R/h < 0.05), :558-660.
-__device__ inline void d_series_eps(const FinState& s, double r, double zf, double zp, double g[6],
+HGD inline void d_series_eps(const FinState& s, double r, double zf, double zp, double g[6],
                                     bool pid) {
   double gs[101], gr[101], gz[101], scratch[101];
   const double h = s.h, v = s.v, rhp = fabs(r / h);
@@ -538,7 +564,7 @@ struct LintonPar {
 };
 
 // Integrands G1/G2/G3 (:1904-2057) of the deep-water-like correction.
-__device__ inline double d_gfun(const LintonPar& p, double t, int tag) {
+HGD inline double d_gfun(const LintonPar& p, double t, int tag) {
   if (fabs(t) < 1.0e-8) return 0.0;
   const double val[4] = {-p.zp - p.zf, 2.0 * p.h - p.zp + p.zf, 2.0 * p.h + p.zp - p.zf,
                          4.0 * p.h + p.zp + p.zf};
@@ -556,23 +582,23 @@ __device__ inline double d_gfun(const LintonPar& p, double t, int tag) {
   return ex * sum / t;
 }
 // Integrands F1/F2 (:1795-1880) of the expansion coefficients.
-__device__ __forceinline__ double d_ffun(double r, double wvn, int no, double t, int tag) {
+HGD inline double d_ffun(double r, double wvn, int no, double t, int tag) {
   if (fabs(t) < 1.0e-8) return 0.0;
   const double e = (no == 1) ? exp(-r * r / 4.0 / t + wvn * wvn * t) : exp(-r * r / 4.0 / t - wvn * wvn * t);
   return tag == 1 ? e / 4.0 / HG_PI / t : -r * e / 8.0 / HG_PI / (t * t);
 }
 
-__constant__ double c_xgq[7] = {-0.949107912342759, -0.741531185599394, -0.405845151377397, 0.0,
+HGD_TABLE double c_xgq[7] = {-0.949107912342759, -0.741531185599394, -0.405845151377397, 0.0,
                                 0.405845151377397, 0.741531185599394, 0.949107912342759};
-__constant__ double c_wgq[7] = {0.129484966168870, 0.279705391489277, 0.381830050505119,
+HGD_TABLE double c_wgq[7] = {0.129484966168870, 0.279705391489277, 0.381830050505119,
                                 0.417959183673469, 0.381830050505119, 0.279705391489277,
                                 0.129484966168870};
-__constant__ double c_xkq[15] = {-0.991455371120813, -0.949107912342759, -0.864864423359769,
+HGD_TABLE double c_xkq[15] = {-0.991455371120813, -0.949107912342759, -0.864864423359769,
                                  -0.741531185599394, -0.586087235467691, -0.405845151377397,
                                  -0.207784955007898, 0.0, 0.207784955007898, 0.405845151377397,
                                  0.586087235467691, 0.741531185599394, 0.864864423359769,
                                  0.949107912342759, 0.991455371120813};
-__constant__ double c_wkq[15] = {0.022935322010529, 0.063092092629979, 0.104790010322250,
+HGD_TABLE double c_wkq[15] = {0.022935322010529, 0.063092092629979, 0.104790010322250,
                                  0.140653259715525, 0.169004726639267, 0.190350578064785,
                                  0.204432940075298, 0.209482141084728, 0.204432940075298,
                                  0.190350578064785, 0.169004726639267, 0.140653259715525,
@@ -582,7 +608,7 @@ __constant__ double c_wkq[15] = {0.022935322010529, 0.063092092629979, 0.1047900
 // explicit stack: an interval is split while (200|K-G|)^1.5 > eps and it is
 // wider than eps.  kind 0 integrates d_gfun(tag), kind 1 d_ffun(no, tag).
 template <int KIND>
-__device__ inline double d_aquad(const LintonPar& lp, double r, double wvn, int no, double a, double b,
+HGD inline double d_aquad(const LintonPar& lp, double r, double wvn, int no, double a, double b,
                                  double eps, int tag, int* status) {
   const int kMaxStack = 64;
   double sa[kMaxStack], sb[kMaxStack];
@@ -623,7 +649,7 @@ __device__ inline double d_aquad(const LintonPar& lp, double r, double wvn, int 
 }
 
 // SA0 / DSA0 (:1389-1524): series for the m=0 coefficient and its R-derivative.
-__device__ inline void d_sa0(double r, double pa, double wk, double& sa, double& dsa, int* status) {
+HGD inline void d_sa0(double r, double pa, double wk, double& sa, double& dsa, int* status) {
   const double ga = 0.5772156649015328, eps = SPD(1.e-6);
   const double x = (r / pa) * (r / pa), ex = exp(-x), lg = log(wk * r / 2.0);
   // SA0 uses E_{n+1}(x), DSA0 uses E_n(x), n = 1, 2, ...
@@ -659,7 +685,7 @@ __device__ inline void d_sa0(double r, double pa, double wk, double& sa, double&
 }
 
 // SAM / DSAM (:1575-1693) for m >= 1.
-__device__ inline void d_sam(double r, double pa, double wvn, double& sa, double& dsa, int* status) {
+HGD inline void d_sam(double r, double pa, double wvn, double& sa, double& dsa, int* status) {
   const double eps = SPD(1.e-6);
   const double x = (wvn * pa / 2.0) * (wvn * pa / 2.0), ex = exp(-x);
   double e = d_e1xa(x);  // E_{n+1} for n = 0
@@ -688,7 +714,7 @@ __device__ inline void d_sam(double r, double pa, double wvn, double& sa, double
   dsa = ds / 4.0 / HG_PI;
 }
 
-__device__ inline void d_linton(const FinState& st, double r, double zf, double zp, double g[6]) {
+HGD inline void d_linton(const FinState& st, double r, double zf, double zp, double g[6]) {
   const double eps = SPD(1.e-6), v = st.v, wk = st.wk, h = st.h;
   double a;
   if (v < 0.02) a = 3324.2 * (v * v * v) - 258.89 * (v * v) + 8.3958 * v + 1.3208;
@@ -808,7 +834,7 @@ __device__ inline void d_linton(const FinState& st, double r, double zf, double 
 }
 
 // FINGREEN3D (FinGreen3D.f90:81-155) for source (xq,yq,zq) and field (xp,yp,zp).
-__device__ inline void fin_green(const FinState& st, double xq, double yq, double zq, double xp,
+HGD inline void fin_green(const FinState& st, double xq, double yq, double zq, double xp,
                                  double yp, double zp, int flag, double2 g[4]) {
   const double xpq = xq - xp, ypq = yq - yp, zpq = zq + zp;
   const double rr = sqrt(xpq * xpq + ypq * ypq);

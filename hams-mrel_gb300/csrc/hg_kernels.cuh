@@ -18,6 +18,12 @@ template <typename OUT>
 cudaError_t launch_green_fill(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
                               const FinState& fs, bool deep, int grn_kind, OUT* A, OUT* S, long lda, int* status);
 
+template <typename OUT>
+cudaError_t launch_green_fill_fin(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
+                                  const FinState& fs, int grn_kind, OUT* A, OUT* S, long lda, int* status);
+cudaError_t launch_green_points_fin(cudaStream_t st, int npts, const double* pts, const int* flags, const FinState& fs,
+                                    double* out);
+
 cudaError_t launch_incident(cudaStream_t st, int n, const double* xyz_p, const double* dxyz_p, int nbeta,
                             const double* betas, double v, double wk, double w1, double h, double2* w);
 

@@ -22,7 +22,8 @@ EXPORTS = [
     "hg_default_opts", "hg_create", "hg_destroy", "hg_last_error", "hg_set_mesh", "hg_set_frequency",
     "hg_fill_factor", "hg_solve_radiation", "hg_solve_all_headings", "hg_solve_diffraction", "hg_forces",
     "hg_solve_frequency", "hg_keep_matrices", "hg_get_matrix", "hg_green_points", "hg_refine_info",
-    "hg_stage_times", "hg_dispersion", "hg_wave_properties", "hg_panel_geometry",
+    "hg_stage_times", "hg_dispersion", "hg_wave_properties", "hg_panel_geometry", "hg_mark", "hg_elapsed",
+    "hg_bench_gemm",
 ]
 
 
@@ -78,6 +79,8 @@ def load(build_if_missing: bool = True):
     L.hg_green_points.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p]
     L.hg_refine_info.argtypes = [c_void_p, P(c_int), P(c_double)]
     L.hg_stage_times.argtypes = [c_void_p, P(ctypes.c_float)]
+    L.hg_mark.argtypes = [c_void_p, c_int]
+    L.hg_elapsed.argtypes = [c_void_p, c_int, c_int, P(ctypes.c_float)]
     L.hg_dispersion.argtypes = [c_double, c_double, c_int, c_void_p]
     L.hg_wave_properties.argtypes = [c_int, c_double, c_double, c_int, P(c_double), P(c_double), P(c_double),
                                      c_void_p]
@@ -244,6 +247,14 @@ class Solver:
         s = ctypes.c_int(); r = ctypes.c_double()
         self.L.hg_refine_info(self.h, ctypes.byref(s), ctypes.byref(r))
         return s.value, r.value
+
+    def mark(self, slot):
+        self._check(self.L.hg_mark(self.h, slot))
+
+    def elapsed_ms(self, s0, s1):
+        ms = ctypes.c_float()
+        self._check(self.L.hg_elapsed(self.h, s0, s1, ctypes.byref(ms)))
+        return ms.value
 
     def stage_times(self):
         a = (ctypes.c_float * 4)()

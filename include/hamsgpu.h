@@ -153,6 +153,18 @@ int hg_panel_geometry(int n, int ntnd, const double *nodes, const int *ncon, con
 /* Refinement sweeps taken and final relative residual of the last mixed-form solve. */
 int hg_refine_info(const hg_ctx *ctx, int *sweeps, double *residual);
 
+/* CUDA events on the context's stream, for callers that time a sequence of
+ * calls on the device: hg_mark records event slot (0..15); hg_elapsed waits
+ * for the later one and returns the milliseconds between two slots. */
+int hg_mark(hg_ctx *ctx, int slot);
+int hg_elapsed(hg_ctx *ctx, int slot0, int slot1, float *ms);
+
+/* Average device time (ms) of the library's complex GEMM kernel
+ * C = C - A B on an m x n x k problem (precision: 0 complex128, 1 complex64),
+ * over iters launches on scratch buffers; used to report the roofline of the
+ * LU trailing update. */
+int hg_bench_gemm(hg_ctx *ctx, int precision, int m, int n, int k, int iters, float *ms_per_launch);
+
 /* Time (milliseconds, CUDA events on the context stream) of the stages of the
  * last hg_solve_frequency: [0] fill, [1] LU, [2] solves and refinement, [3] forces. */
 int hg_stage_times(const hg_ctx *ctx, float *ms4);

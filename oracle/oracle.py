@@ -53,13 +53,58 @@ def build(force: bool = False) -> str:
 
 
 _LIB = None
+FMA_LIB_PATH = os.path.join(HERE, "_build", "liboracle_fma.so")
+
+
+def build_fma_variant() -> str:
+    """The same oracle compiled with fused multiply-add contraction.
+
+    The finite-depth Green function of the reference extrapolates its series
+    with Wynn's epsilon algorithm (src/FinGrnExtSubs.f90:370-503), which
+    amplifies last-bit differences.  Comparing the oracle with this variant
+    measures how far the reference's own results move under a different but
+    equally valid rounding; the GPU parity tests of the finite-depth path are
+    held to that spread."""
+    srcs = [os.path.join(HERE, s) for s in SOURCES]
+    if os.path.exists(FMA_LIB_PATH) and os.path.getmtime(FMA_LIB_PATH) >= max(os.path.getmtime(s) for s in srcs):
+        return FMA_LIB_PATH
+    os.makedirs(os.path.dirname(FMA_LIB_PATH), exist_ok=True)
+    tmp = FMA_LIB_PATH + f".tmp{os.getpid()}"
+    arch = ["-mfma"] if os.uname().machine == "x86_64" else []
+    subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=fast"] + arch + ["-o", tmp] + srcs
+                   + ["-lm"], check=True)
+    os.replace(tmp, FMA_LIB_PATH)
+    return FMA_LIB_PATH
+
+
+class use_library:
+    """Context manager: run the oracle functions with another build of liboracle."""
+
+    def __init__(self, path):
+        self.path = path
+
+    def __enter__(self):
+        global _LIB
+        self.saved = _LIB
+        _LIB = _configure(ctypes.CDLL(self.path))
+        return self
+
+    def __exit__(self, *exc):
+        global _LIB
+        _LIB = self.saved
+        return False
 
 
 def lib():
     global _LIB
     if _LIB is None:
         build()
-        L = ctypes.CDLL(LIB_PATH)
+        _LIB = _configure(ctypes.CDLL(LIB_PATH))
+    return _LIB
+
+
+def _configure(L):
+    if True:
         dp = ctypes.POINTER(ctypes.c_double)
         ip = ctypes.POINTER(ctypes.c_int)
         L.or_assemble.argtypes = [ctypes.c_void_p, ctypes.c_double, dp, ctypes.c_int, ctypes.c_double,
@@ -85,8 +130,7 @@ def lib():
         L.or_fingreen_region.restype = ctypes.c_int
         L.or_vinp.argtypes = [ctypes.c_double] * 8
         L.or_vinp.restype = ctypes.c_double * 2
-        _LIB = L
-    return _LIB
+    return L
 
 
 def _dp(a):
