@@ -7,6 +7,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -718,3 +719,66 @@ int hg_stage_times(const hg_ctx* c, float* ms4) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Green-function point evaluation without device allocation.
+//
+// hg_green_points allocates device staging buffers on every call.  Some
+// callers cannot allocate device memory once their run has started: a
+// Fortran driver evaluating the wave field at many points inside its
+// frequency loop under a fixed memory budget, or a serving process whose
+// device memory is carved up once at start-up.  This variant stages the
+// points, flags and results in one fixed array in device global memory
+// that the library defines at file scope, so a call performs no cudaMalloc
+// or cudaFree.  Every GPU that loads the library holds the array (7.25 MiB)
+// until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kNoAllocMaxPoints = HG_NOALLOC_MAX_POINTS;
+// Layout: [6 * P source/field coordinates][8 * P results][P flags as ints].
+constexpr size_t kNoAllocDoubles = (size_t)kNoAllocMaxPoints * (6 + 8) + (size_t)kNoAllocMaxPoints / 2;
+static __device__ __align__(256) double g_points_scratch[kNoAllocDoubles];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+double* g_scratch_addr[kMaxDevices] = {};
+
+// Device address of g_points_scratch on the current device, looked up once
+// per device (the host-side symbol is only a stand-in for it).
+cudaError_t scratch_address(int dev, double** out) {
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_points_scratch);
+    if (e != cudaSuccess) return e;
+    g_scratch_addr[dev] = static_cast<double*>(p);
+  }
+  *out = g_scratch_addr[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" int hg_green_points_noalloc(hg_ctx* c, int npts, const double* pts, const int* flags, double* out) {
+  if (!c) return -1;
+  if (npts <= 0) return fail(c, -2, "npts must be positive");
+  if (npts > kNoAllocMaxPoints)
+    return fail(c, -2, "npts %d exceeds the %d points of the fixed scratch array; split the call", npts,
+                kNoAllocMaxPoints);
+  if (!pts || !flags || !out) return fail(c, -3, "NULL array");
+  if (!c->freq_set) return fail(c, HG_ERR_STATE, "hg_set_frequency must come first");
+  CK(cudaSetDevice(c->o.device));
+  double* base = nullptr;
+  CK(scratch_address(c->o.device, &base));
+  double* d_pts = base;
+  double* d_out = base + (size_t)6 * kNoAllocMaxPoints;
+  int* d_flags = reinterpret_cast<int*>(base + (size_t)14 * kNoAllocMaxPoints);
+  CK(cudaMemcpyAsync(d_pts, pts, (size_t)6 * npts * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(d_flags, flags, (size_t)npts * sizeof(int), cudaMemcpyHostToDevice, c->st));
+  CK(hg::launch_green_points(c->st, npts, d_pts, d_flags, fin_state(c), c->h < 0.0, d_out));
+  CK(cudaMemcpyAsync(out, d_out, (size_t)8 * npts * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return check_status(c);
+}

@@ -23,7 +23,7 @@ EXPORTS = [
     "hg_fill_factor", "hg_solve_radiation", "hg_solve_all_headings", "hg_solve_diffraction", "hg_forces",
     "hg_solve_frequency", "hg_keep_matrices", "hg_get_matrix", "hg_green_points", "hg_refine_info",
     "hg_stage_times", "hg_dispersion", "hg_wave_properties", "hg_panel_geometry", "hg_mark", "hg_elapsed",
-    "hg_bench_gemm",
+    "hg_bench_gemm", "hg_green_points_noalloc",
 ]
 
 
@@ -79,6 +79,7 @@ def load(build_if_missing: bool = True):
     L.hg_green_points.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p]
     L.hg_refine_info.argtypes = [c_void_p, P(c_int), P(c_double)]
     L.hg_stage_times.argtypes = [c_void_p, P(ctypes.c_float)]
+    L.hg_green_points_noalloc.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p]
     L.hg_mark.argtypes = [c_void_p, c_int]
     L.hg_elapsed.argtypes = [c_void_p, c_int, c_int, P(ctypes.c_float)]
     L.hg_dispersion.argtypes = [c_double, c_double, c_int, c_void_p]
@@ -241,6 +242,14 @@ class Solver:
         fl = np.ascontiguousarray(flags, dtype=np.int32)
         out = np.zeros((len(fl), 8))
         self._check(self.L.hg_green_points(self.h, len(fl), _ptr(p), _ptr(fl), _ptr(out)))
+        return out[:, 0::2] + 1j * out[:, 1::2]
+
+    def green_points_noalloc(self, pts, flags):
+        """hg_green_points through the entry point that allocates no device memory."""
+        p = np.ascontiguousarray(pts, dtype=np.float64)
+        fl = np.ascontiguousarray(flags, dtype=np.int32)
+        out = np.zeros((len(fl), 8))
+        self._check(self.L.hg_green_points_noalloc(self.h, len(fl), _ptr(p), _ptr(fl), _ptr(out)))
         return out[:, 0::2] + 1j * out[:, 1::2]
 
     def refine_info(self):

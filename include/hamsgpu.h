@@ -150,6 +150,24 @@ int hg_wave_properties(int inft, double value, double h, int nk, double *v, doub
 int hg_panel_geometry(int n, int ntnd, const double *nodes, const int *ncon, const int *ncn, const double *xr,
                       double *xyz_p, double *ds, double *pnsz, double *dxyz_p);
 
+/* hg_green_points without device allocation.  No counterpart in the
+ * reference.  For callers that cannot allocate device memory once their run
+ * is under way (a driver loop evaluating the wave field under a fixed memory
+ * budget, a server that carves up device memory at start-up): the points,
+ * flags and results are staged in one fixed array the library keeps in
+ * device global memory (7.25 MiB on every GPU that loads the library, held
+ * until exit), so the call makes no cudaMalloc / cudaFree.
+ *   - npts may not exceed HG_NOALLOC_MAX_POINTS; larger calls return -2 with
+ *     a message in hg_last_error (split them).
+ *   - The first call on a device looks up the array's device address; make
+ *     that first call before any stream capture.
+ *   - All calls on a device share the array, and each call overwrites the
+ *     part it uses: calls that overlap on the GPU (several host threads or
+ *     contexts at once) race and must be serialised by the caller.
+ * Arguments, results and errors are those of hg_green_points. */
+#define HG_NOALLOC_MAX_POINTS 65536
+int hg_green_points_noalloc(hg_ctx *ctx, int npts, const double *pts, const int *flags, double *out);
+
 /* Refinement sweeps taken and final relative residual of the last mixed-form solve. */
 int hg_refine_info(const hg_ctx *ctx, int *sweeps, double *residual);
 
