@@ -59,7 +59,7 @@ struct hg_ctx {
   bool freq_set = false;
   DevBuf<double> wvn;
   // matrices
-  DevBuf<double2> A, S, C, A64, B, X, R, R2, W, part, exfc;
+  DevBuf<double2> A, S, C, A64, B, X, R, R2, W, part, exfc, gws;  // gws: split-K GEMM workspace
   DevBuf<float2> Af, Sf, Cf, Bf;
   DevBuf<double> amas, bdmp;
   int irsp = 0;
@@ -132,6 +132,7 @@ int ensure_rhs(hg_ctx* c, int nbeta) {
   CK(c->W.ensure((size_t)c->n * (nbeta > 0 ? nbeta : 1)));
   CK(c->part.ensure(hg::rhs_work_bytes(c->n, c->tn, c->nbody, nbeta) / sizeof(double2) + 1));
   CK(c->betas.ensure(nbeta > 0 ? nbeta : 1));
+  CK(c->gws.ensure((size_t)16 * c->tn * nc));
   if (mixed(c)) {
     CK(c->R.ensure((size_t)c->tn * nc));
     CK(c->R2.ensure((size_t)c->n * nc));
@@ -141,6 +142,9 @@ int ensure_rhs(hg_ctx* c, int nbeta) {
   }
   return 0;
 }
+
+// Split-K workspace of the context (for the tall-skinny residual products).
+#define WS(c) (void*)(c)->gws.p, (c)->gws.cap * sizeof(double2)
 
 // Column norms of a complex128 block: out[k] = max over rows |re|+|im|.
 __global__ void k_colmax(int rows, const double2* __restrict__ M, long ld, double* __restrict__ out) {
@@ -171,7 +175,7 @@ int solve_cols(hg_ctx* c, int c0, int c1) {
   double2* Xc = c->X.p + (size_t)c0 * n;
   if (!mixed(c)) {
     if (c->irsp == 1) {
-      CK(hg::gemm<double>(c->st, true, n, nc, tn, one, c->A.p, tn, Bc, tn, zero, Xc, n));
+      CK(hg::gemm<double>(c->st, true, n, nc, tn, one, c->A.p, tn, Bc, tn, zero, Xc, n, WS(c)));
       CK(hg::getrs<double>(c->st, n, nc, c->C.p, n, c->ipiv.p, Xc, n));
     } else {
       CK(cudaMemcpy2DAsync(Xc, (size_t)n * sizeof(double2), Bc, (size_t)tn * sizeof(double2), (size_t)n * sizeof(double2),
@@ -187,7 +191,7 @@ int solve_cols(hg_ctx* c, int c0, int c1) {
   const long ldlu = (c->irsp == 1) ? n : tn;
   double2* Rh = c->R2.p + (size_t)c0 * n;  // n x nc right-hand side of the square system
   float2* Bf = c->Bf.p + (size_t)c0 * n;
-  if (c->irsp == 1) CK(hg::gemm<double>(c->st, true, n, nc, tn, one, c->A64.p, tn, Bc, tn, zero, Rh, n));
+  if (c->irsp == 1) CK(hg::gemm<double>(c->st, true, n, nc, tn, one, c->A64.p, tn, Bc, tn, zero, Rh, n, WS(c)));
   else CK(cudaMemcpy2DAsync(Rh, (size_t)n * sizeof(double2), Bc, (size_t)tn * sizeof(double2), (size_t)n * sizeof(double2),
                             nc, cudaMemcpyDeviceToDevice, c->st));
   // norms of the square-system right-hand side
@@ -209,12 +213,12 @@ int solve_cols(hg_ctx* c, int c0, int c1) {
       double2* R1 = c->R.p + (size_t)c0 * tn;
       CK(cudaMemcpy2DAsync(R1, (size_t)tn * sizeof(double2), Bc, (size_t)tn * sizeof(double2), (size_t)tn * sizeof(double2),
                            nc, cudaMemcpyDeviceToDevice, c->st));
-      CK(hg::gemm<double>(c->st, false, tn, nc, n, mone, c->A64.p, tn, Xc, n, one, R1, tn));
-      CK(hg::gemm<double>(c->st, true, n, nc, tn, one, c->A64.p, tn, R1, tn, zero, Rh, n));
+      CK(hg::gemm<double>(c->st, false, tn, nc, n, mone, c->A64.p, tn, Xc, n, one, R1, tn, WS(c)));
+      CK(hg::gemm<double>(c->st, true, n, nc, tn, one, c->A64.p, tn, R1, tn, zero, Rh, n, WS(c)));
     } else {
       CK(cudaMemcpy2DAsync(Rh, (size_t)n * sizeof(double2), Bc, (size_t)tn * sizeof(double2), (size_t)n * sizeof(double2),
                            nc, cudaMemcpyDeviceToDevice, c->st));
-      CK(hg::gemm<double>(c->st, false, n, nc, n, mone, c->A64.p, tn, Xc, n, one, Rh, n));
+      CK(hg::gemm<double>(c->st, false, n, nc, n, mone, c->A64.p, tn, Xc, n, one, Rh, n, WS(c)));
     }
     k_colmax<<<nc, 256, 0, c->st>>>(n, Rh, n, nb.p + nc);
     CK(cudaMemcpyAsync(rnorm.data(), nb.p + nc, nc * sizeof(double), cudaMemcpyDeviceToHost, c->st));
@@ -268,7 +272,7 @@ void hg_default_opts(hg_opts* o) {
   o->precision = HG_PREC_FP64;
   o->grn_kind = 8;
   o->max_refine = 10;
-  o->refine_tol = 1e-12;
+  o->refine_tol = 1e-10;
   o->rho = 1000.0;
   o->g = 9.80665;
 }
@@ -305,7 +309,7 @@ void hg_destroy(hg_ctx* c) {
   for (auto* b : dbs) b->release();
   DevBuf<int>* ibs[] = {&c->ncon, &c->ncn, &c->body_of, &c->body_start, &c->body_end, &c->ipiv, &c->status, &c->info};
   for (auto* b : ibs) b->release();
-  DevBuf<double2>* zbs[] = {&c->A, &c->S, &c->C, &c->A64, &c->B, &c->X, &c->R, &c->R2, &c->W, &c->part, &c->exfc};
+  DevBuf<double2>* zbs[] = {&c->A, &c->S, &c->C, &c->A64, &c->B, &c->X, &c->R, &c->R2, &c->W, &c->part, &c->exfc, &c->gws};
   for (auto* b : zbs) b->release();
   DevBuf<float2>* cbs[] = {&c->Af, &c->Sf, &c->Cf, &c->Bf};
   for (auto* b : cbs) b->release();
@@ -459,8 +463,12 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
     CK(c->Af.ensure((size_t)tn * n));
     CK(c->Sf.ensure((size_t)tn * n));
     CK(c->A64.ensure((size_t)tn * n));
-    CK(hg::launch_green_fill<float2>(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, deep, c->o.grn_kind, c->Af.p, c->Sf.p, tn,
-                                     c->status.p));
+    const bool special = std::fabs(c->v) < (double)1.e-8f || std::fabs(c->v + 1.0) < (double)1.e-8f;
+    if (deep && !special && c->o.grn_kind == 8)
+      CK(hg::launch_green_fill_mixed(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, c->v, c->Af.p, c->Sf.p, tn, c->status.p));
+    else
+      CK(hg::launch_green_fill<float2>(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, deep, c->o.grn_kind, c->Af.p,
+                                       c->Sf.p, tn, c->status.p));
     CK(hg::convert_c2z(c->st, (long)tn * n, c->Af.p, c->A64.p));
     CK(cudaEventRecord(c->ev[1], c->st));
     if (irsp == 1) {

@@ -13,6 +13,8 @@
 #include "hg_kernels.cuh"
 #include "hg_tma.cuh"
 #include "hg_fill_kernel.cuh"
+#include "hg_green32.cuh"
+#include <cmath>
 
 namespace hg {
 
@@ -109,6 +111,154 @@ cudaError_t launch_green_fill(cudaStream_t st, const double* rec, const double* 
   if (!deep) return launch_green_fill_fin<OUT>(st, rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, status);
   dim3 grid((tn + FILL_ROWS - 1) / FILL_ROWS, (n + FILL_COLS - 1) / FILL_COLS);
   k_green_fill<true, OUT><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, status);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Mixed form, deep water: the pair kernel in single precision.
+//   - FLAG (dist <= 50 PNSZ) is decided in double exactly as in the plain
+//     kernel, so both forms integrate the same pairs analytically;
+//   - pairs closer than 4 PNSZ (self and adjacent panels) keep the
+//     double-precision Newman integral;
+//   - coordinate differences are formed in double, everything else (Green
+//     function, far Newman integrals, assembly) in single precision.
+// ---------------------------------------------------------------------------
+// Monomial coefficients in rho of the Wu-Noblesse local-flow polynomials
+// A, B, C, D (InfGreen_Appr.f90:298-416) and A', B', C' (:494-580).
+static const double kWuPoly[7][10] = {
+    {1.21, -13.328, 215.896, -1763.96, 8418.94, -24314.21, 42002.57, -41592.9, 21859.0, -4838.6},
+    {0.938, 5.373, -67.92, 796.534, -4780.77, 17137.74, -36618.81, 44894.06, -29030.24, 7671.22},
+    {1.268, -9.747, 209.653, -1397.89, 5155.67, -9844.35, 9136.4, -3272.62, 0.0, 0.0},
+    {0.632, -40.97, 667.16, -6072.07, 31127.39, -96293.05, 181856.75, -205690.43, 128170.2, -33744.6},
+    {2.948, -24.53, 249.69, -754.85, -1187.71, 16370.75, -48811.41, 68220.87, -46688.0, 12622.25},
+    {1.11, 2.894, -76.765, 1565.35, -11336.19, 44270.15, -97014.11, 118879.26, -76209.82, 19923.28},
+    {14.19, -148.24, 847.8, -2318.58, 3168.35, -1590.27, 0.0, 0.0, 0.0, 0.0}};
+
+// Chebyshev coefficients (in x = 2 rho - 1) of a degree-9 polynomial in rho.
+static void monomial_to_chebyshev(const double* c, double* t) {
+  double q[kChebTerms] = {0};  // coefficients in x: rho = (x + 1) / 2
+  for (int i = 0; i < kChebTerms; ++i) {
+    // ((x + 1) / 2)^i = 2^-i sum_k binom(i, k) x^k
+    double binom = 1.0, scale = std::ldexp(1.0, -i);
+    for (int k = 0; k <= i; ++k) {
+      q[k] += c[i] * scale * binom;
+      binom = binom * (i - k) / (k + 1);
+    }
+  }
+  double r[kChebTerms + 1] = {0};
+  for (int i = kChebTerms - 1; i >= 0; --i) {
+    // r <- x * r + q_i in the Chebyshev basis: x T0 = T1, x Tn = (T(n+1) + T(n-1)) / 2
+    double s[kChebTerms + 1] = {0};
+    for (int nn = 0; nn < kChebTerms; ++nn) {
+      if (r[nn] == 0.0) continue;
+      if (nn == 0) s[1] += r[0];
+      else { s[nn + 1] += 0.5 * r[nn]; s[nn - 1] += 0.5 * r[nn]; }
+    }
+    s[0] += q[i];
+    for (int nn = 0; nn <= kChebTerms; ++nn) r[nn] = s[nn];
+  }
+  for (int nn = 0; nn < kChebTerms; ++nn) t[nn] = r[nn];
+}
+
+static cudaError_t upload_cheb_constants() {
+  static bool done[64] = {false};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
+  float h[7][kChebTerms];
+  for (int p = 0; p < 7; ++p) {
+    double t[kChebTerms];
+    monomial_to_chebyshev(kWuPoly[p], t);
+    for (int k = 0; k < kChebTerms; ++k) h[p][k] = (float)t[k];
+  }
+  e = cudaMemcpyToSymbol(c_cheb, h, sizeof(h));
+  if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
+  return e;
+}
+
+constexpr int kPanelFloats = 24;  // ui, uj, uk, ksi, eta, l (3+3+3+4+4+4) + nv, ds, n0..n2
+
+__global__ void __launch_bounds__(FILL_ROWS)
+k_green_fill_mixed(const double* __restrict__ rec, const double* __restrict__ fx, int ldf, int n, int tn, float vf,
+                   float2* __restrict__ A, float2* __restrict__ S, long lda, int* status) {
+  __shared__ alignas(128) double tile[FILL_COLS * PR_SIZE];
+  __shared__ alignas(8) uint64_t bar;
+  __shared__ PanelF pfs[FILL_COLS];
+  __shared__ float pds[FILL_COLS][4];  // area, normal
+  const int col0 = blockIdx.y * FILL_COLS;
+  const int ncol = min(FILL_COLS, n - col0);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_expect_tx(&bar, (uint32_t)(ncol * PR_SIZE * sizeof(double)));
+    bulk_g2s(tile, rec + (size_t)col0 * PR_SIZE, (uint32_t)(ncol * PR_SIZE * sizeof(double)), &bar);
+  }
+  __syncthreads();
+  if (!mbar_wait_bounded(&bar, 0, 1L << 24)) {
+    hg_set_status(status, HG_DEV_WAIT_TIMEOUT);
+    mbar_wait_bounded(&bar, 0, 1L << 24);
+    return;
+  }
+  if (threadIdx.x < ncol) {
+    const double* pr = tile + threadIdx.x * PR_SIZE;
+    PanelF& q = pfs[threadIdx.x];
+    for (int k = 0; k < 3; ++k) {
+      q.ui[k] = (float)pr[PR_UI + k]; q.uj[k] = (float)pr[PR_UJ + k]; q.uk[k] = (float)pr[PR_UK + k];
+    }
+    for (int k = 0; k < 4; ++k) {
+      q.ksi[k] = (float)pr[PR_KSI + k]; q.eta[k] = (float)pr[PR_ETA + k]; q.l[k] = (float)pr[PR_L + k];
+    }
+    q.nv = (int)pr[PR_NCN];
+    pds[threadIdx.x][0] = (float)pr[PR_DS];
+    for (int k = 0; k < 3; ++k) pds[threadIdx.x][1 + k] = (float)pr[PR_N + k];
+  }
+  __syncthreads();
+  const int i = blockIdx.x * FILL_ROWS + threadIdx.x;
+  if (i >= tn) return;
+  const double xp = fx[i], yp = fx[i + ldf], zp = fx[i + 2 * (size_t)ldf];
+  for (int jj = 0; jj < ncol; ++jj) {
+    const double* pr = tile + jj * PR_SIZE;
+    const int j = col0 + jj;
+    const double dx = pr[PR_XQ] - xp, dy = pr[PR_XQ + 1] - yp, zq = pr[PR_XQ + 2];
+    const double dist = sqrt(dx * dx + dy * dy + (zp - zq) * (zp - zq));
+    const double flagd = pr[PR_FLAGD];
+    const int flag = (dist <= flagd) ? 1 : 0;
+    float sij = 0.f, d0 = 0.f, d1 = 0.f, d2 = 0.f;
+    if (flag) {
+      if (dist <= 0.08 * flagd) {
+        double s64, e0, e1, e2;
+        newman_pair(pr, xp, yp, zp, s64, e0, e1, e2);
+        sij = (float)s64; d0 = (float)e0; d1 = (float)e1; d2 = (float)e2;
+      } else {
+        newman_pair_f(pfs[jj], (float)(xp - pr[PR_PO]), (float)(yp - pr[PR_PO + 1]), (float)(zp - pr[PR_PO + 2]),
+                      sij, d0, d1, d2);
+      }
+    }
+    float2 g[4];
+    inf_green_f((float)dx, (float)dy, (float)(zp + zq), (float)(zp - zq), vf, flag, g);
+    const float ear = pds[jj][0], n0 = pds[jj][1], n1 = pds[jj][2], n2 = pds[jj][3];
+    float ar, ai, sr;
+    if (flag) {
+      ar = (d0 + g[1].x * ear) * n0 + (d1 + g[2].x * ear) * n1 + (d2 + g[3].x * ear) * n2;
+      ai = (g[1].y * ear) * n0 + (g[2].y * ear) * n1 + (g[3].y * ear) * n2;
+      sr = sij + g[0].x * ear;
+    } else {
+      ar = (g[1].x * n0 + g[2].x * n1 + g[3].x * n2) * ear;
+      ai = (g[1].y * n0 + g[2].y * n1 + g[3].y * n2) * ear;
+      sr = g[0].x * ear;
+    }
+    if (i == j) ar += 6.28318530717959f;
+    A[i + (long)j * lda] = make_float2(ar, ai);
+    S[i + (long)j * lda] = make_float2(sr, g[0].y * ear);
+  }
+}
+
+cudaError_t launch_green_fill_mixed(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
+                                    double v, float2* A, float2* S, long lda, int* status) {
+  cudaError_t e = upload_cheb_constants();
+  if (e != cudaSuccess) return e;
+  dim3 grid((tn + FILL_ROWS - 1) / FILL_ROWS, (n + FILL_COLS - 1) / FILL_COLS);
+  k_green_fill_mixed<<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, (float)v, A, S, lda, status);
   return cudaGetLastError();
 }
 template cudaError_t launch_green_fill<double2>(cudaStream_t, const double*, const double*, int, int, int,

@@ -45,19 +45,29 @@ template <typename R, int BM, int BN, int BK, int TM, int TN, bool TA>
 __global__ void __launch_bounds__((BM / TM) * (BN / TN))
 k_gemm(int m, int n, int k, typename cx<R>::T alpha, const typename cx<R>::T* __restrict__ A, long lda,
        const typename cx<R>::T* __restrict__ B, long ldb, typename cx<R>::T beta,
-       typename cx<R>::T* __restrict__ C, long ldc) {
+       typename cx<R>::T* __restrict__ C, long ldc, int kchunk, typename cx<R>::T* __restrict__ ws) {
+  // Split-K when gridDim.z > 1: this CTA sums k in [z*kchunk, (z+1)*kchunk)
+  // and writes alpha * partial into the z-th m x n slice of ws (no beta).
   typedef typename cx<R>::T T;
   constexpr int TX = BM / TM, TY = BN / TN, NT = TX * TY;
   __shared__ R as_re[BK][BM], as_im[BK][BM], bs_re[BK][BN], bs_im[BK][BN];
   const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  const bool split = gridDim.z > 1;
+  const int kbeg = split ? blockIdx.z * kchunk : 0;
+  const int kend = split ? min(k, kbeg + kchunk) : k;
+  if (split) {
+    C = ws + (long)blockIdx.z * m * n;
+    ldc = m;
+    beta.x = 0; beta.y = 0;
+  }
   R acr[TM][TN], aci[TM][TN];
 #pragma unroll
   for (int i = 0; i < TM; ++i)
 #pragma unroll
     for (int j = 0; j < TN; ++j) { acr[i][j] = 0; aci[i][j] = 0; }
 
-  for (int kk = 0; kk < k; kk += BK) {
+  for (int kk = kbeg; kk < kend; kk += BK) {
 #pragma unroll
     for (int e = tid; e < BM * BK; e += NT) {
       int i, l;
@@ -65,7 +75,7 @@ k_gemm(int m, int n, int k, typename cx<R>::T alpha, const typename cx<R>::T* __
       const int gm = m0 + i, gk = kk + l;
       T v;
       v.x = 0; v.y = 0;
-      if (gm < m && gk < k) v = TA ? A[gk + (long)gm * lda] : A[gm + (long)gk * lda];
+      if (gm < m && gk < kend) v = TA ? A[gk + (long)gm * lda] : A[gm + (long)gk * lda];
       as_re[l][i] = v.x; as_im[l][i] = v.y;
     }
 #pragma unroll
@@ -73,7 +83,7 @@ k_gemm(int m, int n, int k, typename cx<R>::T alpha, const typename cx<R>::T* __
       const int l = e % BK, j = e / BK, gk = kk + l, gn = n0 + j;
       T v;
       v.x = 0; v.y = 0;
-      if (gn < n && gk < k) v = B[gk + (long)gn * ldb];
+      if (gn < n && gk < kend) v = B[gk + (long)gn * ldb];
       bs_re[l][j] = v.x; bs_im[l][j] = v.y;
     }
     __syncthreads();
@@ -119,29 +129,76 @@ k_gemm(int m, int n, int k, typename cx<R>::T alpha, const typename cx<R>::T* __
   }
 }
 
+// C = sum over slices of the split-K partials + beta * C
+template <typename T>
+__global__ void k_splitk_reduce(int m, int n, int slices, const T* __restrict__ ws, T beta, T* __restrict__ C,
+                                long ldc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i >= m) return;
+  T acc;
+  acc.x = 0; acc.y = 0;
+  for (int z = 0; z < slices; ++z) {
+    const T v = ws[(long)z * m * n + i + (long)j * m];
+    acc.x += v.x; acc.y += v.y;
+  }
+  T* c = C + i + (long)j * ldc;
+  if (beta.x != 0 || beta.y != 0) {
+    const T o = *c;
+    acc.x += beta.x * o.x - beta.y * o.y;
+    acc.y += beta.x * o.y + beta.y * o.x;
+  }
+  *c = acc;
+}
+
+constexpr int kNumSMs = 152;
+
 template <typename R, int BM, int BN, int BK, int TM, int TN>
 static cudaError_t launch_gemm(cudaStream_t st, bool transa, int m, int n, int k, typename cx<R>::T alpha,
                                const typename cx<R>::T* A, long lda, const typename cx<R>::T* B, long ldb,
-                               typename cx<R>::T beta, typename cx<R>::T* C, long ldc) {
+                               typename cx<R>::T beta, typename cx<R>::T* C, long ldc, void* ws, size_t ws_bytes) {
+  typedef typename cx<R>::T T;
   if (m <= 0 || n <= 0) return cudaSuccess;
-  dim3 grid((m + BM - 1) / BM, (n + BN - 1) / BN);
+  dim3 grid((m + BM - 1) / BM, (n + BN - 1) / BN, 1);
   const int nt = (BM / TM) * (BN / TN);
-  if (transa) k_gemm<R, BM, BN, BK, TM, TN, true><<<grid, nt, 0, st>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
-  else k_gemm<R, BM, BN, BK, TM, TN, false><<<grid, nt, 0, st>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  // Tall-skinny products (the refinement residuals, the normal-equation
+  // right-hand sides) have too few output tiles to fill the GPU: split K.
+  int slices = 1;
+  const int tiles = grid.x * grid.y;
+  if (ws && k >= 4 * 256 && tiles < 2 * kNumSMs) {
+    slices = (2 * kNumSMs + tiles - 1) / tiles;
+    slices = min(slices, k / 256);
+    while (slices > 1 && (size_t)slices * m * n * sizeof(T) > ws_bytes) --slices;
+  }
+  int kchunk = k;
+  if (slices > 1) {
+    kchunk = ((k + slices - 1) / slices + BK - 1) / BK * BK;
+    slices = (k + kchunk - 1) / kchunk;
+    grid.z = slices;
+  }
+  T* w = static_cast<T*>(ws);
+  if (transa)
+    k_gemm<R, BM, BN, BK, TM, TN, true><<<grid, nt, 0, st>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, w);
+  else
+    k_gemm<R, BM, BN, BK, TM, TN, false><<<grid, nt, 0, st>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, w);
+  if (slices > 1) k_splitk_reduce<T><<<dim3((m + 255) / 256, n), 256, 0, st>>>(m, n, slices, w, beta, C, ldc);
   return cudaGetLastError();
 }
 
 template <>
 cudaError_t gemm<double>(cudaStream_t st, bool transa, int m, int n, int k, double2 alpha, const double2* A,
-                         long lda, const double2* B, long ldb, double2 beta, double2* C, long ldc) {
-  if (n <= 32) return launch_gemm<double, 64, 32, 8, 4, 2>(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
-  return launch_gemm<double, 64, 64, 8, 4, 4>(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+                         long lda, const double2* B, long ldb, double2 beta, double2* C, long ldc, void* ws,
+                         size_t ws_bytes) {
+  if (n <= 32)
+    return launch_gemm<double, 64, 32, 8, 4, 2>(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, ws, ws_bytes);
+  return launch_gemm<double, 64, 64, 8, 4, 4>(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, ws, ws_bytes);
 }
 template <>
 cudaError_t gemm<float>(cudaStream_t st, bool transa, int m, int n, int k, float2 alpha, const float2* A,
-                        long lda, const float2* B, long ldb, float2 beta, float2* C, long ldc) {
-  if (n <= 64) return launch_gemm<float, 64, 32, 8, 4, 2>(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
-  return launch_gemm<float, 128, 128, 8, 8, 8>(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+                        long lda, const float2* B, long ldb, float2 beta, float2* C, long ldc, void* ws,
+                        size_t ws_bytes) {
+  if (n <= 64)
+    return launch_gemm<float, 64, 32, 8, 4, 2>(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, ws, ws_bytes);
+  return launch_gemm<float, 128, 128, 8, 8, 8>(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, ws, ws_bytes);
 }
 
 // ------------------------------------------------------------------------
@@ -304,9 +361,15 @@ cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* i
   if (e != cudaSuccess) return e;
   T mone, one;
   mone.x = -1; mone.y = 0; one.x = 1; one.y = 0;
+  const bool use_cluster = panel_cluster_supported<R>(n);
   for (int k = 0; k < n; k += kNB) {
     const int jb = (n - k < kNB) ? n - k : kNB;
-    k_getf2<R><<<1, kPanelThreads, 0, st>>>(A + k + (long)k * lda, lda, n - k, jb, ipiv, k, info);
+    if (use_cluster) {
+      e = panel_cluster<R>(st, A + k + (long)k * lda, lda, n - k, jb, ipiv, k, info);
+      if (e != cudaSuccess) return e;
+    } else {
+      k_getf2<R><<<1, kPanelThreads, 0, st>>>(A + k + (long)k * lda, lda, n - k, jb, ipiv, k, info);
+    }
     k_laswp<T><<<(n + 127) / 128, 128, 0, st>>>(A, lda, n, ipiv, k, k + jb, k, k + jb);
     const int rest = n - k - jb;
     if (rest > 0) {
@@ -320,6 +383,8 @@ cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* i
   return cudaGetLastError();
 }
 
+constexpr int kSolveNB = 256;
+
 template <typename R>
 cudaError_t getrs(cudaStream_t st, int n, int nrhs, const typename cx<R>::T* LU, long lda, const int* ipiv,
                   typename cx<R>::T* B, long ldb) {
@@ -327,22 +392,23 @@ cudaError_t getrs(cudaStream_t st, int n, int nrhs, const typename cx<R>::T* LU,
   T mone, one;
   mone.x = -1; mone.y = 0; one.x = 1; one.y = 0;
   k_laswp<T><<<(nrhs + 127) / 128, 128, 0, st>>>(B, ldb, nrhs, ipiv, 0, n, 0, 0);
-  for (int k = 0; k < n; k += kNB) {
-    const int jb = (n - k < kNB) ? n - k : kNB;
-    k_trsm_lower_unit<T><<<(nrhs + 127) / 128, 128, 0, st>>>(LU + k + (long)k * lda, lda, jb, B + k, ldb, nrhs);
+  for (int k = 0; k < n; k += kSolveNB) {
+    const int jb = (n - k < kSolveNB) ? n - k : kSolveNB;
+    cudaError_t e = trsm_cols<R>(st, false, LU + k + (long)k * lda, lda, jb, B + k, ldb, nrhs);
+    if (e != cudaSuccess) return e;
     const int rest = n - k - jb;
     if (rest > 0) {
-      cudaError_t e = gemm<R>(st, false, rest, nrhs, jb, mone, LU + (k + jb) + (long)k * lda, lda, B + k, ldb, one,
-                              B + k + jb, ldb);
+      e = gemm<R>(st, false, rest, nrhs, jb, mone, LU + (k + jb) + (long)k * lda, lda, B + k, ldb, one, B + k + jb, ldb);
       if (e != cudaSuccess) return e;
     }
   }
-  const int last = ((n - 1) / kNB) * kNB;
-  for (int k = last; k >= 0; k -= kNB) {
-    const int jb = (n - k < kNB) ? n - k : kNB;
-    k_trsm_upper<T><<<(nrhs + 127) / 128, 128, 0, st>>>(LU + k + (long)k * lda, lda, jb, B + k, ldb, nrhs);
+  const int last = ((n - 1) / kSolveNB) * kSolveNB;
+  for (int k = last; k >= 0; k -= kSolveNB) {
+    const int jb = (n - k < kSolveNB) ? n - k : kSolveNB;
+    cudaError_t e = trsm_cols<R>(st, true, LU + k + (long)k * lda, lda, jb, B + k, ldb, nrhs);
+    if (e != cudaSuccess) return e;
     if (k > 0) {
-      cudaError_t e = gemm<R>(st, false, k, nrhs, jb, mone, LU + (long)k * lda, lda, B + k, ldb, one, B, ldb);
+      e = gemm<R>(st, false, k, nrhs, jb, mone, LU + (long)k * lda, lda, B + k, ldb, one, B, ldb);
       if (e != cudaSuccess) return e;
     }
   }

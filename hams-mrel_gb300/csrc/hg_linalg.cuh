@@ -18,7 +18,8 @@ template <> struct cx<float> { typedef float2 T; };
 template <typename R>
 cudaError_t gemm(cudaStream_t st, bool transa, int m, int n, int k, typename cx<R>::T alpha,
                  const typename cx<R>::T* A, long lda, const typename cx<R>::T* B, long ldb,
-                 typename cx<R>::T beta, typename cx<R>::T* C, long ldc);
+                 typename cx<R>::T beta, typename cx<R>::T* C, long ldc, void* ws = nullptr,
+                 size_t ws_bytes = 0);
 
 // In-place LU with partial pivoting of the n x n matrix A (lda).  ipiv is a
 // device array of n 1-based pivot rows, LAPACK style.  info (device int) is
@@ -33,6 +34,17 @@ cudaError_t getrs(cudaStream_t st, int n, int nrhs, const typename cx<R>::T* LU,
                   typename cx<R>::T* B, long ldb);
 
 size_t lu_work_bytes(int n);
+
+// Panel LU on a 16-CTA cluster (hg_lu_cluster.cu): rows [0, m) x columns
+// [0, jb <= 32) of P, pivots written 1-based as k0 + row + 1.
+template <typename R>
+cudaError_t panel_cluster(cudaStream_t st, typename cx<R>::T* P, long lda, int m, int jb, int* ipiv, int k0, int* info);
+template <typename R>
+bool panel_cluster_supported(int m);
+// Column-parallel triangular solve of a jb <= 256 diagonal block for ncols columns.
+template <typename R>
+cudaError_t trsm_cols(cudaStream_t st, bool upper, const typename cx<R>::T* A, long lda, int jb,
+                      typename cx<R>::T* X, long ldx, int ncols);
 
 // Elementwise conversions between complex128 and complex64 buffers.
 cudaError_t convert_z2c(cudaStream_t st, long count, const double2* src, float2* dst);

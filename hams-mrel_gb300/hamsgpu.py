@@ -136,7 +136,7 @@ class Solver:
     """One library context (device buffers, stream, factorisation)."""
 
     def __init__(self, precision: int = HG_PREC_FP64, device: int = 0, grn_kind: int = 8,
-                 max_refine: int = 10, refine_tol: float = 1e-12, rho: float = 1000.0, g: float = 9.80665):
+                 max_refine: int = 10, refine_tol: float = 1e-10, rho: float = 1000.0, g: float = 9.80665):
         self.L = load()
         opts = HgOpts()
         self.L.hg_default_opts(ctypes.byref(opts))

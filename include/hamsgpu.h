@@ -42,7 +42,7 @@ typedef struct {
                             before assembly, as the reference's GRN_KIND=4 storage
                             (src/WavDynMods.f90:47) */
     int max_refine;      /* mixed form: maximum refinement sweeps (default 10) */
-    double refine_tol;   /* mixed form: stop when max_k ||A x_k - b_k|| / ||b_k|| <= tol (default 1e-12) */
+    double refine_tol;   /* mixed form: stop when max_k ||A x_k - b_k|| / ||b_k|| <= tol (default 1e-10) */
     double rho;          /* fluid density for the forces (reference Const_mod: 1000) */
     double g;            /* gravity for VINP (reference Const_mod: 9.80665) */
 } hg_opts;
