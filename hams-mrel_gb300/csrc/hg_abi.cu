@@ -25,6 +25,10 @@ template <typename T>
 struct DevBuf {
   T* p = nullptr;
   size_t cap = 0;  // elements
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
   cudaError_t ensure(size_t count) {
     if (count <= cap && p) return cudaSuccess;
     if (p) cudaFree(p);
@@ -60,7 +64,8 @@ struct hg_ctx {
   DevBuf<double> wvn;
   // matrices
   DevBuf<double2> A, S, C, A64, B, X, R, R2, W, part, exfc, gws;  // gws: split-K GEMM workspace
-  DevBuf<float2> Af, Sf, Cf, Bf;
+  DevBuf<float2> Af, Sf, Cf, Bf, Aof;  // Aof: unfactorised copy of Af (mixed form, irsp = 0)
+  DevBuf<unsigned char> rws;             // workspace of the double-float residual
   DevBuf<double> amas, bdmp;
   int irsp = 0;
   bool factored = false;
@@ -137,6 +142,7 @@ int ensure_rhs(hg_ctx* c, int nbeta) {
     CK(c->R.ensure((size_t)c->tn * nc));
     CK(c->R2.ensure((size_t)c->n * nc));
     CK(c->Bf.ensure((size_t)c->n * nc));
+    CK(c->rws.ensure(hg::resid_work_bytes(c->tn, nc, c->tn)));
   } else if (c->irsp == 1) {
     CK(c->R2.ensure((size_t)c->n * nc));
   }
@@ -170,7 +176,7 @@ __global__ void k_colmax(int rows, const double2* __restrict__ M, long ld, doubl
 int solve_cols(hg_ctx* c, int c0, int c1) {
   const int n = c->n, tn = c->tn, nc = c1 - c0;
   if (nc <= 0) return 0;
-  const double2 one = make_double2(1, 0), zero = make_double2(0, 0), mone = make_double2(-1, 0);
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
   double2* Bc = c->B.p + (size_t)c0 * tn;
   double2* Xc = c->X.p + (size_t)c0 * n;
   if (!mixed(c)) {
@@ -187,11 +193,16 @@ int solve_cols(hg_ctx* c, int c0, int c1) {
     return 0;
   }
   // ---- mixed form: complex64 LU + FP64 iterative refinement ----
+  // Residuals use the complex64 matrix that was factorised (exact in single
+  // precision), read as such, in double-float arithmetic (hg_resid.cu).
   const float2* LU = (c->irsp == 1) ? c->Cf.p : c->Af.p;
+  const float2* A0 = (c->irsp == 1) ? c->Af.p : c->Aof.p;
+  void* rws = c->rws.p;
+  const size_t rws_bytes = c->rws.cap;
   const long ldlu = (c->irsp == 1) ? n : tn;
   double2* Rh = c->R2.p + (size_t)c0 * n;  // n x nc right-hand side of the square system
   float2* Bf = c->Bf.p + (size_t)c0 * n;
-  if (c->irsp == 1) CK(hg::gemm<double>(c->st, true, n, nc, tn, one, c->A64.p, tn, Bc, tn, zero, Rh, n, WS(c)));
+  if (c->irsp == 1) CK(hg::resid_df(c->st, true, n, nc, tn, A0, tn, Bc, tn, nullptr, 0, 1.0, Rh, n, rws, rws_bytes));
   else CK(cudaMemcpy2DAsync(Rh, (size_t)n * sizeof(double2), Bc, (size_t)tn * sizeof(double2), (size_t)n * sizeof(double2),
                             nc, cudaMemcpyDeviceToDevice, c->st));
   // norms of the square-system right-hand side
@@ -211,14 +222,10 @@ int solve_cols(hg_ctx* c, int c0, int c1) {
     // r = b - M x in FP64 (M = A, or A^T A applied as A^T (B - A x))
     if (c->irsp == 1) {
       double2* R1 = c->R.p + (size_t)c0 * tn;
-      CK(cudaMemcpy2DAsync(R1, (size_t)tn * sizeof(double2), Bc, (size_t)tn * sizeof(double2), (size_t)tn * sizeof(double2),
-                           nc, cudaMemcpyDeviceToDevice, c->st));
-      CK(hg::gemm<double>(c->st, false, tn, nc, n, mone, c->A64.p, tn, Xc, n, one, R1, tn, WS(c)));
-      CK(hg::gemm<double>(c->st, true, n, nc, tn, one, c->A64.p, tn, R1, tn, zero, Rh, n, WS(c)));
+      CK(hg::resid_df(c->st, false, tn, nc, n, A0, tn, Xc, n, Bc, tn, -1.0, R1, tn, rws, rws_bytes));
+      CK(hg::resid_df(c->st, true, n, nc, tn, A0, tn, R1, tn, nullptr, 0, 1.0, Rh, n, rws, rws_bytes));
     } else {
-      CK(cudaMemcpy2DAsync(Rh, (size_t)n * sizeof(double2), Bc, (size_t)tn * sizeof(double2), (size_t)n * sizeof(double2),
-                           nc, cudaMemcpyDeviceToDevice, c->st));
-      CK(hg::gemm<double>(c->st, false, n, nc, n, mone, c->A64.p, tn, Xc, n, one, Rh, n, WS(c)));
+      CK(hg::resid_df(c->st, false, n, nc, n, A0, tn, Xc, n, Bc, tn, -1.0, Rh, n, rws, rws_bytes));
     }
     k_colmax<<<nc, 256, 0, c->st>>>(n, Rh, n, nb.p + nc);
     CK(cudaMemcpyAsync(rnorm.data(), nb.p + nc, nc * sizeof(double), cudaMemcpyDeviceToHost, c->st));
@@ -311,8 +318,9 @@ void hg_destroy(hg_ctx* c) {
   for (auto* b : ibs) b->release();
   DevBuf<double2>* zbs[] = {&c->A, &c->S, &c->C, &c->A64, &c->B, &c->X, &c->R, &c->R2, &c->W, &c->part, &c->exfc, &c->gws};
   for (auto* b : zbs) b->release();
-  DevBuf<float2>* cbs[] = {&c->Af, &c->Sf, &c->Cf, &c->Bf};
+  DevBuf<float2>* cbs[] = {&c->Af, &c->Sf, &c->Cf, &c->Bf, &c->Aof};
   for (auto* b : cbs) b->release();
+  c->rws.release();
   for (int k = 0; k < 5; ++k)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   for (int k = 0; k < 16; ++k)
@@ -462,14 +470,16 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
   } else {
     CK(c->Af.ensure((size_t)tn * n));
     CK(c->Sf.ensure((size_t)tn * n));
-    CK(c->A64.ensure((size_t)tn * n));
     const bool special = std::fabs(c->v) < (double)1.e-8f || std::fabs(c->v + 1.0) < (double)1.e-8f;
     if (deep && !special && c->o.grn_kind == 8)
       CK(hg::launch_green_fill_mixed(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, c->v, c->Af.p, c->Sf.p, tn, c->status.p));
     else
       CK(hg::launch_green_fill<float2>(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, deep, c->o.grn_kind, c->Af.p,
                                        c->Sf.p, tn, c->status.p));
-    CK(hg::convert_c2z(c->st, (long)tn * n, c->Af.p, c->A64.p));
+    if (irsp == 0) {
+      CK(c->Aof.ensure((size_t)tn * n));
+      CK(cudaMemcpyAsync(c->Aof.p, c->Af.p, (size_t)tn * n * sizeof(float2), cudaMemcpyDeviceToDevice, c->st));
+    }
     CK(cudaEventRecord(c->ev[1], c->st));
     if (irsp == 1) {
       CK(c->Cf.ensure((size_t)n * n));
@@ -622,12 +632,10 @@ int hg_get_matrix(hg_ctx* c, int which, double* out, int ld) {
     else if (c->keep) src = c->A64.p;
     else return fail(c, HG_ERR_STATE, "the influence matrix was factorised in place; call hg_keep_matrices(ctx, 1) first");
   } else {
-    if (which == 0) src = c->A64.p;
-    else {
-      CK(tmp.ensure((size_t)tn * n));
-      CK(hg::convert_c2z(c->st, (long)tn * n, c->Sf.p, tmp.p));
-      src = tmp.p;
-    }
+    const float2* f = (which == 1) ? c->Sf.p : (c->irsp == 1 ? c->Af.p : c->Aof.p);
+    CK(tmp.ensure((size_t)tn * n));
+    CK(hg::convert_c2z(c->st, (long)tn * n, f, tmp.p));
+    src = tmp.p;
   }
   CK(cudaMemcpy2DAsync(out, (size_t)ld * sizeof(double2), src, (size_t)tn * sizeof(double2), (size_t)tn * sizeof(double2), n,
                        cudaMemcpyDeviceToHost, c->st));
@@ -659,6 +667,105 @@ int hg_refine_info(const hg_ctx* c, int* sweeps, double* residual) {
   if (!c) return -1;
   if (sweeps) *sweeps = c->sweeps;
   if (residual) *residual = c->resid;
+  return 0;
+}
+
+int hg_gesv(hg_ctx* c, int precision, int n, int nrhs, double* a, int lda, int* ipiv, double* b, int ldb, int* iter,
+            int* info) {
+  if (!c) return -1;
+  if (precision != HG_PREC_FP64 && precision != HG_PREC_MIXED) return fail(c, -2, "precision must be 0 or 1");
+  if (n <= 0) return fail(c, -3, "n must be positive");
+  if (nrhs < 0) return fail(c, -4, "nrhs must be >= 0");
+  if (!a) return fail(c, -5, "a is NULL");
+  if (lda < n) return fail(c, -6, "lda %d < n %d", lda, n);
+  if (!ipiv) return fail(c, -7, "ipiv is NULL");
+  if (nrhs > 0 && !b) return fail(c, -8, "b is NULL");
+  if (nrhs > 0 && ldb < n) return fail(c, -9, "ldb %d < n %d", ldb, n);
+  CK(cudaSetDevice(c->o.device));
+  const size_t nn = (size_t)n * n, nb = (size_t)n * (nrhs > 0 ? nrhs : 1);
+  DevBuf<double2> dA, dB, dX, dR, ws;
+  DevBuf<float2> dAf, dBf;
+  DevBuf<int> dpiv, dinfo;
+  DevBuf<double> norms;
+  const double2 one = make_double2(1, 0), mone = make_double2(-1, 0);
+  CK(dA.ensure(nn));
+  CK(dB.ensure(nb));
+  CK(dpiv.ensure(n));
+  CK(dinfo.ensure(1));
+  CK(cudaMemcpy2DAsync(dA.p, (size_t)n * sizeof(double2), a, (size_t)lda * sizeof(double2), (size_t)n * sizeof(double2),
+                       n, cudaMemcpyHostToDevice, c->st));
+  if (nrhs > 0)
+    CK(cudaMemcpy2DAsync(dB.p, (size_t)n * sizeof(double2), b, (size_t)ldb * sizeof(double2),
+                         (size_t)n * sizeof(double2), nrhs, cudaMemcpyHostToDevice, c->st));
+  int it = 0, inf = 0;
+  bool fp64 = precision == HG_PREC_FP64;
+  const double2* result = dB.p;
+  if (!fp64) {
+    CK(dAf.ensure(nn));
+    CK(dBf.ensure(nb));
+    CK(dX.ensure(nb));
+    CK(dR.ensure(nb));
+    CK(ws.ensure((size_t)16 * nb));
+    CK(norms.ensure(2 * (size_t)(nrhs > 0 ? nrhs : 1)));
+    CK(hg::convert_z2c(c->st, (long)nn, dA.p, dAf.p));
+    CK(hg::getrf<float>(c->st, n, dAf.p, n, dpiv.p, dinfo.p, nullptr));
+    CK(cudaMemcpyAsync(&inf, dinfo.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    if (inf != 0) {
+      // a zero pivot in complex64: fall back to the complex128 factorisation
+      fp64 = true;
+      it = -31;
+    } else if (nrhs > 0) {
+      std::vector<double> bn(nrhs), rn(nrhs);
+      k_colmax<<<nrhs, 256, 0, c->st>>>(n, dB.p, n, norms.p);
+      CK(cudaMemcpyAsync(bn.data(), norms.p, nrhs * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+      CK(hg::convert_z2c(c->st, (long)nb, dB.p, dBf.p));
+      CK(hg::getrs<float>(c->st, n, nrhs, dAf.p, n, dpiv.p, dBf.p, n));
+      CK(hg::convert_c2z(c->st, (long)nb, dBf.p, dX.p));
+      bool ok = false;
+      for (int sweep = 0;; ++sweep) {
+        CK(cudaMemcpyAsync(dR.p, dB.p, nb * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
+        CK(hg::gemm<double>(c->st, false, n, nrhs, n, mone, dA.p, n, dX.p, n, one, dR.p, n, (void*)ws.p,
+                            ws.cap * sizeof(double2)));
+        k_colmax<<<nrhs, 256, 0, c->st>>>(n, dR.p, n, norms.p + nrhs);
+        CK(cudaMemcpyAsync(rn.data(), norms.p + nrhs, nrhs * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        double worst = 0.0;
+        for (int k = 0; k < nrhs; ++k) worst = std::fmax(worst, bn[k] > 0 ? rn[k] / bn[k] : rn[k]);
+        if (worst <= c->o.refine_tol) { ok = true; it = sweep; break; }
+        if (sweep >= c->o.max_refine) break;
+        CK(hg::convert_z2c(c->st, (long)nb, dR.p, dBf.p));
+        CK(hg::getrs<float>(c->st, n, nrhs, dAf.p, n, dpiv.p, dBf.p, n));
+        CK(hg::add_c2z_2d(c->st, n, nrhs, dBf.p, n, dX.p, n));
+      }
+      if (ok) {
+        result = dX.p;
+        CK(hg::convert_c2z(c->st, (long)nn, dAf.p, dA.p));
+      } else {
+        fp64 = true;
+        it = -31;
+      }
+    } else {
+      CK(hg::convert_c2z(c->st, (long)nn, dAf.p, dA.p));
+    }
+  }
+  if (fp64) {
+    // dA still holds the caller's matrix whenever this branch runs
+    CK(hg::getrf<double>(c->st, n, dA.p, n, dpiv.p, dinfo.p, nullptr));
+    CK(cudaMemcpyAsync(&inf, dinfo.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    if (inf == 0 && nrhs > 0) CK(hg::getrs<double>(c->st, n, nrhs, dA.p, n, dpiv.p, dB.p, n));
+    result = dB.p;
+  }
+  CK(cudaMemcpy2DAsync(a, (size_t)lda * sizeof(double2), dA.p, (size_t)n * sizeof(double2), (size_t)n * sizeof(double2),
+                       n, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(ipiv, dpiv.p, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  if (nrhs > 0 && inf == 0)
+    CK(cudaMemcpy2DAsync(b, (size_t)ldb * sizeof(double2), result, (size_t)n * sizeof(double2),
+                         (size_t)n * sizeof(double2), nrhs, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (iter) *iter = it;
+  if (info) *info = inf;
   return 0;
 }
 

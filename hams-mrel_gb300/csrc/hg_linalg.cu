@@ -198,7 +198,7 @@ cudaError_t gemm<float>(cudaStream_t st, bool transa, int m, int n, int k, float
                         size_t ws_bytes) {
   if (n <= 64)
     return launch_gemm<float, 64, 32, 8, 4, 2>(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, ws, ws_bytes);
-  return launch_gemm<float, 128, 128, 8, 8, 8>(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, ws, ws_bytes);
+  return cgemm_wide(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
 }
 
 // ------------------------------------------------------------------------

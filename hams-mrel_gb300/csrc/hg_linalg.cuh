@@ -21,6 +21,20 @@ cudaError_t gemm(cudaStream_t st, bool transa, int m, int n, int k, typename cx<
                  typename cx<R>::T beta, typename cx<R>::T* C, long ldc, void* ws = nullptr,
                  size_t ws_bytes = 0);
 
+// Complex64 GEMM for wide outputs (hg_gemm32.cu): same contract as gemm<float>
+// without split-K; used by gemm<float> when N > 64.
+cudaError_t cgemm_wide(cudaStream_t st, bool transa, int m, int n, int k, float2 alpha, const float2* A, long lda,
+                       const float2* B, long ldb, float2 beta, float2* C, long ldc);
+
+// out = Bin + sign * op(A) Y (hg_resid.cu): A complex64 (exact entries), Y and
+// Bin complex128 (Bin may be null), result complex128 in double-float
+// arithmetic on the FP32 pipes.  M x NC result, inner dimension K.  ws: a
+// 256-byte aligned device workspace of at least resid_work_bytes(m, nc, k).
+size_t resid_work_bytes(int m, int nc, int k);
+cudaError_t resid_df(cudaStream_t st, bool transa, int m, int nc, int k, const float2* A, long lda, const double2* Y,
+                     long ldy, const double2* Bin, long ldb, double sign, double2* out, long ldo, void* ws,
+                     size_t ws_bytes);
+
 // In-place LU with partial pivoting of the n x n matrix A (lda).  ipiv is a
 // device array of n 1-based pivot rows, LAPACK style.  info (device int) is
 // set to the first zero pivot (1-based) or left at 0.  work is a device

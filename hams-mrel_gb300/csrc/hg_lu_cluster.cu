@@ -5,15 +5,15 @@
 // contiguous slice of the panel's rows in shared memory, so the whole panel
 // (up to ~3.5 MB) stays on chip in distributed shared memory for all 32
 // column steps.  Per column: every CTA finds its local pivot candidate
-// (max |re|+|im|, the IZAMAX rule, first row on ties), a cluster barrier
-// publishes the candidates, every CTA reads the 16 candidates and the pivot
-// row straight out of the owners' shared memory, a second cluster barrier
-// orders those reads before the row interchange is written, and each CTA
-// scales and rank-1 updates its own rows.
+// (max |re|+|im|, the IZAMAX rule, first row on ties) and publishes it with
+// its row, one cluster barrier, every CTA reads the 16 candidates and rows
+// out of the other CTAs' shared memory, takes the same pivot, and scales and
+// rank-1 updates its own rows.
 #include <climits>
 #include <cooperative_groups.h>
 
 #include "hg_linalg.cuh"
+#include "hg_tma.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -49,24 +49,42 @@ template <typename T> __device__ __forceinline__ T c_div(T a, T b) {
 constexpr int kClusterCTAs = 16;
 constexpr int kClusterNB = 32;
 constexpr int kClusterThreads = 512;
+// Dynamic shared memory of one panel CTA (its rows of the panel); with the
+// kernel's static buffers (< 11 KB) it stays under the 227 KB per-CTA limit.
+constexpr int kPanelSmemMax = 208 * 1024;
 
+// Per column jj (q = jj & 1 selects one of two publication slots):
+//  (a) each thread scans its own rows (fixed thread-to-row map, so no
+//      barrier is needed after its own updates of the previous column); the
+//      CTA reduces to one candidate, and publishes the candidate's value,
+//      index and whole row in pub_*[q]; the owner of row jj publishes row jj.
+//  cluster barrier (the only one per column)
+//  (b) every CTA reads all 16 published candidates and candidate rows and
+//      the published row jj (one round trip of distributed shared memory),
+//      and makes the same pivot decision.
+//  (c) row interchange and (d) scaling and rank-1 update of local rows.
+// Only the pub_* slots are read remotely, never the tile, so the tile can be
+// updated without a second barrier.  A slot written at column jj + 2 cannot
+// race a remote read of it at column jj: the writer has passed the barrier
+// of column jj + 1, which the reader only reaches after that read.
 template <typename R>
 __global__ void __launch_bounds__(kClusterThreads)
 k_getf2_cluster(typename cx<R>::T* __restrict__ P, long lda, int m, int jb, int rpc, int* __restrict__ ipiv, int k0,
                 int* __restrict__ info) {
   typedef typename cx<R>::T T;
+  constexpr int kWarps = kClusterThreads / 32;
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* tile = reinterpret_cast<T*>(smem_raw);  // [jb][rpc], row index fastest
-  __shared__ R s_cval;
-  __shared__ int s_cidx;
-  __shared__ R red_v[kClusterThreads / 32];
-  __shared__ int red_i[kClusterThreads / 32];
-  __shared__ T s_prow[kClusterNB];
-  __shared__ T s_tmp[kClusterNB];
-  __shared__ int s_p;
-  __shared__ R s_pmax;
+  __shared__ R pub_val[2];
+  __shared__ int pub_idx[2];
+  __shared__ T pub_row[2][kClusterNB];
+  __shared__ T pub_jrow[2][kClusterNB];
+  __shared__ R red_v[kWarps];
+  __shared__ int red_i[kWarps];
+  __shared__ T s_cand[kClusterCTAs][kClusterNB];
+  __shared__ T s_jrow[kClusterNB];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int r0 = rank * rpc;
   const int rl = max(0, min(rpc, m - r0));
@@ -75,9 +93,12 @@ k_getf2_cluster(typename cx<R>::T* __restrict__ P, long lda, int m, int jb, int 
     const int r = e % rl, c = e / rl;
     tile[c * rpc + r] = P[(r0 + r) + (long)c * lda];
   }
+  // row 0 of the panel for column 0's publication
+  if (rank == 0 && tid < jb) pub_jrow[0][tid] = tile[tid * rpc];
   __syncthreads();
 
   for (int jj = 0; jj < jb; ++jj) {
+    const int q = jj & 1;
     // (a) local pivot candidate among rows >= jj
     R best = -1;
     int bidx = INT_MAX;
@@ -96,67 +117,81 @@ k_getf2_cluster(typename cx<R>::T* __restrict__ P, long lda, int m, int jb, int 
     }
     if (lane == 0) { red_v[warp] = best; red_i[warp] = bidx; }
     __syncthreads();
-    if (tid == 0) {
-      R b = -1;
-      int bi = INT_MAX;
-      for (int w = 0; w < kClusterThreads / 32; ++w)
-        if (red_v[w] > b || (red_v[w] == b && red_i[w] < bi)) { b = red_v[w]; bi = red_i[w]; }
-      s_cval = b;
-      s_cidx = bi;
-    }
-    cluster.sync();  // (1) candidates visible cluster-wide
-
-    // (b) the pivot: same decision in every CTA
     if (warp == 0) {
-      R v = -1;
-      int i = INT_MAX;
-      if (lane < kClusterCTAs) {
-        v = *cluster.map_shared_rank(&s_cval, lane);
-        i = *cluster.map_shared_rank(&s_cidx, lane);
-      }
+      R v = (lane < kWarps) ? red_v[lane] : (R)-1;
+      int i = (lane < kWarps) ? red_i[lane] : INT_MAX;
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) {
         const R ov = __shfl_down_sync(0xffffffffu, v, off);
         const int oi = __shfl_down_sync(0xffffffffu, i, off);
         if (ov > v || (ov == v && oi < i)) { v = ov; i = oi; }
       }
-      if (lane == 0) {
-        s_p = (i == INT_MAX) ? jj : i;
-        s_pmax = v;
-      }
+      v = __shfl_sync(0xffffffffu, v, 0);
+      i = __shfl_sync(0xffffffffu, i, 0);
+      if (lane == 0) { pub_val[q] = v; pub_idx[q] = i; }
+      if (i != INT_MAX && lane < jb) pub_row[q][lane] = tile[lane * rpc + (i - r0)];
     }
-    __syncthreads();
-    const int p = s_p;
-    const R pmax = s_pmax;
-    const int op = p / rpc, lp = p - op * rpc;
+    cluster.sync();
+
+    // (b) all candidates, their rows and row jj from the cluster
     const int oj = jj / rpc, lj = jj - oj * rpc;
-    // (c) read the old pivot row; the owner of row p also reads the old row jj
-    if (tid < jb) {
-      s_prow[tid] = *cluster.map_shared_rank(&tile[tid * rpc + lp], op);
-      if (rank == op && p != jj) s_tmp[tid] = *cluster.map_shared_rank(&tile[tid * rpc + lj], oj);
+    {
+      const int src = tid / kClusterNB, c = tid % kClusterNB;  // 512 threads = 16 CTAs x 32 columns
+      if (c < jb) s_cand[src][c] = *cluster.map_shared_rank(&pub_row[q][c], src);
+      if (tid < jb) s_jrow[tid] = *cluster.map_shared_rank(&pub_jrow[q][tid], oj);
     }
-    cluster.sync();  // (2) every read of the old rows precedes the interchange
-    if (tid < jb) {
-      if (rank == oj) tile[tid * rpc + lj] = s_prow[tid];
-      if (rank == op && p != jj) tile[tid * rpc + lp] = s_tmp[tid];
+    R pmax = -1;
+    int p = INT_MAX;
+    if (lane < kClusterCTAs) {
+      pmax = *cluster.map_shared_rank(&pub_val[q], lane);
+      p = *cluster.map_shared_rank(&pub_idx[q], lane);
     }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const R ov = __shfl_down_sync(0xffffffffu, pmax, off);
+      const int oi = __shfl_down_sync(0xffffffffu, p, off);
+      if (ov > pmax || (ov == pmax && oi < p)) { pmax = ov; p = oi; }
+    }
+    pmax = __shfl_sync(0xffffffffu, pmax, 0);
+    p = __shfl_sync(0xffffffffu, p, 0);
+    if (p == INT_MAX) p = jj;
+    __syncthreads();  // s_cand and s_jrow complete
+    const int op = p / rpc;
+    const bool swap = pmax > 0 && p != jj;
+    const T* prow = s_cand[op];
     if (rank == 0 && tid == 0) {
       ipiv[k0 + jj] = k0 + p + 1;
       if (!(pmax > 0) && *info == 0) *info = k0 + jj + 1;
     }
-    __syncthreads();
-    // (d) scale the column below the pivot and update this CTA's rows
+    // (c) row jj becomes the pivot row (U row of this column)
+    if (swap && rank == oj && tid < jb) tile[tid * rpc + lj] = prow[tid];
+    // (d) scale below the pivot and update; the owner of row p takes old row jj
     if (pmax > 0) {
-      const T rp = c_recip(s_prow[jj]);
+      const T rp = c_recip(prow[jj]);
       for (int r = tid; r < rl; r += blockDim.x) {
-        if (r0 + r > jj) {
-          const T l = c_mul(tile[jj * rpc + r], rp);
+        const int gr = r0 + r;
+        if (gr > jj) {
+          const bool moved = swap && gr == p;
+          T l = moved ? s_jrow[jj] : tile[jj * rpc + r];
+          l = c_mul(l, rp);
           tile[jj * rpc + r] = l;
-          for (int c = jj + 1; c < jb; ++c) tile[c * rpc + r] = c_sub(tile[c * rpc + r], c_mul(l, s_prow[c]));
+          for (int c = jj + 1; c < jb; ++c) {
+            const T a = moved ? s_jrow[c] : tile[c * rpc + r];
+            tile[c * rpc + r] = c_sub(a, c_mul(l, prow[c]));
+          }
+          if (moved) {
+            for (int c = 0; c < jj; ++c) tile[c * rpc + r] = s_jrow[c];
+          }
         }
       }
     }
-    __syncthreads();
+    // publish row jj + 1 for the next column (its owner thread updated it)
+    if (jj + 1 < jb) {
+      const int gr = jj + 1;
+      if (gr >= r0 && gr < r0 + rl && ((gr - r0) % blockDim.x) == tid) {
+        for (int c = 0; c < jb; ++c) pub_jrow[q ^ 1][c] = tile[c * rpc + (gr - r0)];
+      }
+    }
   }
   cluster.sync();  // no CTA leaves while another could still read its shared memory
   for (int e = tid; e < rl * jb; e += blockDim.x) {
@@ -174,11 +209,11 @@ cudaError_t panel_cluster(cudaStream_t st, typename cx<R>::T* P, long lda, int m
   const size_t smem = (size_t)rpc * jb * sizeof(T);
   static int attr_done[2] = {0, 0};
   const int idx = sizeof(R) == 8 ? 1 : 0;
-  if (smem > 220 * 1024) return cudaErrorNotSupported;
+  if (smem > (size_t)kPanelSmemMax) return cudaErrorNotSupported;
   auto kern = k_getf2_cluster<R>;
   if (!attr_done[idx]) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kPanelSmemMax);
     if (e != cudaSuccess) return e;
     attr_done[idx] = 1;
   }
@@ -207,17 +242,17 @@ bool panel_cluster_supported(int m) {
   static int cached[2] = {-1, -1};
   const int idx = sizeof(R) == 8 ? 1 : 0;
   const int rpc = (m + kClusterCTAs - 1) / kClusterCTAs;
-  if ((size_t)rpc * kClusterNB * sizeof(T) > 220 * 1024) return false;
+  if ((size_t)rpc * kClusterNB * sizeof(T) > (size_t)kPanelSmemMax) return false;
   if (cached[idx] < 0) {
     auto kern = k_getf2_cluster<R>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kPanelSmemMax);
     int ncl = 0;
     if (e == cudaSuccess) {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(kClusterCTAs, 1, 1);
       cfg.blockDim = dim3(kClusterThreads, 1, 1);
-      cfg.dynamicSmemBytes = 220 * 1024;
+      cfg.dynamicSmemBytes = kPanelSmemMax;
       cudaLaunchAttribute attr[1];
       attr[0].id = cudaLaunchAttributeClusterDimension;
       attr[0].val.clusterDim.x = kClusterCTAs;
@@ -236,33 +271,98 @@ template bool panel_cluster_supported<float>(int);
 template bool panel_cluster_supported<double>(int);
 
 // ---------------------------------------------------------------------------
-// Triangular solves, one CTA per right-hand-side column, rows across threads
-// (jb <= 256): X = L^{-1} X (unit lower) or X = U^{-1} X (upper, divides by
-// the diagonal as ZTRSM does).
+// Triangular solves, one CTA per right-hand-side column (jb <= 256 rows):
+// X = L^{-1} X (unit lower) or X = U^{-1} X (upper, divides by the diagonal
+// as ZTRSM does).  The block is walked in sub-blocks of SB columns staged in
+// shared memory by cp.async, the next sub-block in flight while the current
+// one is used.  One warp solves the SB x SB diagonal part with shuffles (no
+// CTA barrier per row), then every thread updates its own row with the SB
+// new unknowns: two CTA barriers per sub-block instead of one or two per row.
 // ---------------------------------------------------------------------------
 constexpr int kTrsmBlock = 256;
+
+template <typename T> struct TrsmSub;
+template <> struct TrsmSub<float2> { static constexpr int SB = 32; };
+template <> struct TrsmSub<double2> { static constexpr int SB = 16; };
+
+template <typename T>
+__device__ __forceinline__ void cp_elem(T* dst, const T* src, bool pred);
+template <> __device__ __forceinline__ void cp_elem<float2>(float2* dst, const float2* src, bool pred) {
+  cp_async8(dst, src, pred);
+}
+template <> __device__ __forceinline__ void cp_elem<double2>(double2* dst, const double2* src, bool pred) {
+  cp_async16(dst, src, pred ? 16 : 0);
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl_c(T v, int src) {
+  v.x = __shfl_sync(0xffffffffu, v.x, src);
+  v.y = __shfl_sync(0xffffffffu, v.y, src);
+  return v;
+}
+
+template <typename T, bool UPPER>
+__device__ __forceinline__ void trsm_stage(T* buf, const T* __restrict__ A, long lda, int jb, int s, int tid) {
+  constexpr int SB = TrsmSub<T>::SB;
+  const int c0 = s * SB, w = min(SB, jb - c0);
+  // lower: rows >= c0 are used; upper: rows < c0 + w
+#pragma unroll 4
+  for (int e = tid; e < SB * kTrsmBlock; e += kTrsmBlock) {
+    const int r = e % kTrsmBlock, j = e / kTrsmBlock;
+    const bool need = j < w && r < jb && (UPPER ? r < c0 + w : r >= c0);
+    cp_elem<T>(buf + j * kTrsmBlock + r, need ? A + r + (long)(c0 + j) * lda : A, need);
+  }
+}
 
 template <typename T, bool UPPER>
 __global__ void __launch_bounds__(kTrsmBlock)
 k_trsm_col(const T* __restrict__ A, long lda, int jb, T* __restrict__ X, long ldx) {
+  constexpr int SB = TrsmSub<T>::SB;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* bufs = reinterpret_cast<T*>(smem_raw);  // 2 x [SB][kTrsmBlock]
   __shared__ T x[kTrsmBlock];
-  const int col = blockIdx.x, tid = threadIdx.x;
+  const int col = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   T* xc = X + (long)col * ldx;
+  T zero;
+  zero.x = 0; zero.y = 0;
+  const int nsb = (jb + SB - 1) / SB;
   if (tid < jb) x[tid] = xc[tid];
-  __syncthreads();
-  if (!UPPER) {
-    for (int c = 0; c < jb; ++c) {
-      if (tid > c && tid < jb) x[tid] = c_sub(x[tid], c_mul(A[tid + (long)c * lda], x[c]));
-      __syncthreads();
+  int s = UPPER ? nsb - 1 : 0;
+  trsm_stage<T, UPPER>(bufs, A, lda, jb, s, tid);
+  cp_async_commit();
+  for (int it = 0; it < nsb; ++it, s += (UPPER ? -1 : 1)) {
+    T* cur = bufs + (it & 1) * SB * kTrsmBlock;
+    cp_async_wait<0>();
+    __syncthreads();  // sub-block landed; x and the other buffer are free
+    if (it + 1 < nsb)
+      trsm_stage<T, UPPER>(bufs + ((it + 1) & 1) * SB * kTrsmBlock, A, lda, jb, s + (UPPER ? -1 : 1), tid);
+    cp_async_commit();
+    const int c0 = s * SB, w = min(SB, jb - c0);
+    if (warp == 0) {
+      T xr = (lane < w) ? x[c0 + lane] : zero;
+      if (!UPPER) {
+        for (int j = 0; j < w; ++j) {
+          const T xj = shfl_c(xr, j);
+          if (lane > j && lane < w) xr = c_sub(xr, c_mul(cur[j * kTrsmBlock + c0 + lane], xj));
+        }
+      } else {
+        for (int j = w - 1; j >= 0; --j) {
+          if (lane == j) xr = c_div(xr, cur[j * kTrsmBlock + c0 + j]);
+          const T xj = shfl_c(xr, j);
+          if (lane < j) xr = c_sub(xr, c_mul(cur[j * kTrsmBlock + c0 + lane], xj));
+        }
+      }
+      if (lane < w) x[c0 + lane] = xr;
     }
-  } else {
-    for (int c = jb - 1; c >= 0; --c) {
-      if (tid == c) x[c] = c_div(x[c], A[c + (long)c * lda]);
-      __syncthreads();
-      if (tid < c) x[tid] = c_sub(x[tid], c_mul(A[tid + (long)c * lda], x[c]));
-      __syncthreads();
+    __syncthreads();
+    const bool mine = UPPER ? (tid < c0) : (tid >= c0 + w && tid < jb);
+    if (mine) {
+      T acc = x[tid];
+      for (int j = 0; j < w; ++j) acc = c_sub(acc, c_mul(cur[j * kTrsmBlock + tid], x[c0 + j]));
+      x[tid] = acc;
     }
   }
+  __syncthreads();
   if (tid < jb) xc[tid] = x[tid];
 }
 
@@ -271,9 +371,12 @@ cudaError_t trsm_cols(cudaStream_t st, bool upper, const typename cx<R>::T* A, l
                       typename cx<R>::T* X, long ldx, int ncols) {
   typedef typename cx<R>::T T;
   if (jb > kTrsmBlock) return cudaErrorInvalidValue;
-  if (ncols <= 0) return cudaSuccess;
-  if (upper) k_trsm_col<T, true><<<ncols, kTrsmBlock, 0, st>>>(A, lda, jb, X, ldx);
-  else k_trsm_col<T, false><<<ncols, kTrsmBlock, 0, st>>>(A, lda, jb, X, ldx);
+  if (ncols <= 0 || jb <= 0) return cudaSuccess;
+  const int smem = 2 * TrsmSub<T>::SB * kTrsmBlock * (int)sizeof(T);
+  auto kern = upper ? k_trsm_col<T, true> : k_trsm_col<T, false>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  kern<<<ncols, kTrsmBlock, smem, st>>>(A, lda, jb, X, ldx);
   return cudaGetLastError();
 }
 template cudaError_t trsm_cols<float>(cudaStream_t, bool, const float2*, long, int, float2*, long, int);

@@ -1,7 +1,10 @@
-// Bulk asynchronous copies (the TMA engine's non-tensor form) into shared
-// memory, completed on an mbarrier.  Every wait is bounded: a wait that
-// runs out of iterations reports failure and the caller records it in the
-// device status word instead of spinning forever.
+// Asynchronous copies into shared memory.
+//  - Bulk copies (the TMA engine's non-tensor form) completed on an mbarrier.
+//    Every mbarrier wait is bounded: a wait that runs out of iterations
+//    reports failure and the caller records it in the device status word
+//    instead of spinning forever.
+//  - Per-thread cp.async copies of 8 or 16 bytes with zero fill, grouped by
+//    commit/wait_group (waits on the thread's own copies, which always end).
 #pragma once
 #include <stdint.h>
 
@@ -47,6 +50,22 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase,
     if (mbar_try_wait(bar, phase)) return true;
   }
   return false;
+}
+
+// 8-byte copy; pred false writes zeros and reads nothing.
+__device__ __forceinline__ void cp_async8(void* dst, const void* src, bool pred) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(smem_addr(dst)), "l"(src), "r"(pred ? 8 : 0)
+               : "memory");
+}
+// 16-byte copy of `bytes` (0, 8 or 16) source bytes, the rest zero; dst and
+// src 16-byte aligned.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, int bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_addr(dst)), "l"(src), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
 }  // namespace hg

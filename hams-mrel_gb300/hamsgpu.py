@@ -23,7 +23,7 @@ EXPORTS = [
     "hg_fill_factor", "hg_solve_radiation", "hg_solve_all_headings", "hg_solve_diffraction", "hg_forces",
     "hg_solve_frequency", "hg_keep_matrices", "hg_get_matrix", "hg_green_points", "hg_refine_info",
     "hg_stage_times", "hg_dispersion", "hg_wave_properties", "hg_panel_geometry", "hg_mark", "hg_elapsed",
-    "hg_bench_gemm", "hg_green_points_noalloc",
+    "hg_bench_gemm", "hg_green_points_noalloc", "hg_gesv",
 ]
 
 
@@ -80,6 +80,8 @@ def load(build_if_missing: bool = True):
     L.hg_refine_info.argtypes = [c_void_p, P(c_int), P(c_double)]
     L.hg_stage_times.argtypes = [c_void_p, P(ctypes.c_float)]
     L.hg_green_points_noalloc.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p]
+    L.hg_gesv.argtypes = [c_void_p, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_void_p, c_int, P(c_int),
+                          P(c_int)]
     L.hg_mark.argtypes = [c_void_p, c_int]
     L.hg_elapsed.argtypes = [c_void_p, c_int, c_int, P(ctypes.c_float)]
     L.hg_dispersion.argtypes = [c_double, c_double, c_int, c_void_p]
@@ -251,6 +253,22 @@ class Solver:
         out = np.zeros((len(fl), 8))
         self._check(self.L.hg_green_points_noalloc(self.h, len(fl), _ptr(p), _ptr(fl), _ptr(out)))
         return out[:, 0::2] + 1j * out[:, 1::2]
+
+    def gesv(self, a, b, precision=HG_PREC_FP64):
+        """Dense solve A X = B on the device (hg_gesv).
+
+        Returns (lu, ipiv, x, iter, info): lu the n x n factors (unit-lower L
+        below the diagonal, U on and above), ipiv 1-based LAPACK pivots."""
+        lu = np.array(a, dtype=np.complex128, order="F", copy=True)
+        n = lu.shape[0]
+        bb = np.array(b, dtype=np.complex128, order="F", copy=True)
+        if bb.ndim == 1:
+            bb = bb.reshape(n, 1, order="F")
+        ipiv = np.zeros(n, dtype=np.int32)
+        it = ctypes.c_int(); info = ctypes.c_int()
+        self._check(self.L.hg_gesv(self.h, precision, n, bb.shape[1], _ptr(lu), n, _ptr(ipiv), _ptr(bb), n,
+                                   ctypes.byref(it), ctypes.byref(info)))
+        return lu, ipiv, bb, it.value, info.value
 
     def refine_info(self):
         s = ctypes.c_int(); r = ctypes.c_double()

@@ -168,6 +168,21 @@ int hg_panel_geometry(int n, int ntnd, const double *nodes, const int *ncon, con
 #define HG_NOALLOC_MAX_POINTS 65536
 int hg_green_points_noalloc(hg_ctx *ctx, int npts, const double *pts, const int *flags, double *out);
 
+/* Dense complex solve A X = B on the device, the ZGETRF + ZGETRS pair of
+ * src/AssbMatx.f90:111,277 (and AssbMatx_irr.f90:175,491) for a matrix the
+ * caller already holds.  a: n x n COMPLEX*16 (lda >= n), b: n x nrhs
+ * (ldb >= n), ipiv: n 1-based pivot rows.
+ *   precision 0 (ZGESV): a <- complex128 LU factors, b <- X, *iter = 0.
+ *   precision 1 (ZCGESV-style): LU in complex64, X refined with residuals
+ *     against the complex128 matrix until max|r|/max|b| <= refine_tol per
+ *     column; a <- the complex64 factors widened to complex128, *iter = the
+ *     sweeps taken.  If max_refine sweeps do not reach the tolerance the
+ *     solve is redone in complex128 (a <- complex128 factors) and *iter = -31.
+ * *info = 0, or i > 0 when U(i,i) is exactly zero (b is then left as it came).
+ * Device buffers are allocated for the call and freed before it returns. */
+int hg_gesv(hg_ctx *ctx, int precision, int n, int nrhs, double *a, int lda, int *ipiv, double *b, int ldb,
+            int *iter, int *info);
+
 /* Refinement sweeps taken and final relative residual of the last mixed-form solve. */
 int hg_refine_info(const hg_ctx *ctx, int *sweeps, double *residual);
 
