@@ -63,7 +63,7 @@ struct hg_ctx {
   bool freq_set = false;
   DevBuf<double> wvn;
   // matrices
-  DevBuf<double2> A, S, C, A64, B, X, R, R2, W, part, exfc, gws;  // gws: split-K GEMM workspace
+  DevBuf<double2> A, S, C, A64, B, X, R, R2, W, Wz, part, exfc, gws;  // gws: split-K GEMM workspace
   DevBuf<float2> Af, Sf, Cf, Bf, Aof;  // Aof: unfactorised copy of Af (mixed form, irsp = 0)
   DevBuf<unsigned char> rws;             // workspace of the double-float residual
   DevBuf<double> amas, bdmp;
@@ -252,10 +252,14 @@ int build_rhs(hg_ctx* c, int nbeta, const double* betas_h, bool modes) {
     CK(cudaMemcpyAsync(c->betas.p, betas_h, nbeta * sizeof(double), cudaMemcpyHostToDevice, c->st));
     CK(hg::launch_incident(c->st, c->n, c->xyz_p.p, c->dxyz.p, nbeta, c->betas.p, c->v, c->wk, c->w1, c->h, c->W.p));
   }
-  if (mixed(c))
-    CK(hg::launch_rhs<float2>(c->st, c->n, c->tn, c->Sf.p, c->tn, c->dxyz.p, c->body_of.p, c->nbody, nbeta, c->W.p,
-                              c->part.p, c->B.p, c->tn));
-  else
+  if (mixed(c)) {
+    // B = S [modes | headings] as one product of the single-precision S
+    const int nc = 6 * c->nbody + nbeta;
+    CK(c->Wz.ensure((size_t)c->n * nc));
+    CK(hg::launch_rhs_cols(c->st, c->n, c->dxyz.p, c->body_of.p, c->nbody, nbeta, c->W.p, c->Wz.p, c->n));
+    CK(hg::resid_df(c->st, false, c->tn, nc, c->n, c->Sf.p, c->tn, c->Wz.p, c->n, nullptr, 0, 1.0, c->B.p, c->tn,
+                    c->rws.p, c->rws.cap, false));
+  } else
     CK(hg::launch_rhs<double2>(c->st, c->n, c->tn, c->S.p, c->tn, c->dxyz.p, c->body_of.p, c->nbody, nbeta, c->W.p,
                                c->part.p, c->B.p, c->tn));
   (void)modes;
@@ -316,7 +320,7 @@ void hg_destroy(hg_ctx* c) {
   for (auto* b : dbs) b->release();
   DevBuf<int>* ibs[] = {&c->ncon, &c->ncn, &c->body_of, &c->body_start, &c->body_end, &c->ipiv, &c->status, &c->info};
   for (auto* b : ibs) b->release();
-  DevBuf<double2>* zbs[] = {&c->A, &c->S, &c->C, &c->A64, &c->B, &c->X, &c->R, &c->R2, &c->W, &c->part, &c->exfc, &c->gws};
+  DevBuf<double2>* zbs[] = {&c->A, &c->S, &c->C, &c->A64, &c->B, &c->X, &c->R, &c->R2, &c->W, &c->Wz, &c->part, &c->exfc, &c->gws};
   for (auto* b : zbs) b->release();
   DevBuf<float2>* cbs[] = {&c->Af, &c->Sf, &c->Cf, &c->Bf, &c->Aof};
   for (auto* b : cbs) b->release();
@@ -500,6 +504,7 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
   CK(cudaEventElapsedTime(&c->stage_ms[1], c->ev[1], c->ev[2]));
   c->factored = (info == 0);
   c->rad_done = c->dif_done = false;
+  if (info < 0) return fail(c, HG_ERR_DEVICE, "LU panel: a bounded cluster wait ran out (info %d)", info);
   if (info != 0) return fail(c, info, "zero pivot at row %d", info);
   return 0;
 }
@@ -711,6 +716,7 @@ int hg_gesv(hg_ctx* c, int precision, int n, int nrhs, double* a, int lda, int* 
     CK(hg::getrf<float>(c->st, n, dAf.p, n, dpiv.p, dinfo.p, nullptr));
     CK(cudaMemcpyAsync(&inf, dinfo.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
+    if (inf < 0) return fail(c, HG_ERR_DEVICE, "LU panel: a bounded cluster wait ran out (info %d)", inf);
     if (inf != 0) {
       // a zero pivot in complex64: fall back to the complex128 factorisation
       fp64 = true;
@@ -754,6 +760,7 @@ int hg_gesv(hg_ctx* c, int precision, int n, int nrhs, double* a, int lda, int* 
     CK(hg::getrf<double>(c->st, n, dA.p, n, dpiv.p, dinfo.p, nullptr));
     CK(cudaMemcpyAsync(&inf, dinfo.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
+    if (inf < 0) return fail(c, HG_ERR_DEVICE, "LU panel: a bounded cluster wait ran out (info %d)", inf);
     if (inf == 0 && nrhs > 0) CK(hg::getrs<double>(c->st, n, nrhs, dA.p, n, dpiv.p, dB.p, n));
     result = dB.p;
   }

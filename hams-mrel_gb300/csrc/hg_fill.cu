@@ -194,9 +194,9 @@ k_green_fill_mixed(const double* __restrict__ rec, const double* __restrict__ fx
     bulk_g2s(tile, rec + (size_t)col0 * PR_SIZE, (uint32_t)(ncol * PR_SIZE * sizeof(double)), &bar);
   }
   __syncthreads();
-  if (!mbar_wait_bounded(&bar, 0, 1L << 24)) {
+  if (!mbar_wait_timed(&bar, 0, 2000000000ull)) {
     hg_set_status(status, HG_DEV_WAIT_TIMEOUT);
-    mbar_wait_bounded(&bar, 0, 1L << 24);
+    mbar_wait_timed(&bar, 0, 2000000000ull);
     return;
   }
   if (threadIdx.x < ncol) {
@@ -413,6 +413,25 @@ template cudaError_t launch_rhs<double2>(cudaStream_t, int, int, const double2*,
                                          int, const double2*, double2*, double2*, long);
 template cudaError_t launch_rhs<float2>(cudaStream_t, int, int, const float2*, long, const double*, const int*, int,
                                         int, const double2*, double2*, double2*, long);
+
+__global__ void k_rhs_cols(int n, const double* __restrict__ dxyz_p, const int* __restrict__ body_of, int nbody,
+                           int nbeta, const double2* __restrict__ w, double2* __restrict__ W, long ldw) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+  if (j >= n) return;
+  double2 v = make_double2(0.0, 0.0);
+  if (c < 6 * nbody) {
+    if (body_of[j] == c / 6) v.x = dxyz_p[j + (size_t)(c % 6) * n];
+  } else {
+    v = w[j + (size_t)(c - 6 * nbody) * n];
+  }
+  W[j + (long)c * ldw] = v;
+}
+
+cudaError_t launch_rhs_cols(cudaStream_t st, int n, const double* dxyz_p, const int* body_of, int nbody, int nbeta,
+                            const double2* w, double2* W, long ldw) {
+  k_rhs_cols<<<dim3((n + 255) / 256, 6 * nbody + nbeta), 256, 0, st>>>(n, dxyz_p, body_of, nbody, nbeta, w, W, ldw);
+  return cudaGetLastError();
+}
 
 // ---------------------------------------------------------------------------
 // Forces.  One CTA per (body m, potential column c): six direction sums over

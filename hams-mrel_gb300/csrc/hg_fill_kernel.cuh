@@ -31,9 +31,9 @@ k_green_fill(const double* __restrict__ rec, const double* __restrict__ fx /* ld
     bulk_g2s(tile, rec + (size_t)col0 * PR_SIZE, (uint32_t)(ncol * PR_SIZE * sizeof(double)), &bar);
   }
   __syncthreads();
-  if (!mbar_wait_bounded(&bar, 0, 1L << 24)) {
+  if (!mbar_wait_timed(&bar, 0, 2000000000ull)) {
     hg_set_status(status, HG_DEV_WAIT_TIMEOUT);
-    mbar_wait_bounded(&bar, 0, 1L << 24);  // drain the copy before shared memory goes away
+    mbar_wait_timed(&bar, 0, 2000000000ull);  // drain the copy before shared memory goes away
     return;
   }
   const int i = blockIdx.x * FILL_ROWS + threadIdx.x;

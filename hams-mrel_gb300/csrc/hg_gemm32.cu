@@ -224,7 +224,128 @@ cudaError_t launch_wide(cudaStream_t st, int m, int n, int k, float2 alpha, cons
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Skinny products, N <= 40 (the blocked triangular solves' updates
+// B2 -= L21 X1 with all right-hand sides at once): 32 rows x CW = 4*CPT
+// columns per CTA, 128 threads (one row x CPT columns each), 32-deep stages
+// double-buffered by cp.async.  Small tiles give enough CTAs to fill the GPU
+// without splitting K.
+// ---------------------------------------------------------------------------
+constexpr int kSRows = 32, kSK = 32, kSThreads = 128, kSMaxCW = 40;
+
+template <int CPT, bool VEC>
+__device__ __forceinline__ void skinny_stage(float2* As, float2* Bs, const float2* __restrict__ A, long lda,
+                                             const float2* __restrict__ B, long ldb, int m, int n, int k, int m0,
+                                             int k0, int tid) {
+  constexpr int CW = 4 * CPT;
+  if (VEC) {
+#pragma unroll
+    for (int it = 0; it < kSK * kSRows / 2 / kSThreads; ++it) {
+      const int e = tid + it * kSThreads;
+      const int i = (e % (kSRows / 2)) * 2, l = e / (kSRows / 2);
+      const int gm = m0 + i, gk = k0 + l;
+      int bytes = 0;
+      if (gk < k) bytes = (gm + 1 < m) ? 16 : (gm < m ? 8 : 0);
+      cp_async16(As + l * kSRows + i, bytes ? A + gm + (long)gk * lda : A, bytes);
+    }
+  } else {
+#pragma unroll
+    for (int it = 0; it < kSK * kSRows / kSThreads; ++it) {
+      const int e = tid + it * kSThreads;
+      const int i = e % kSRows, l = e / kSRows;
+      const int gm = m0 + i, gk = k0 + l;
+      const bool ok = gm < m && gk < k;
+      cp_async8(As + l * kSRows + i, ok ? A + gm + (long)gk * lda : A, ok);
+    }
+  }
+  for (int e = tid; e < kSK * CW; e += kSThreads) {
+    const int l = e % kSK, c = e / kSK;
+    const int gk = k0 + l;
+    const bool ok = c < n && gk < k;
+    cp_async8(Bs + l * CW + c, ok ? B + gk + (long)c * ldb : B, ok);
+  }
+}
+
+template <int CPT, bool VEC>
+__global__ void __launch_bounds__(kSThreads)
+k_cgemm_skinny(int m, int n, int k, float2 alpha, const float2* __restrict__ A, long lda,
+               const float2* __restrict__ B, long ldb, float2 beta, float2* __restrict__ C, long ldc) {
+  constexpr int CW = 4 * CPT;
+  __shared__ __align__(16) float2 As[2][kSK * kSRows];
+  __shared__ __align__(16) float2 Bs[2][kSK * CW];
+  const int tid = threadIdx.x, tx = tid & 31, cg = tid >> 5;
+  const int m0 = blockIdx.x * kSRows;
+  float ar[CPT], ai[CPT];
+#pragma unroll
+  for (int j = 0; j < CPT; ++j) { ar[j] = 0.f; ai[j] = 0.f; }
+  const int nst = (k + kSK - 1) / kSK;
+  skinny_stage<CPT, VEC>(As[0], Bs[0], A, lda, B, ldb, m, n, k, m0, 0, tid);
+  cp_async_commit();
+  for (int s = 0; s < nst; ++s) {
+    const int b = s & 1;
+    if (s + 1 < nst) skinny_stage<CPT, VEC>(As[b ^ 1], Bs[b ^ 1], A, lda, B, ldb, m, n, k, m0, (s + 1) * kSK, tid);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    const float2* as = As[b];
+    const float2* bs = Bs[b] + cg * CPT;
+#pragma unroll 4
+    for (int l = 0; l < kSK; ++l) {
+      const float2 a = as[l * kSRows + tx];
+#pragma unroll
+      for (int j = 0; j < CPT; j += 2) {
+        const float4 bb = *reinterpret_cast<const float4*>(bs + l * CW + j);
+        ar[j] = fmaf(a.x, bb.x, ar[j]);
+        ar[j] = fmaf(-a.y, bb.y, ar[j]);
+        ai[j] = fmaf(a.x, bb.y, ai[j]);
+        ai[j] = fmaf(a.y, bb.x, ai[j]);
+        ar[j + 1] = fmaf(a.x, bb.z, ar[j + 1]);
+        ar[j + 1] = fmaf(-a.y, bb.w, ar[j + 1]);
+        ai[j + 1] = fmaf(a.x, bb.w, ai[j + 1]);
+        ai[j + 1] = fmaf(a.y, bb.z, ai[j + 1]);
+      }
+    }
+    __syncthreads();
+  }
+  const int row = m0 + tx;
+  if (row >= m) return;
+  const bool zb = (beta.x == 0.f && beta.y == 0.f);
+#pragma unroll
+  for (int j = 0; j < CPT; ++j) {
+    const int col = cg * CPT + j;
+    if (col < n) {
+      float2* c = C + row + (long)col * ldc;
+      const float2 o = zb ? make_float2(0.f, 0.f) : *c;
+      *c = axpby(alpha, ar[j], ai[j], beta, o);
+    }
+  }
+}
+
+template <int CPT>
+cudaError_t launch_skinny(cudaStream_t st, bool vec, int m, int n, int k, float2 alpha, const float2* A, long lda,
+                          const float2* B, long ldb, float2 beta, float2* C, long ldc) {
+  const dim3 grid((m + kSRows - 1) / kSRows);
+  if (vec)
+    k_cgemm_skinny<CPT, true><<<grid, kSThreads, 0, st>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  else
+    k_cgemm_skinny<CPT, false><<<grid, kSThreads, 0, st>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  return cudaGetLastError();
+}
+
 }  // namespace
+
+cudaError_t cgemm_skinny(cudaStream_t st, int m, int n, int k, float2 alpha, const float2* A, long lda,
+                         const float2* B, long ldb, float2 beta, float2* C, long ldc) {
+  if (m <= 0 || n <= 0) return cudaSuccess;
+  if (n > kSMaxCW) return cudaErrorInvalidValue;
+  const bool vec = (reinterpret_cast<uintptr_t>(A) % 16 == 0) && (lda % 2 == 0);
+  const int per = (n + 3) / 4;
+  if (per <= 2) return launch_skinny<2>(st, vec, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  if (per <= 4) return launch_skinny<4>(st, vec, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  if (per <= 6) return launch_skinny<6>(st, vec, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  if (per <= 8) return launch_skinny<8>(st, vec, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  return launch_skinny<10>(st, vec, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
 
 cudaError_t cgemm_wide(cudaStream_t st, bool transa, int m, int n, int k, float2 alpha, const float2* A, long lda,
                        const float2* B, long ldb, float2 beta, float2* C, long ldc) {

@@ -36,6 +36,13 @@ template <typename IN>
 cudaError_t launch_rhs(cudaStream_t st, int n, int tn, const IN* S, long lds, const double* dxyz_p, const int* body_of,
                        int nbody, int nbeta, const double2* w, double2* part, double2* B, long ldb);
 
+// Source columns of the right-hand sides as one n x (6 nbody + nbeta) complex
+// matrix: column 6b + k holds the k-th generalised normal on body b's panels
+// (zero elsewhere), column 6 nbody + h the incident normal velocity w[:, h].
+// B = S W then gives every right-hand side at once.
+cudaError_t launch_rhs_cols(cudaStream_t st, int n, const double* dxyz_p, const int* body_of, int nbody, int nbeta,
+                            const double2* w, double2* W, long ldw);
+
 cudaError_t launch_forces(cudaStream_t st, int n, const double2* X, long ldx, const double* xyz_p, const double* ds,
                           const double* dxyz_p, const int* body_start, const int* body_end, int nbody, int nbeta,
                           const double* betas, double v, double wk, double w1, double h, int isol, double rho,

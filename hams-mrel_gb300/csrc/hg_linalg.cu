@@ -25,9 +25,9 @@ template <typename T> __device__ __forceinline__ T cmul(T a, T b) {
 }
 template <typename T> __device__ __forceinline__ T csub(T a, T b) { T r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
 template <typename T> __device__ __forceinline__ T crecip(T a) {
-  // 1/a with Smith's scaling
+  // 1/a with Smith's scaling, compared in the element type
   T r;
-  if (fabs((double)a.x) >= fabs((double)a.y)) {
+  if (fabs(a.x) >= fabs(a.y)) {
     auto q = a.y / a.x, d = a.x + a.y * q;
     r.x = 1 / d; r.y = -q / d;
   } else {
@@ -196,6 +196,10 @@ template <>
 cudaError_t gemm<float>(cudaStream_t st, bool transa, int m, int n, int k, float2 alpha, const float2* A,
                         long lda, const float2* B, long ldb, float2 beta, float2* C, long ldc, void* ws,
                         size_t ws_bytes) {
+  // Split-K (a workspace and a deep K) keeps the older kernel; otherwise
+  // the cp.async kernels: skinny (N <= 40) or wide.
+  const bool splitk = ws && k >= 1024;
+  if (!transa && n <= 40 && !splitk) return cgemm_skinny(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
   if (n <= 64)
     return launch_gemm<float, 64, 32, 8, 4, 2>(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, ws, ws_bytes);
   return cgemm_wide(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);

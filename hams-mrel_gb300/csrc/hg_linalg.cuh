@@ -30,10 +30,16 @@ cudaError_t cgemm_wide(cudaStream_t st, bool transa, int m, int n, int k, float2
 // Bin complex128 (Bin may be null), result complex128 in double-float
 // arithmetic on the FP32 pipes.  M x NC result, inner dimension K.  ws: a
 // 256-byte aligned device workspace of at least resid_work_bytes(m, nc, k).
+// exact = false: single-precision products and 32-term partial sums,
+// compensated across partial sums (untransposed A only).
 size_t resid_work_bytes(int m, int nc, int k);
 cudaError_t resid_df(cudaStream_t st, bool transa, int m, int nc, int k, const float2* A, long lda, const double2* Y,
                      long ldy, const double2* Bin, long ldb, double sign, double2* out, long ldo, void* ws,
-                     size_t ws_bytes);
+                     size_t ws_bytes, bool exact = true);
+
+// Complex64 GEMM for N <= 40 untransposed (hg_gemm32.cu), without split-K.
+cudaError_t cgemm_skinny(cudaStream_t st, int m, int n, int k, float2 alpha, const float2* A, long lda,
+                         const float2* B, long ldb, float2 beta, float2* C, long ldc);
 
 // In-place LU with partial pivoting of the n x n matrix A (lda).  ipiv is a
 // device array of n 1-based pivot rows, LAPACK style.  info (device int) is
@@ -53,6 +59,10 @@ size_t lu_work_bytes(int n);
 // [0, jb <= 32) of P, pivots written 1-based as k0 + row + 1.
 template <typename R>
 cudaError_t panel_cluster(cudaStream_t st, typename cx<R>::T* P, long lda, int m, int jb, int* ipiv, int k0, int* info);
+template <>
+cudaError_t panel_cluster<float>(cudaStream_t st, float2* P, long lda, int m, int jb, int* ipiv, int k0, int* info);
+template <>
+cudaError_t panel_cluster<double>(cudaStream_t st, double2* P, long lda, int m, int jb, int* ipiv, int k0, int* info);
 template <typename R>
 bool panel_cluster_supported(int m);
 // Column-parallel triangular solve of a jb <= 256 diagonal block for ncols columns.

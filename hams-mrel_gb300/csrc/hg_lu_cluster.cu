@@ -23,9 +23,11 @@ template <typename T> __device__ __forceinline__ T c_mul(T a, T b) {
   T r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
 }
 template <typename T> __device__ __forceinline__ T c_sub(T a, T b) { T r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+// Smith's algorithm; the comparisons stay in the element type (a double
+// conversion would run on the FP64 pipes, 1/64 of the FP32 rate here).
 template <typename T> __device__ __forceinline__ T c_recip(T a) {
   T r;
-  if (fabs((double)a.x) >= fabs((double)a.y)) {
+  if (fabs(a.x) >= fabs(a.y)) {
     auto q = a.y / a.x, d = a.x + a.y * q;
     r.x = 1 / d; r.y = -q / d;
   } else {
@@ -34,18 +36,6 @@ template <typename T> __device__ __forceinline__ T c_recip(T a) {
   }
   return r;
 }
-template <typename T> __device__ __forceinline__ T c_div(T a, T b) {
-  T r;
-  if (fabs((double)b.x) >= fabs((double)b.y)) {
-    auto q = b.y / b.x, d = b.x + b.y * q;
-    r.x = (a.x + a.y * q) / d; r.y = (a.y - a.x * q) / d;
-  } else {
-    auto q = b.x / b.y, d = b.y + b.x * q;
-    r.x = (a.x * q + a.y) / d; r.y = (a.y * q - a.x) / d;
-  }
-  return r;
-}
-
 constexpr int kClusterCTAs = 16;
 constexpr int kClusterNB = 32;
 constexpr int kClusterThreads = 512;
@@ -200,9 +190,182 @@ k_getf2_cluster(typename cx<R>::T* __restrict__ P, long lda, int m, int jb, int 
   }
 }
 
+// Single-precision panel with pushed candidates.  The per-column exchange is
+// the latency-critical step of the whole LU (n column steps in sequence), so
+// it is done with the cluster's asynchronous copy engine instead of loads:
+// every CTA packs one message (its candidate's value, index and row, and, if
+// it owns row jj, row jj) and sends it with 16 bulk copies into slot [rank]
+// of every CTA's receive buffer, each copy completing on the receiver's
+// mbarrier.  A CTA then waits on its own mbarrier (bounded) and finds the
+// pivot among 16 local messages: no cluster barrier and no remote loads per
+// column, 16 bulk transfers instead of thousands of small DSMEM requests.
+//
+// Buffers alternate by column parity q.  Reuse is safe one step ahead: a CTA
+// sends column jj + 2's message only after receiving everyone's column jj + 1
+// message, which each CTA sends only after it has finished reading the
+// column-jj slots (and its own column-jj copies have landed everywhere).  For
+// the same reason a copy can only reach an mbarrier whose previous phase has
+// completed.  The mbarrier of parity q is re-armed (one arrival with the
+// expected bytes) right after its phase completes.
+struct __align__(16) PanelMsg {
+  float val;
+  int idx;
+  int pad[2];
+  float2 cand[kClusterNB];  // the candidate row
+  float2 jrow[kClusterNB];  // row jj, from its owner only
+};
+static_assert(sizeof(PanelMsg) % 16 == 0, "bulk copies move multiples of 16 bytes");
+constexpr uint64_t kPanelWaitNs = 2000000000ull;  // 2 s
+constexpr int kPanelTimeout = -1000;  // info value of a wait that ran out
+
+__device__ __forceinline__ bool better(float v, int i, float bv, int bi) {
+  return v > bv || (v == bv && i < bi);
+}
+
+__global__ void __launch_bounds__(kClusterThreads, 1)
+k_getf2_cluster_push(float2* __restrict__ P, long lda, int m, int jb, int rpc, int* __restrict__ ipiv, int k0,
+                     int* __restrict__ info) {
+  constexpr int kWarps = kClusterThreads / 32;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* tile = reinterpret_cast<float2*>(smem_raw);  // [jb][rpc], row index fastest
+  __shared__ PanelMsg sendbuf[2];
+  __shared__ PanelMsg recv[2][kClusterCTAs];
+  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ float red_v[kWarps];
+  __shared__ int red_i[kWarps];
+  __shared__ int s_bad;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int r0 = rank * rpc;
+  const int rl = max(0, min(rpc, m - r0));
+  constexpr uint32_t kMsgBytes = sizeof(PanelMsg);
+
+  for (int e = tid; e < rl * jb; e += blockDim.x) {
+    const int r = e % rl, c = e / rl;
+    tile[c * rpc + r] = P[(r0 + r) + (long)c * lda];
+  }
+  if (tid == 0) {
+    s_bad = 0;
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    mbar_expect_tx(&mbar[0], kClusterCTAs * kMsgBytes);
+    if (jb > 1) mbar_expect_tx(&mbar[1], kClusterCTAs * kMsgBytes);
+  }
+  cluster.sync();  // barriers initialised and armed everywhere before any copy
+
+  bool bad = false;
+  for (int jj = 0; jj < jb; ++jj) {
+    const int q = jj & 1;
+    const int oj = jj / rpc, lj = jj - oj * rpc;
+    // (a) this CTA's candidate for column jj (rows >= jj)
+    float v = -1.f;
+    int idx = INT_MAX;
+    for (int r = tid; r < rl; r += blockDim.x) {
+      if (r0 + r >= jj) {
+        const float2 a = tile[jj * rpc + r];
+        const float av = fabsf(a.x) + fabsf(a.y);
+        if (better(av, r0 + r, v, idx)) { v = av; idx = r0 + r; }
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const float ov = __shfl_down_sync(0xffffffffu, v, off);
+      const int oi = __shfl_down_sync(0xffffffffu, idx, off);
+      if (better(ov, oi, v, idx)) { v = ov; idx = oi; }
+    }
+    if (lane == 0) { red_v[warp] = v; red_i[warp] = idx; }
+    __syncthreads();  // also orders every thread's column jj - 1 updates before the copies below
+    if (warp == 0) {
+      v = (lane < kWarps) ? red_v[lane] : -1.f;
+      idx = (lane < kWarps) ? red_i[lane] : INT_MAX;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const float ov = __shfl_down_sync(0xffffffffu, v, off);
+        const int oi = __shfl_down_sync(0xffffffffu, idx, off);
+        if (better(ov, oi, v, idx)) { v = ov; idx = oi; }
+      }
+      v = __shfl_sync(0xffffffffu, v, 0);
+      idx = __shfl_sync(0xffffffffu, idx, 0);
+      // (b) pack and push the message
+      PanelMsg& msg = sendbuf[q];
+      if (lane == 0) { msg.val = v; msg.idx = idx; }
+      if (lane < jb) {
+        if (idx != INT_MAX) msg.cand[lane] = tile[lane * rpc + (idx - r0)];
+        if (rank == oj) msg.jrow[lane] = tile[lane * rpc + lj];
+      }
+      fence_proxy_async_smem();
+      __syncwarp();
+      if (lane < kClusterCTAs) {
+        const uint32_t dst = mapa_shared(smem_addr(&recv[q][rank]), lane);
+        const uint32_t bar = mapa_shared(smem_addr(&mbar[q]), lane);
+        bulk_s2s_cluster(dst, smem_addr(&msg), kMsgBytes, bar);
+      }
+    }
+    // (c) wait for the 16 messages of this column
+    if (!mbar_wait_timed(&mbar[q], (jj >> 1) & 1, kPanelWaitNs)) bad = true;
+    if (__syncthreads_or(bad)) {
+      if (tid == 0) s_bad = 1;
+      break;
+    }
+    if (tid == 0 && jj + 2 < jb) mbar_expect_tx(&mbar[q], kClusterCTAs * kMsgBytes);
+    // (d) the pivot: every warp reduces the 16 local messages
+    float pmax = (lane < kClusterCTAs) ? recv[q][lane].val : -1.f;
+    int p = (lane < kClusterCTAs) ? recv[q][lane].idx : INT_MAX;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const float ov = __shfl_down_sync(0xffffffffu, pmax, off);
+      const int oi = __shfl_down_sync(0xffffffffu, p, off);
+      if (better(ov, oi, pmax, p)) { pmax = ov; p = oi; }
+    }
+    pmax = __shfl_sync(0xffffffffu, pmax, 0);
+    p = __shfl_sync(0xffffffffu, p, 0);
+    if (p == INT_MAX) p = jj;
+    const int op = p / rpc;
+    const float2* prow = recv[q][op].cand;
+    const float2* jrow = recv[q][oj].jrow;
+    const bool swap = pmax > 0.f && p != jj;
+    if (rank == 0 && tid == 0) {
+      ipiv[k0 + jj] = k0 + p + 1;
+      if (!(pmax > 0.f) && *info == 0) *info = k0 + jj + 1;
+    }
+    // (e) row jj becomes the pivot row; the owner of row p takes old row jj
+    if (swap && rank == oj && tid < jb) tile[tid * rpc + lj] = prow[tid];
+    if (pmax > 0.f) {
+      const float2 rp = c_recip(prow[jj]);
+      for (int r = tid; r < rl; r += blockDim.x) {
+        const int gr = r0 + r;
+        if (gr <= jj) continue;
+        if (swap && gr == p) {
+          for (int c = 0; c < jb; ++c) tile[c * rpc + r] = jrow[c];
+        }
+        const float2 l = c_mul(tile[jj * rpc + r], rp);
+        tile[jj * rpc + r] = l;
+        for (int c = jj + 1; c < jb; ++c) {
+          const float2 u = prow[c];
+          float2 a = tile[c * rpc + r];
+          a.x = fmaf(-l.x, u.x, fmaf(l.y, u.y, a.x));
+          a.y = fmaf(-l.x, u.y, fmaf(-l.y, u.x, a.y));
+          tile[c * rpc + r] = a;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (s_bad) {
+    if (rank == 0 && tid == 0) *info = kPanelTimeout;
+  } else {
+    for (int e = tid; e < rl * jb; e += blockDim.x) {
+      const int r = e % rl, c = e / rl;
+      P[(r0 + r) + (long)c * lda] = tile[c * rpc + r];
+    }
+  }
+  cluster.sync();  // no CTA leaves while a copy into its shared memory could be pending
+}
+
 template <typename R>
-cudaError_t panel_cluster(cudaStream_t st, typename cx<R>::T* P, long lda, int m, int jb, int* ipiv, int k0,
-                          int* info) {
+cudaError_t panel_cluster_smem(cudaStream_t st, typename cx<R>::T* P, long lda, int m, int jb, int* ipiv, int k0,
+                               int* info) {
   typedef typename cx<R>::T T;
   if (jb > kClusterNB) return cudaErrorNotSupported;
   const int rpc = (m + kClusterCTAs - 1) / kClusterCTAs;
@@ -232,8 +395,41 @@ cudaError_t panel_cluster(cudaStream_t st, typename cx<R>::T* P, long lda, int m
   return cudaLaunchKernelEx(&cfg, kern, P, lda, m, jb, rpc, ipiv, k0, info);
 }
 
-template cudaError_t panel_cluster<float>(cudaStream_t, float2*, long, int, int, int*, int, int*);
-template cudaError_t panel_cluster<double>(cudaStream_t, double2*, long, int, int, int*, int, int*);
+// Single precision: the pushed-candidate panel (its tile plus the message
+// buffers must fit one CTA's shared memory), else the loading panel.
+constexpr int kPushStaticSmem = 20 * 1024;  // message buffers, barriers, reductions
+
+template <>
+cudaError_t panel_cluster<float>(cudaStream_t st, float2* P, long lda, int m, int jb, int* ipiv, int k0, int* info) {
+  if (jb > kClusterNB) return cudaErrorNotSupported;
+  const int rpc = (m + kClusterCTAs - 1) / kClusterCTAs;
+  const size_t smem = (size_t)rpc * jb * sizeof(float2);
+  if (smem > (size_t)(kPanelSmemMax - kPushStaticSmem)) return panel_cluster_smem<float>(st, P, lda, m, jb, ipiv, k0, info);
+  cudaError_t e = cudaFuncSetAttribute(k_getf2_cluster_push, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_getf2_cluster_push, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kPanelSmemMax - kPushStaticSmem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kClusterCTAs, 1, 1);
+  cfg.blockDim = dim3(kClusterThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kClusterCTAs;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_getf2_cluster_push, P, lda, m, jb, rpc, ipiv, k0, info);
+}
+template <>
+cudaError_t panel_cluster<double>(cudaStream_t st, double2* P, long lda, int m, int jb, int* ipiv, int k0,
+                                  int* info) {
+  return panel_cluster_smem<double>(st, P, lda, m, jb, ipiv, k0, info);
+}
+
 
 // Whether a 16-CTA cluster with the given dynamic shared memory can run here.
 template <typename R>
@@ -272,8 +468,8 @@ template bool panel_cluster_supported<double>(int);
 
 // ---------------------------------------------------------------------------
 // Triangular solves, one CTA per right-hand-side column (jb <= 256 rows):
-// X = L^{-1} X (unit lower) or X = U^{-1} X (upper, divides by the diagonal
-// as ZTRSM does).  The block is walked in sub-blocks of SB columns staged in
+// X = L^{-1} X (unit lower) or X = U^{-1} X (upper; multiplies by the
+// reciprocal of each diagonal entry, computed for a whole sub-block at once).  The block is walked in sub-blocks of SB columns staged in
 // shared memory by cp.async, the next sub-block in flight while the current
 // one is used.  One warp solves the SB x SB diagonal part with shuffles (no
 // CTA barrier per row), then every thread updates its own row with the SB
@@ -346,8 +542,11 @@ k_trsm_col(const T* __restrict__ A, long lda, int jb, T* __restrict__ X, long ld
           if (lane > j && lane < w) xr = c_sub(xr, c_mul(cur[j * kTrsmBlock + c0 + lane], xj));
         }
       } else {
+        // reciprocals of the diagonal, all lanes at once, off the serial chain
+        T rd = zero;
+        if (lane < w) rd = c_recip(cur[lane * kTrsmBlock + c0 + lane]);
         for (int j = w - 1; j >= 0; --j) {
-          if (lane == j) xr = c_div(xr, cur[j * kTrsmBlock + c0 + j]);
+          if (lane == j) xr = c_mul(xr, rd);
           const T xj = shfl_c(xr, j);
           if (lane < j) xr = c_sub(xr, c_mul(cur[j * kTrsmBlock + c0 + lane], xj));
         }

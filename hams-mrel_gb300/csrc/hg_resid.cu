@@ -17,6 +17,13 @@
 // contracting the TwoSum steps into fused operations, which would break the
 // error-free transformations.
 //
+// A cheaper mode (exact = false) serves products whose operands carry single
+// precision anyway (the mixed form's right-hand sides, B = S W with S from the
+// single-precision fill): products a * yh in FP32, summed in FP32 within each
+// 32-deep stage, and the stage sums accumulated with TwoSum as above, so the
+// error is that of a 32-term single-precision sum (~1e-7 of sum |a||y|), not
+// of an n-term one.
+//
 // Tiling: 64 rows x CW = 4*CPT columns per CTA, 256 threads (64 rows x 4
 // column groups of CPT), 32-deep stages of A (complex64) and of the split y
 // (float4 = yh.re, yl.re, yh.im, yl.im) double-buffered by cp.async.  The
@@ -121,7 +128,7 @@ __device__ __forceinline__ void resid_stage(float2* As, float4* Yt, const float2
   }
 }
 
-template <int CPT, bool TA, bool VEC>
+template <int CPT, bool TA, bool VEC, bool EXACT>
 __global__ void __launch_bounds__(kRThreads, 2)
 k_resid_df(int m, int nc, int k, int kchunk, const float2* __restrict__ A, long lda, const float4* __restrict__ Ys,
            double2* __restrict__ part) {
@@ -152,11 +159,34 @@ k_resid_df(int m, int nc, int k, int kchunk, const float2* __restrict__ A, long 
     __syncthreads();
     const float2* as = reinterpret_cast<const float2*>(cur);
     const float4* yt = reinterpret_cast<const float4*>(cur + kRATile) + cg * CPT;
+    if (EXACT) {
 #pragma unroll 4
-    for (int l = 0; l < kRK; ++l) {
-      const float2 a = as[l * kRRows + tx];
+      for (int l = 0; l < kRK; ++l) {
+        const float2 a = as[l * kRRows + tx];
 #pragma unroll
-      for (int j = 0; j < CPT; ++j) mac_df(a.x, a.y, yt[l * CW + j], Sr[j], sr[j], Si[j], si[j]);
+        for (int j = 0; j < CPT; ++j) mac_df(a.x, a.y, yt[l * CW + j], Sr[j], sr[j], Si[j], si[j]);
+      }
+    } else {
+      float pr[CPT], pi[CPT];
+#pragma unroll
+      for (int j = 0; j < CPT; ++j) { pr[j] = 0.f; pi[j] = 0.f; }
+#pragma unroll 4
+      for (int l = 0; l < kRK; ++l) {
+        const float2 a = as[l * kRRows + tx];
+#pragma unroll
+        for (int j = 0; j < CPT; ++j) {
+          const float4 y = yt[l * CW + j];
+          pr[j] = fmaf(a.x, y.x, pr[j]);
+          pr[j] = fmaf(-a.y, y.z, pr[j]);
+          pi[j] = fmaf(a.x, y.z, pi[j]);
+          pi[j] = fmaf(a.y, y.x, pi[j]);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < CPT; ++j) {
+        two_sum_acc(Sr[j], sr[j], pr[j]);
+        two_sum_acc(Si[j], si[j], pi[j]);
+      }
     }
     __syncthreads();
   }
@@ -202,7 +232,7 @@ int pick_cpt(int nc) {
 
 size_t align256(size_t b) { return (b + 255) / 256 * 256; }
 
-template <int CPT, bool TA, bool VEC>
+template <int CPT, bool TA, bool VEC, bool EXACT>
 cudaError_t launch_resid(cudaStream_t st, int m, int nc, int k, const float2* A, long lda, const double2* Y, long ldy,
                          const double2* Bin, long ldb, double sign, double2* out, long ldo, void* ws, size_t ws_bytes) {
   constexpr int CW = 4 * CPT;
@@ -218,7 +248,7 @@ cudaError_t launch_resid(cudaStream_t st, int m, int nc, int k, const float2* A,
   float4* Ys = static_cast<float4*>(ws);
   double2* part = reinterpret_cast<double2*>(static_cast<unsigned char*>(ws) + ys_bytes);
   k_split_y<<<4 * 152, 256, 0, st>>>(k, nc, CW, ncb, Y, ldy, Ys);
-  auto kern = k_resid_df<CPT, TA, VEC>;
+  auto kern = k_resid_df<CPT, TA, VEC, EXACT>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRSmem);
   if (e != cudaSuccess) return e;
   kern<<<dim3(gx, ncb, slices), kRThreads, kRSmem, st>>>(m, nc, k, kchunk, A, lda, Ys, part);
@@ -227,12 +257,20 @@ cudaError_t launch_resid(cudaStream_t st, int m, int nc, int k, const float2* A,
 }
 
 template <int CPT>
-cudaError_t dispatch(cudaStream_t st, bool transa, bool vec, int m, int nc, int k, const float2* A, long lda,
-                     const double2* Y, long ldy, const double2* Bin, long ldb, double sign, double2* out, long ldo,
-                     void* ws, size_t ws_bytes) {
-  if (transa) return launch_resid<CPT, true, false>(st, m, nc, k, A, lda, Y, ldy, Bin, ldb, sign, out, ldo, ws, ws_bytes);
-  if (vec) return launch_resid<CPT, false, true>(st, m, nc, k, A, lda, Y, ldy, Bin, ldb, sign, out, ldo, ws, ws_bytes);
-  return launch_resid<CPT, false, false>(st, m, nc, k, A, lda, Y, ldy, Bin, ldb, sign, out, ldo, ws, ws_bytes);
+cudaError_t dispatch(cudaStream_t st, bool transa, bool vec, bool exact, int m, int nc, int k, const float2* A,
+                     long lda, const double2* Y, long ldy, const double2* Bin, long ldb, double sign, double2* out,
+                     long ldo, void* ws, size_t ws_bytes) {
+#define HG_RES(TA, V, EX) \
+  return launch_resid<CPT, TA, V, EX>(st, m, nc, k, A, lda, Y, ldy, Bin, ldb, sign, out, ldo, ws, ws_bytes)
+  if (!exact) {
+    if (transa) return cudaErrorNotSupported;
+    if (vec) HG_RES(false, true, false);
+    HG_RES(false, false, false);
+  }
+  if (transa) HG_RES(true, false, true);
+  if (vec) HG_RES(false, true, true);
+  HG_RES(false, false, true);
+#undef HG_RES
 }
 
 }  // namespace
@@ -245,17 +283,17 @@ size_t resid_work_bytes(int m, int nc, int k) {
 
 cudaError_t resid_df(cudaStream_t st, bool transa, int m, int nc, int k, const float2* A, long lda, const double2* Y,
                      long ldy, const double2* Bin, long ldb, double sign, double2* out, long ldo, void* ws,
-                     size_t ws_bytes) {
+                     size_t ws_bytes, bool exact) {
   if (m <= 0 || nc <= 0) return cudaSuccess;
   if (k <= 0) return cudaErrorInvalidValue;
   if (reinterpret_cast<uintptr_t>(ws) % 256 != 0) return cudaErrorInvalidValue;
   const bool vec = !transa && reinterpret_cast<uintptr_t>(A) % 16 == 0 && lda % 2 == 0;
   switch (pick_cpt(nc)) {
-    case 2: return dispatch<2>(st, transa, vec, m, nc, k, A, lda, Y, ldy, Bin, ldb, sign, out, ldo, ws, ws_bytes);
-    case 4: return dispatch<4>(st, transa, vec, m, nc, k, A, lda, Y, ldy, Bin, ldb, sign, out, ldo, ws, ws_bytes);
-    case 6: return dispatch<6>(st, transa, vec, m, nc, k, A, lda, Y, ldy, Bin, ldb, sign, out, ldo, ws, ws_bytes);
-    case 8: return dispatch<8>(st, transa, vec, m, nc, k, A, lda, Y, ldy, Bin, ldb, sign, out, ldo, ws, ws_bytes);
-    default: return dispatch<10>(st, transa, vec, m, nc, k, A, lda, Y, ldy, Bin, ldb, sign, out, ldo, ws, ws_bytes);
+    case 2: return dispatch<2>(st, transa, vec, exact, m, nc, k, A, lda, Y, ldy, Bin, ldb, sign, out, ldo, ws, ws_bytes);
+    case 4: return dispatch<4>(st, transa, vec, exact, m, nc, k, A, lda, Y, ldy, Bin, ldb, sign, out, ldo, ws, ws_bytes);
+    case 6: return dispatch<6>(st, transa, vec, exact, m, nc, k, A, lda, Y, ldy, Bin, ldb, sign, out, ldo, ws, ws_bytes);
+    case 8: return dispatch<8>(st, transa, vec, exact, m, nc, k, A, lda, Y, ldy, Bin, ldb, sign, out, ldo, ws, ws_bytes);
+    default: return dispatch<10>(st, transa, vec, exact, m, nc, k, A, lda, Y, ldy, Bin, ldb, sign, out, ldo, ws, ws_bytes);
   }
 }
 

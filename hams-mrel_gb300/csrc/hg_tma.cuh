@@ -1,8 +1,8 @@
 // Asynchronous copies into shared memory.
 //  - Bulk copies (the TMA engine's non-tensor form) completed on an mbarrier.
-//    Every mbarrier wait is bounded: a wait that runs out of iterations
-//    reports failure and the caller records it in the device status word
-//    instead of spinning forever.
+//    Every mbarrier wait is bounded in time: a wait that runs out reports
+//    failure and the caller records it (device status word, LU info) instead
+//    of spinning forever.
 //  - Per-thread cp.async copies of 8 or 16 bytes with zero fill, grouped by
 //    commit/wait_group (waits on the thread's own copies, which always end).
 #pragma once
@@ -44,12 +44,44 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
   return ok != 0;
 }
 
-// Returns false if the phase did not complete within max_iter polls.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase, long max_iter) {
-  for (long it = 0; it < max_iter; ++it) {
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Returns false if the phase did not complete within ns_limit nanoseconds
+// (try_wait may suspend the thread for a while per poll, so the limit is on
+// elapsed time, not on the number of polls).
+__device__ __forceinline__ bool mbar_wait_timed(uint64_t* bar, uint32_t phase, uint64_t ns_limit) {
+  if (mbar_try_wait(bar, phase)) return true;
+  const uint64_t t0 = global_ns();
+  for (;;) {
     if (mbar_try_wait(bar, phase)) return true;
+    if (global_ns() - t0 > ns_limit) return false;
   }
-  return false;
+}
+
+// Address of the same shared-memory variable in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t mapa_shared(uint32_t addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+
+// Bulk copy from this CTA's shared memory into another CTA's shared memory of
+// the cluster, completed on that CTA's mbarrier (dst and mbar are cluster
+// addresses from mapa_shared; 16-byte aligned, bytes a multiple of 16).
+__device__ __forceinline__ void bulk_s2s_cluster(uint32_t dst, uint32_t src, uint32_t bytes, uint32_t mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "r"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+
+// Orders this thread's generic-proxy writes to shared memory before later
+// async-proxy reads of it (the bulk copies).
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
 // 8-byte copy; pred false writes zeros and reads nothing.
