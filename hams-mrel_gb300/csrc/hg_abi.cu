@@ -66,6 +66,7 @@ struct hg_ctx {
   DevBuf<double2> A, S, C, A64, B, X, R, R2, W, Wz, part, exfc, gws;  // gws: split-K GEMM workspace
   DevBuf<float2> Af, Sf, Cf, Bf, Aof;  // Aof: unfactorised copy of Af (mixed form, irsp = 0)
   DevBuf<unsigned char> rws;             // workspace of the double-float residual
+  DevBuf<unsigned char> luws;            // packed operands of the tensor-core LU updates
   DevBuf<double> amas, bdmp;
   int irsp = 0;
   bool factored = false;
@@ -286,6 +287,7 @@ void hg_default_opts(hg_opts* o) {
   o->refine_tol = 1e-10;
   o->rho = 1000.0;
   o->g = 9.80665;
+  o->lu_tensor = 3;
 }
 
 int hg_create(hg_ctx** out, const hg_opts* opts) {
@@ -297,6 +299,7 @@ int hg_create(hg_ctx** out, const hg_opts* opts) {
   if (opts) c->o = *opts;
   if (c->o.precision != HG_PREC_FP64 && c->o.precision != HG_PREC_MIXED) { delete c; return -2; }
   if (c->o.grn_kind != 4 && c->o.grn_kind != 8) { delete c; return -2; }
+  if (c->o.lu_tensor != 0 && c->o.lu_tensor != 1 && c->o.lu_tensor != 3) { delete c; return -2; }
   cudaError_t e = cudaSetDevice(c->o.device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
   for (int k = 0; k < 5 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
@@ -489,9 +492,13 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
       CK(c->Cf.ensure((size_t)n * n));
       CK(hg::gemm<float>(c->st, true, n, n, tn, make_float2(1, 0), c->Af.p, tn, c->Af.p, tn, make_float2(0, 0), c->Cf.p,
                          n));
-      CK(hg::getrf<float>(c->st, n, c->Cf.p, n, c->ipiv.p, c->info.p, nullptr));
+    }
+    const size_t lwb = hg::lu_work_bytes(n, c->o.lu_tensor);
+    if (lwb) CK(c->luws.ensure(lwb));
+    if (irsp == 1) {
+      CK(hg::getrf<float>(c->st, n, c->Cf.p, n, c->ipiv.p, c->info.p, c->luws.p, lwb, c->o.lu_tensor));
     } else {
-      CK(hg::getrf<float>(c->st, n, c->Af.p, tn, c->ipiv.p, c->info.p, nullptr));
+      CK(hg::getrf<float>(c->st, n, c->Af.p, tn, c->ipiv.p, c->info.p, c->luws.p, lwb, c->o.lu_tensor));
     }
   }
   CK(cudaEventRecord(c->ev[2], c->st));
@@ -713,7 +720,10 @@ int hg_gesv(hg_ctx* c, int precision, int n, int nrhs, double* a, int lda, int* 
     CK(ws.ensure((size_t)16 * nb));
     CK(norms.ensure(2 * (size_t)(nrhs > 0 ? nrhs : 1)));
     CK(hg::convert_z2c(c->st, (long)nn, dA.p, dAf.p));
-    CK(hg::getrf<float>(c->st, n, dAf.p, n, dpiv.p, dinfo.p, nullptr));
+    DevBuf<unsigned char> luws;
+    const size_t lwb = hg::lu_work_bytes(n, c->o.lu_tensor);
+    if (lwb) CK(luws.ensure(lwb));
+    CK(hg::getrf<float>(c->st, n, dAf.p, n, dpiv.p, dinfo.p, luws.p, lwb, c->o.lu_tensor));
     CK(cudaMemcpyAsync(&inf, dinfo.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
     if (inf < 0) return fail(c, HG_ERR_DEVICE, "LU panel: a bounded cluster wait ran out (info %d)", inf);
@@ -776,19 +786,46 @@ int hg_gesv(hg_ctx* c, int precision, int n, int nrhs, double* a, int lda, int* 
   return 0;
 }
 
+namespace {
+
+// C -= A B with one of the library's complex GEMM kernels on device buffers
+// (variant 0 complex128 SIMT, 1 complex64 SIMT, 2 complex64 tensor cores
+// 3xTF32, 3 complex64 tensor cores TF32).
+cudaError_t gemm_variant(hg_ctx* c, int variant, int m, int n, int k, void* a, int lda, void* b, int ldb, void* cc,
+                         int ldc, void* ws, size_t ws_bytes, int* status) {
+  switch (variant) {
+    case 0:
+      return hg::gemm<double>(c->st, false, m, n, k, make_double2(-1, 0), (double2*)a, lda, (double2*)b, ldb,
+                              make_double2(1, 0), (double2*)cc, ldc);
+    case 1:
+      return hg::gemm<float>(c->st, false, m, n, k, make_float2(-1, 0), (float2*)a, lda, (float2*)b, ldb,
+                             make_float2(1, 0), (float2*)cc, ldc);
+    case 2:
+    case 3:
+      return hg::cgemm_tc(c->st, variant == 2 ? 3 : 1, m, n, k, (float2*)a, lda, (float2*)b, ldb, (float2*)cc, ldc, ws,
+                          ws_bytes, status);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
 int hg_bench_gemm(hg_ctx* c, int precision, int m, int n, int k, int iters, float* ms_per_launch) {
   if (!c) return -1;
-  if (precision != 0 && precision != 1) return fail(c, -2, "precision must be 0 or 1");
+  if (precision < 0 || precision > 3) return fail(c, -2, "precision must be 0..3");
+  if ((precision >= 2) && !hg::cgemm_tc_supported()) return fail(c, -2, "tensor-core GEMM needs an sm_103 device");
   if (m <= 0 || n <= 0 || k <= 0) return fail(c, -3, "bad shape");
   if (iters <= 0) return fail(c, -6, "iters must be positive");
   if (!ms_per_launch) return fail(c, -7, "ms_per_launch is NULL");
   cudaSetDevice(c->o.device);
   const size_t es = precision ? sizeof(float2) : sizeof(double2);
-  void *a = nullptr, *b = nullptr, *cc = nullptr;
+  const size_t wsb = precision >= 2 ? hg::cgemm_tc_work_bytes(m, n, k) : 0;
+  void *a = nullptr, *b = nullptr, *cc = nullptr, *ws = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaError_t e = cudaMalloc(&a, (size_t)m * k * es);
   if (e == cudaSuccess) e = cudaMalloc(&b, (size_t)k * n * es);
   if (e == cudaSuccess) e = cudaMalloc(&cc, (size_t)m * n * es);
+  if (e == cudaSuccess && wsb) e = cudaMalloc(&ws, wsb);
   if (e == cudaSuccess) e = cudaMemsetAsync(a, 0, (size_t)m * k * es, c->st);
   if (e == cudaSuccess) e = cudaMemsetAsync(b, 0, (size_t)k * n * es, c->st);
   if (e == cudaSuccess) e = cudaMemsetAsync(cc, 0, (size_t)m * n * es, c->st);
@@ -797,12 +834,7 @@ int hg_bench_gemm(hg_ctx* c, int precision, int m, int n, int k, int iters, floa
   for (int it = -1; it < iters && e == cudaSuccess; ++it) {
     if (it == 0) e = cudaEventRecord(e0, c->st);
     if (e != cudaSuccess) break;
-    if (precision)
-      e = hg::gemm<float>(c->st, false, m, n, k, make_float2(-1, 0), (float2*)a, m, (float2*)b, k, make_float2(1, 0),
-                          (float2*)cc, m);
-    else
-      e = hg::gemm<double>(c->st, false, m, n, k, make_double2(-1, 0), (double2*)a, m, (double2*)b, k,
-                           make_double2(1, 0), (double2*)cc, m);
+    e = gemm_variant(c, precision, m, n, k, a, m, b, k, cc, m, ws, wsb, c->status.p);
   }
   if (e == cudaSuccess) e = cudaEventRecord(e1, c->st);
   if (e == cudaSuccess) e = cudaEventSynchronize(e1);
@@ -811,9 +843,49 @@ int hg_bench_gemm(hg_ctx* c, int precision, int m, int n, int k, int iters, floa
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   cudaFree(a); cudaFree(b); cudaFree(cc);
+  if (ws) cudaFree(ws);
   if (e != cudaSuccess) return fail(c, HG_ERR_CUDA, "hg_bench_gemm: %s", cudaGetErrorString(e));
   *ms_per_launch = ms / iters;
-  return 0;
+  return check_status(c);
+}
+
+int hg_gemm_check(hg_ctx* c, int variant, int m, int n, int k, const double* a, int lda, const double* b, int ldb,
+                  double* cm, int ldc) {
+  if (!c) return -1;
+  if (variant < 0 || variant > 3) return fail(c, -2, "variant must be 0..3");
+  if (variant >= 2 && !hg::cgemm_tc_supported()) return fail(c, -2, "tensor-core GEMM needs an sm_103 device");
+  if (m <= 0 || n <= 0 || k <= 0) return fail(c, -3, "bad shape");
+  if (!a || lda < m) return fail(c, -6, "bad a / lda");
+  if (!b || ldb < k) return fail(c, -8, "bad b / ldb");
+  if (!cm || ldc < m) return fail(c, -10, "bad c / ldc");
+  CK(cudaSetDevice(c->o.device));
+  const size_t na = (size_t)lda * k, nb = (size_t)ldb * n, nc = (size_t)ldc * n;
+  DevBuf<double2> da, db, dc;
+  DevBuf<float2> fa, fb, fc;
+  DevBuf<unsigned char> ws;
+  CK(da.ensure(na));
+  CK(db.ensure(nb));
+  CK(dc.ensure(nc));
+  CK(cudaMemcpyAsync(da.p, a, na * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(db.p, b, nb * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(dc.p, cm, nc * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+  if (variant == 0) {
+    CK(gemm_variant(c, 0, m, n, k, da.p, lda, db.p, ldb, dc.p, ldc, nullptr, 0, c->status.p));
+  } else {
+    CK(fa.ensure(na));
+    CK(fb.ensure(nb));
+    CK(fc.ensure(nc));
+    CK(hg::convert_z2c(c->st, (long)na, da.p, fa.p));
+    CK(hg::convert_z2c(c->st, (long)nb, db.p, fb.p));
+    CK(hg::convert_z2c(c->st, (long)nc, dc.p, fc.p));
+    const size_t wsb = variant >= 2 ? hg::cgemm_tc_work_bytes(m, n, k) : 0;
+    if (wsb) CK(ws.ensure(wsb));
+    CK(gemm_variant(c, variant, m, n, k, fa.p, lda, fb.p, ldb, fc.p, ldc, ws.p, wsb, c->status.p));
+    CK(hg::convert_c2z(c->st, (long)nc, fc.p, dc.p));
+  }
+  CK(cudaMemcpyAsync(cm, dc.p, nc * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return check_status(c);
 }
 
 int hg_mark(hg_ctx* c, int slot) {

@@ -1,10 +1,13 @@
 // Blocked complex LU with partial pivoting and triangular solves.
 //
-// getrf: right-looking, panel width NB.  Per panel: a one-CTA panel
-// factorisation (pivot = max |re|+|im| as LAPACK's IZAMAX, row swaps,
-// reciprocal scaling, rank-1 updates), the row interchanges applied to the
-// columns outside the panel, a unit-lower triangular solve for the U12 block
-// and the trailing update A22 -= L21 U12, the only O(n^3) step.
+// getrf: right-looking, panel width NB = 32.  Per panel: the panel
+// factorisation (16-CTA cluster kernel, or one CTA when a cluster does not
+// fit: pivot = max |re|+|im| as LAPACK's IZAMAX, row swaps, reciprocal
+// scaling, rank-1 updates), the row interchanges applied to the columns
+// outside the panel, a unit-lower triangular solve for the U12 block and the
+// trailing update A22 -= L21 U12, the only O(n^3) step.  Complex64 with
+// tensor cores: two levels, 256-wide outer panels factorised by that loop
+// and their trailing updates on tcgen05 (hg_tc.cu).
 #include <climits>
 #include "hg_linalg.cuh"
 
@@ -356,31 +359,109 @@ __global__ void k_trsm_upper(const T* U, long lda, int jb, T* X, long ldx, int n
     if (r < jb) xc[r] = x[r];
 }
 
-size_t lu_work_bytes(int) { return 0; }
+// Outer panel width of the two-level LU whose trailing updates run on the
+// tensor cores: the inner dimension of the update GEMM (512 real), wide
+// enough that its C tile read and write amortise over the multiply.
+constexpr int kOuterNB = 256;
+// Below this order the one-level loop is used (few outer panels to amortise).
+constexpr int kTcMinN = 1024;
 
+// Workspace: the tensor-core GEMM's packed operands, then the 256 x 256
+// block I - L11^-1 used to form U12 by a GEMM.
+size_t lu_work_bytes(int n, int tc_passes) {
+  if (tc_passes == 0 || n < kTcMinN) return 0;
+  return cgemm_tc_work_bytes(n, n, kOuterNB) + (size_t)kOuterNB * kOuterNB * sizeof(float2) + 256;
+}
+
+namespace {
+
+// LU of the panel rows [k0, n) x columns [k0, k0 + jb) (jb <= 32), pivots
+// written 1-based as global rows.
 template <typename R>
-cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* ipiv, int* info, void*) {
+cudaError_t panel(cudaStream_t st, bool use_cluster, int n, typename cx<R>::T* A, long lda, int k0, int jb, int* ipiv,
+                  int* info) {
+  if (use_cluster) return panel_cluster<R>(st, A + k0 + (long)k0 * lda, lda, n - k0, jb, ipiv, k0, info);
+  k_getf2<R><<<1, kPanelThreads, 0, st>>>(A + k0 + (long)k0 * lda, lda, n - k0, jb, ipiv, k0, info);
+  return cudaGetLastError();
+}
+
+// Columns [c0, c1) of A through one level of right-looking blocking with
+// 32-wide panels (pivots applied only inside [c0, c1)).
+template <typename R>
+cudaError_t factor_columns(cudaStream_t st, bool use_cluster, int n, typename cx<R>::T* A, long lda, int c0, int c1,
+                           int* ipiv, int* info) {
   typedef typename cx<R>::T T;
-  cudaError_t e = cudaMemsetAsync(info, 0, sizeof(int), st);
-  if (e != cudaSuccess) return e;
   T mone, one;
   mone.x = -1; mone.y = 0; one.x = 1; one.y = 0;
-  const bool use_cluster = panel_cluster_supported<R>(n);
-  for (int k = 0; k < n; k += kNB) {
-    const int jb = (n - k < kNB) ? n - k : kNB;
-    if (use_cluster) {
-      e = panel_cluster<R>(st, A + k + (long)k * lda, lda, n - k, jb, ipiv, k, info);
-      if (e != cudaSuccess) return e;
-    } else {
-      k_getf2<R><<<1, kPanelThreads, 0, st>>>(A + k + (long)k * lda, lda, n - k, jb, ipiv, k, info);
-    }
-    k_laswp<T><<<(n + 127) / 128, 128, 0, st>>>(A, lda, n, ipiv, k, k + jb, k, k + jb);
-    const int rest = n - k - jb;
+  for (int k = c0; k < c1; k += kNB) {
+    const int jb = (c1 - k < kNB) ? c1 - k : kNB;
+    cudaError_t e = panel<R>(st, use_cluster, n, A, lda, k, jb, ipiv, info);
+    if (e != cudaSuccess) return e;
+    const int w = c1 - c0;
+    k_laswp<T><<<(w + 127) / 128, 128, 0, st>>>(A + (long)c0 * lda, lda, w, ipiv, k, k + jb, k - c0, k - c0 + jb);
+    const int rest = c1 - k - jb;
     if (rest > 0) {
       k_trsm_lower_unit<T><<<(rest + 127) / 128, 128, 0, st>>>(A + k + (long)k * lda, lda, jb,
                                                                  A + k + (long)(k + jb) * lda, lda, rest);
-      e = gemm<R>(st, false, rest, rest, jb, mone, A + (k + jb) + (long)k * lda, lda, A + k + (long)(k + jb) * lda,
-                  lda, one, A + (k + jb) + (long)(k + jb) * lda, lda);
+      e = gemm<R>(st, false, n - k - jb, rest, jb, mone, A + (k + jb) + (long)k * lda, lda,
+                  A + k + (long)(k + jb) * lda, lda, one, A + (k + jb) + (long)(k + jb) * lda, lda);
+      if (e != cudaSuccess) return e;
+    }
+  }
+  return cudaGetLastError();
+}
+
+__global__ void k_set_eye(int nb, float2* X) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+  if (r < nb) X[r + (long)c * nb] = make_float2(r == c ? 1.f : 0.f, 0.f);
+}
+// X <- I - X
+__global__ void k_eye_minus(int nb, float2* X) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+  if (r < nb) {
+    float2 v = X[r + (long)c * nb];
+    v.x = (r == c ? 1.f : 0.f) - v.x;
+    v.y = -v.y;
+    X[r + (long)c * nb] = v;
+  }
+}
+
+}  // namespace
+
+template <typename R>
+cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* ipiv, int* info, void* work,
+                  size_t work_bytes, int tc_passes) {
+  cudaError_t e = cudaMemsetAsync(info, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  const bool use_cluster = panel_cluster_supported<R>(n);
+  const bool tc = sizeof(R) == 4 && tc_passes != 0 && n >= kTcMinN && work &&
+                  work_bytes >= lu_work_bytes(n, tc_passes) && cgemm_tc_supported();
+  if (!tc) return factor_columns<R>(st, use_cluster, n, A, lda, 0, n, ipiv, info);
+  // Two levels: 256-wide outer panels factorised by the 32-wide loop above,
+  // then U12 = L11^-1 A12 and the tensor-core update A22 -= L21 U12.  U12
+  // is formed as A12 - (I - L11^-1) A12 on the tensor cores too, with
+  // L11^-1 from one column-parallel triangular solve of the identity (the
+  // GEMM packs its B operand, here A12, before it overwrites A12).
+  typedef typename cx<R>::T T;
+  const size_t tcb = cgemm_tc_work_bytes(n, n, kOuterNB);
+  float2* Minv = reinterpret_cast<float2*>(static_cast<char*>(work) + ((tcb + 255) / 256) * 256);
+  for (int K = 0; K < n; K += kOuterNB) {
+    const int jbo = (n - K < kOuterNB) ? n - K : kOuterNB;
+    e = factor_columns<R>(st, use_cluster, n, A, lda, K, K + jbo, ipiv, info);
+    if (e != cudaSuccess) return e;
+    k_laswp<T><<<(n + 127) / 128, 128, 0, st>>>(A, lda, n, ipiv, K, K + jbo, K, K + jbo);
+    const int rest = n - K - jbo;
+    if (rest > 0) {
+      const dim3 eg((jbo + 127) / 128, jbo);
+      k_set_eye<<<eg, 128, 0, st>>>(jbo, Minv);
+      e = trsm_cols<float>(st, false, reinterpret_cast<const float2*>(A + K + (long)K * lda), lda, jbo, Minv, jbo, jbo);
+      if (e != cudaSuccess) return e;
+      k_eye_minus<<<eg, 128, 0, st>>>(jbo, Minv);
+      float2* A12 = reinterpret_cast<float2*>(A + K + (long)(K + jbo) * lda);
+      e = cgemm_tc(st, tc_passes, jbo, rest, jbo, Minv, jbo, A12, lda, A12, lda, work, tcb, info);
+      if (e != cudaSuccess) return e;
+      e = cgemm_tc(st, tc_passes, rest, rest, jbo, reinterpret_cast<const float2*>(A + (K + jbo) + (long)K * lda), lda,
+                   A12, lda, reinterpret_cast<float2*>(A + (K + jbo) + (long)(K + jbo) * lda), lda, work, tcb, info);
       if (e != cudaSuccess) return e;
     }
   }
@@ -419,8 +500,8 @@ cudaError_t getrs(cudaStream_t st, int n, int nrhs, const typename cx<R>::T* LU,
   return cudaGetLastError();
 }
 
-template cudaError_t getrf<double>(cudaStream_t, int, double2*, long, int*, int*, void*);
-template cudaError_t getrf<float>(cudaStream_t, int, float2*, long, int*, int*, void*);
+template cudaError_t getrf<double>(cudaStream_t, int, double2*, long, int*, int*, void*, size_t, int);
+template cudaError_t getrf<float>(cudaStream_t, int, float2*, long, int*, int*, void*, size_t, int);
 template cudaError_t getrs<double>(cudaStream_t, int, int, const double2*, long, const int*, double2*, long);
 template cudaError_t getrs<float>(cudaStream_t, int, int, const float2*, long, const int*, float2*, long);
 

@@ -43,17 +43,32 @@ cudaError_t cgemm_skinny(cudaStream_t st, int m, int n, int k, float2 alpha, con
 
 // In-place LU with partial pivoting of the n x n matrix A (lda).  ipiv is a
 // device array of n 1-based pivot rows, LAPACK style.  info (device int) is
-// set to the first zero pivot (1-based) or left at 0.  work is a device
-// scratch of at least lu_work_bytes(n) bytes.
+// set to the first zero pivot (1-based) or left at 0 (a negative value: a
+// bounded device wait ran out).  Complex64 only: tc_passes = 3 or 1 runs the
+// trailing updates of 256-wide outer panels on the tensor cores (cgemm_tc,
+// 3xTF32 or TF32) with work a 256-byte aligned device scratch of at least
+// lu_work_bytes(n, tc_passes) bytes; tc_passes = 0 keeps every update on the
+// SIMT kernels (work unused).
 template <typename R>
-cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* ipiv, int* info, void* work);
+cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* ipiv, int* info, void* work,
+                  size_t work_bytes = 0, int tc_passes = 0);
 
 // Solve A X = B with the factors of getrf; B is n x nrhs (ldb), overwritten.
 template <typename R>
 cudaError_t getrs(cudaStream_t st, int n, int nrhs, const typename cx<R>::T* LU, long lda, const int* ipiv,
                   typename cx<R>::T* B, long ldb);
 
-size_t lu_work_bytes(int n);
+size_t lu_work_bytes(int n, int tc_passes);
+
+// Complex64 C -= A B on the tcgen05 tensor cores (hg_tc.cu): A m x k (lda),
+// B k x n (ldb), C m x n (ldc), column-major.  passes 3: split-TF32 products
+// (single-precision quality); passes 1: plain TF32.  ws: 256-byte aligned
+// device scratch of cgemm_tc_work_bytes(m, n, k) bytes for the packed
+// operands.  status (device int) receives -1000 if a bounded wait ran out.
+bool cgemm_tc_supported();
+size_t cgemm_tc_work_bytes(int m, int n, int k);
+cudaError_t cgemm_tc(cudaStream_t st, int passes, int m, int n, int k, const float2* A, long lda, const float2* B,
+                     long ldb, float2* C, long ldc, void* ws, size_t ws_bytes, int* status);
 
 // Panel LU on a 16-CTA cluster (hg_lu_cluster.cu): rows [0, m) x columns
 // [0, jb <= 32) of P, pivots written 1-based as k0 + row + 1.

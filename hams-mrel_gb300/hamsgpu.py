@@ -23,14 +23,14 @@ EXPORTS = [
     "hg_fill_factor", "hg_solve_radiation", "hg_solve_all_headings", "hg_solve_diffraction", "hg_forces",
     "hg_solve_frequency", "hg_keep_matrices", "hg_get_matrix", "hg_green_points", "hg_refine_info",
     "hg_stage_times", "hg_dispersion", "hg_wave_properties", "hg_panel_geometry", "hg_mark", "hg_elapsed",
-    "hg_bench_gemm", "hg_green_points_noalloc", "hg_gesv",
+    "hg_bench_gemm", "hg_green_points_noalloc", "hg_gesv", "hg_gemm_check",
 ]
 
 
 class HgOpts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("precision", ctypes.c_int), ("grn_kind", ctypes.c_int),
                 ("max_refine", ctypes.c_int), ("refine_tol", ctypes.c_double), ("rho", ctypes.c_double),
-                ("g", ctypes.c_double)]
+                ("g", ctypes.c_double), ("lu_tensor", ctypes.c_int)]
 
 
 _LIB = None
@@ -82,6 +82,9 @@ def load(build_if_missing: bool = True):
     L.hg_green_points_noalloc.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p]
     L.hg_gesv.argtypes = [c_void_p, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_void_p, c_int, P(c_int),
                           P(c_int)]
+    L.hg_bench_gemm.argtypes = [c_void_p, c_int, c_int, c_int, c_int, c_int, P(ctypes.c_float)]
+    L.hg_gemm_check.argtypes = [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_void_p,
+                                c_int]
     L.hg_mark.argtypes = [c_void_p, c_int]
     L.hg_elapsed.argtypes = [c_void_p, c_int, c_int, P(ctypes.c_float)]
     L.hg_dispersion.argtypes = [c_double, c_double, c_int, c_void_p]
@@ -138,12 +141,14 @@ class Solver:
     """One library context (device buffers, stream, factorisation)."""
 
     def __init__(self, precision: int = HG_PREC_FP64, device: int = 0, grn_kind: int = 8,
-                 max_refine: int = 10, refine_tol: float = 1e-10, rho: float = 1000.0, g: float = 9.80665):
+                 max_refine: int = 10, refine_tol: float = 1e-10, rho: float = 1000.0, g: float = 9.80665,
+                 lu_tensor: int = 3):
         self.L = load()
         opts = HgOpts()
         self.L.hg_default_opts(ctypes.byref(opts))
         opts.device, opts.precision, opts.grn_kind = device, precision, grn_kind
         opts.max_refine, opts.refine_tol, opts.rho, opts.g = max_refine, refine_tol, rho, g
+        opts.lu_tensor = lu_tensor
         h = ctypes.c_void_p()
         rc = self.L.hg_create(ctypes.byref(h), ctypes.byref(opts))
         if rc != 0:
@@ -269,6 +274,21 @@ class Solver:
         self._check(self.L.hg_gesv(self.h, precision, n, bb.shape[1], _ptr(lu), n, _ptr(ipiv), _ptr(bb), n,
                                    ctypes.byref(it), ctypes.byref(info)))
         return lu, ipiv, bb, it.value, info.value
+
+    def gemm_check(self, variant, a, b, c):
+        """C - A B through GEMM kernel `variant` (hg_gemm_check); complex128 in and out."""
+        a = np.asfortranarray(a, dtype=np.complex128)
+        b = np.asfortranarray(b, dtype=np.complex128)
+        out = np.array(c, dtype=np.complex128, order="F", copy=True)
+        m, k = a.shape
+        n = b.shape[1]
+        self._check(self.L.hg_gemm_check(self.h, variant, m, n, k, _ptr(a), m, _ptr(b), k, _ptr(out), m))
+        return out
+
+    def bench_gemm(self, variant, m, n, k, iters=3):
+        ms = ctypes.c_float()
+        self._check(self.L.hg_bench_gemm(self.h, variant, m, n, k, iters, ctypes.byref(ms)))
+        return ms.value
 
     def refine_info(self):
         s = ctypes.c_int(); r = ctypes.c_double()

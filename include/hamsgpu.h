@@ -45,9 +45,13 @@ typedef struct {
     double refine_tol;   /* mixed form: stop when max_k ||A x_k - b_k|| / ||b_k|| <= tol (default 1e-10) */
     double rho;          /* fluid density for the forces (reference Const_mod: 1000) */
     double g;            /* gravity for VINP (reference Const_mod: 9.80665) */
+    int lu_tensor;       /* mixed form, order >= 1024: trailing updates of the complex64 LU on the
+                            tensor cores, 3 = split TF32 (three products, single-precision
+                            quality; default), 1 = TF32 (one product, more refinement sweeps),
+                            0 = FP32 SIMT kernels only */
 } hg_opts;
 
-/* Fill opts with the defaults above (device 0, FP64, GRN_KIND 8, rho 1000, g 9.80665). */
+/* Fill opts with the defaults above (device 0, FP64, GRN_KIND 8, rho 1000, g 9.80665, lu_tensor 3). */
 void hg_default_opts(hg_opts *opts);
 
 /* Create / destroy a context.  opts may be NULL for the defaults. */
@@ -193,10 +197,19 @@ int hg_mark(hg_ctx *ctx, int slot);
 int hg_elapsed(hg_ctx *ctx, int slot0, int slot1, float *ms);
 
 /* Average device time (ms) of the library's complex GEMM kernel
- * C = C - A B on an m x n x k problem (precision: 0 complex128, 1 complex64),
- * over iters launches on scratch buffers; used to report the roofline of the
- * LU trailing update. */
+ * C = C - A B on an m x n x k problem, over iters launches on scratch
+ * buffers; used to report the roofline of the LU trailing update.
+ * precision (kernel variant): 0 complex128 SIMT, 1 complex64 SIMT,
+ * 2 complex64 tensor cores split TF32 (3 products), 3 complex64 tensor
+ * cores TF32 (1 product); 2 and 3 include their operand packing. */
 int hg_bench_gemm(hg_ctx *ctx, int precision, int m, int n, int k, int iters, float *ms_per_launch);
+
+/* C = C - A B through one of those kernel variants on host arrays (all
+ * COMPLEX*16, column-major; variants 1-3 round A, B, C to complex64 on the
+ * device and widen the result back).  A test hook for the LU update
+ * kernels; the reference's counterpart is the ZGEMM step inside ZGETRF. */
+int hg_gemm_check(hg_ctx *ctx, int variant, int m, int n, int k, const double *a, int lda, const double *b,
+                  int ldb, double *c, int ldc);
 
 /* Time (milliseconds, CUDA events on the context stream) of the stages of the
  * last hg_solve_frequency: [0] fill, [1] LU, [2] solves and refinement, [3] forces. */
