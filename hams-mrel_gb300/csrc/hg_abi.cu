@@ -7,8 +7,12 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/hamsgpu.h"
@@ -80,6 +84,13 @@ struct hg_ctx {
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t user_ev[16] = {};
   float stage_ms[4] = {0, 0, 0, 0};
+  // host copy of the mesh (for the solve slots of hg_solve_sweep)
+  std::vector<double> h_nodes, h_xyz, h_ds, h_pnsz, h_dxyz, h_lid;
+  std::vector<int> h_ncon, h_ncn, h_ranges;
+  // solve slots: child contexts with their own stream and buffers
+  std::vector<hg_ctx*> slots;
+  bool slots_mesh = false;  // slots hold the current mesh
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
 };
 
 namespace {
@@ -328,10 +339,14 @@ void hg_destroy(hg_ctx* c) {
   DevBuf<float2>* cbs[] = {&c->Af, &c->Sf, &c->Cf, &c->Bf, &c->Aof};
   for (auto* b : cbs) b->release();
   c->rws.release();
+  for (hg_ctx* sl : c->slots) hg_destroy(sl);
+  c->slots.clear();
   for (int k = 0; k < 5; ++k)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   for (int k = 0; k < 16; ++k)
     if (c->user_ev[k]) cudaEventDestroy(c->user_ev[k]);
+  if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+  if (c->join_ev) cudaEventDestroy(c->join_ev);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -410,6 +425,17 @@ int hg_set_mesh(hg_ctx* c, int n, int ntnd, const double* nodes, const int* ncon
   CK(cudaStreamSynchronize(c->st));
   int r = check_status(c);
   if (r) return r;
+  c->h_nodes.assign(nodes, nodes + (size_t)ntnd * 3);
+  c->h_ncon.assign(ncon, ncon + (size_t)n * 4);
+  c->h_ncn.assign(ncn, ncn + n);
+  c->h_xyz.assign(xyz_p, xyz_p + (size_t)n * 3);
+  c->h_ds.assign(ds, ds + n);
+  c->h_pnsz.assign(pnsz, pnsz + n);
+  c->h_dxyz.assign(dxyz_p, dxyz_p + (size_t)n * 6);
+  if (nl > 0) c->h_lid.assign(lid_xyz_p, lid_xyz_p + (size_t)nl * 3);
+  else c->h_lid.clear();
+  c->h_ranges.assign(body_ranges, body_ranges + 2 * nbody);
+  c->slots_mesh = false;
   c->mesh_set = true;
   c->factored = false;
   c->rad_done = c->dif_done = false;
@@ -628,6 +654,94 @@ int hg_solve_frequency(hg_ctx* c, double v, double wk, double w1, double h, cons
   CK(cudaEventElapsedTime(&c->stage_ms[2], c->ev[2], c->ev[3]));
   CK(cudaEventElapsedTime(&c->stage_ms[3], c->ev[3], c->ev[4]));
   return check_status(c);
+}
+
+int hg_solve_sweep(hg_ctx* c, int nfreq, const double* v, const double* wk, const double* w1, double h,
+                   const double* wvn, int nk, int irsp, const double* betas, int nbeta, int isol, int nslots,
+                   double* amas, double* bdmp, double* exfc, double* mxpot, int ldm, float* latency_ms) {
+  if (!c) return -1;
+  if (nfreq < 0) return fail(c, -2, "nfreq must be >= 0");
+  if (nfreq > 0 && (!v || !wk || !w1)) return fail(c, -3, "v, wk, w1 must not be NULL");
+  if (h > 0.0 && (!wvn || nk < 20)) return fail(c, -7, "finite depth needs nk >= 20 dispersion roots per frequency");
+  if (nbeta < 0 || (nbeta > 0 && !betas)) return fail(c, -11, "bad betas / nbeta");
+  if (nslots < 1 || nslots > 16) return fail(c, -13, "nslots must be in 1..16");
+  if (!amas || !bdmp || (nbeta > 0 && !exfc)) return fail(c, -14, "output arrays must not be NULL");
+  if (mxpot && ldm < c->n) return fail(c, -18, "ldm %d < n %d", ldm, c->n);
+  if (!c->mesh_set) return fail(c, HG_ERR_STATE, "hg_set_mesh must come first");
+  if (nfreq == 0) return 0;
+  if (!c->slots_mesh) {
+    for (hg_ctx* sl : c->slots) hg_destroy(sl);
+    c->slots.clear();
+  }
+  while ((int)c->slots.size() < nslots) {
+    hg_ctx* sl = nullptr;
+    int r = hg_create(&sl, &c->o);
+    if (r) return fail(c, r, "creating solve slot %d failed", (int)c->slots.size());
+    r = hg_set_mesh(sl, c->n, c->ntnd, c->h_nodes.data(), c->h_ncon.data(), c->h_ncn.data(), c->h_xyz.data(),
+                    c->h_ds.data(), c->h_pnsz.data(), c->h_dxyz.data(), c->nl, c->nl ? c->h_lid.data() : nullptr,
+                    c->nbody, c->h_ranges.data());
+    if (r) {
+      std::string msg = sl->err;
+      hg_destroy(sl);
+      return fail(c, r, "mesh of solve slot %d: %s", (int)c->slots.size(), msg.c_str());
+    }
+    c->slots.push_back(sl);
+  }
+  c->slots_mesh = true;
+  const int nd = 6 * c->nbody;
+  const size_t mx_cols = (size_t)nd + nbeta;
+  // Fork/join on the device: the slots' streams wait for the work queued on
+  // this context's stream so far, and this stream waits for every slot at the
+  // end, so events recorded on it (hg_mark) bracket the whole sweep.
+  if (!c->fork_ev) CK(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));
+  CK(cudaEventRecord(c->fork_ev, c->st));
+  for (int k = 0; k < nslots; ++k) CK(cudaStreamWaitEvent(c->slots[k]->st, c->fork_ev, 0));
+  std::atomic<int> next(0);
+  std::vector<int> slot_rc(nslots, 0), slot_freq(nslots, -1);
+  auto worker = [&](int k) {
+    hg_ctx* sl = c->slots[k];
+    cudaSetDevice(sl->o.device);
+    for (;;) {
+      const int i = next.fetch_add(1);
+      if (i >= nfreq) break;
+      const auto t0 = std::chrono::steady_clock::now();
+      const int r = hg_solve_frequency(sl, v[i], wk[i], w1[i], h, h > 0.0 ? wvn + (size_t)i * nk : nullptr,
+                                       h > 0.0 ? nk : 0, irsp, betas, nbeta, isol, amas + (size_t)i * nd * nd,
+                                       bdmp + (size_t)i * nd * nd, nbeta > 0 ? exfc + (size_t)i * nbeta * nd * 2 : nullptr,
+                                       mxpot ? mxpot + (size_t)i * ldm * mx_cols * 2 : nullptr, ldm);
+      const auto t1 = std::chrono::steady_clock::now();
+      if (latency_ms) latency_ms[i] = std::chrono::duration<float, std::milli>(t1 - t0).count();
+      if (r) {
+        slot_rc[k] = r;
+        slot_freq[k] = i;
+        next.store(nfreq);  // stop handing out work
+        break;
+      }
+    }
+  };
+  if (nslots == 1) {
+    worker(0);
+  } else {
+    std::vector<std::thread> th;
+    for (int k = 0; k < nslots; ++k) th.emplace_back(worker, k);
+    for (auto& t : th) t.join();
+  }
+  for (int k = 0; k < nslots; ++k) {
+    hg_ctx* sl = c->slots[k];
+    if (!sl->join_ev) CK(cudaEventCreateWithFlags(&sl->join_ev, cudaEventDisableTiming));
+    CK(cudaEventRecord(sl->join_ev, sl->st));
+    CK(cudaStreamWaitEvent(c->st, sl->join_ev, 0));
+  }
+  int sw = 0;
+  double res = 0.0;
+  for (int k = 0; k < nslots; ++k) {
+    if (slot_rc[k]) return fail(c, slot_rc[k], "frequency %d (slot %d): %s", slot_freq[k], k, c->slots[k]->err.c_str());
+    sw = std::max(sw, c->slots[k]->sweeps);
+    res = std::fmax(res, c->slots[k]->resid);
+  }
+  c->sweeps = sw;
+  c->resid = res;
+  return 0;
 }
 
 int hg_get_matrix(hg_ctx* c, int which, double* out, int ld) {

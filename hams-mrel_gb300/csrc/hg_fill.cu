@@ -8,6 +8,7 @@
 // Layout: field rows 0..n-1 are hull panels, n..tn-1 lid panels (IRSP=1);
 // source columns are hull panels.  A and S are column-major tn x n with
 // lda = tn, one complex entry per (field, source) pair.
+#include <mutex>
 #include "hg_common.cuh"
 #include "hg_green.cuh"
 #include "hg_kernels.cuh"
@@ -162,6 +163,8 @@ static void monomial_to_chebyshev(const double* c, double* t) {
 
 static cudaError_t upload_cheb_constants() {
   static bool done[64] = {false};
+  static std::mutex mu;  // host threads of several contexts may get here at once
+  std::lock_guard<std::mutex> lock(mu);
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;

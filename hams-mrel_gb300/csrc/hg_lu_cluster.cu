@@ -9,6 +9,7 @@
 // its row, one cluster barrier, every CTA reads the 16 candidates and rows
 // out of the other CTAs' shared memory, takes the same pivot, and scales and
 // rank-1 updates its own rows.
+#include <mutex>
 #include <climits>
 #include <cooperative_groups.h>
 
@@ -371,6 +372,8 @@ cudaError_t panel_cluster_smem(cudaStream_t st, typename cx<R>::T* P, long lda, 
   const int rpc = (m + kClusterCTAs - 1) / kClusterCTAs;
   const size_t smem = (size_t)rpc * jb * sizeof(T);
   static int attr_done[2] = {0, 0};
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
   const int idx = sizeof(R) == 8 ? 1 : 0;
   if (smem > (size_t)kPanelSmemMax) return cudaErrorNotSupported;
   auto kern = k_getf2_cluster<R>;
@@ -436,6 +439,8 @@ template <typename R>
 bool panel_cluster_supported(int m) {
   typedef typename cx<R>::T T;
   static int cached[2] = {-1, -1};
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
   const int idx = sizeof(R) == 8 ? 1 : 0;
   const int rpc = (m + kClusterCTAs - 1) / kClusterCTAs;
   if ((size_t)rpc * kClusterNB * sizeof(T) > (size_t)kPanelSmemMax) return false;

@@ -35,6 +35,7 @@
 // under the main loop of the next.  Every wait is bounded in time: a wait
 // that runs out raises an abort flag that ends every role, and the kernel
 // records the timeout in the caller's status word.
+#include <mutex>
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -345,6 +346,8 @@ __global__ void k_pack_b(int k, int n, int kr, const float2* __restrict__ B, lon
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   static bool tried = false;
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
   if (!tried) {
     tried = true;
     void* p = nullptr;
@@ -408,6 +411,8 @@ cudaError_t launch_tc(cudaStream_t st, int m, int n, int k, const float2* A, lon
 
 bool cgemm_tc_supported() {
   static int cached = -1;
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
   if (cached < 0) {
     int dev = 0, major = 0, minor = 0;
     cached = 0;

@@ -24,6 +24,7 @@ EXPORTS = [
     "hg_solve_frequency", "hg_keep_matrices", "hg_get_matrix", "hg_green_points", "hg_refine_info",
     "hg_stage_times", "hg_dispersion", "hg_wave_properties", "hg_panel_geometry", "hg_mark", "hg_elapsed",
     "hg_bench_gemm", "hg_green_points_noalloc", "hg_gesv", "hg_gemm_check",
+    "hg_solve_sweep",
 ]
 
 
@@ -82,6 +83,9 @@ def load(build_if_missing: bool = True):
     L.hg_green_points_noalloc.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p]
     L.hg_gesv.argtypes = [c_void_p, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_void_p, c_int, P(c_int),
                           P(c_int)]
+    L.hg_solve_sweep.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_int, c_int,
+                                 c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
+                                 c_void_p]
     L.hg_bench_gemm.argtypes = [c_void_p, c_int, c_int, c_int, c_int, c_int, P(ctypes.c_float)]
     L.hg_gemm_check.argtypes = [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_void_p,
                                 c_int]
@@ -243,6 +247,39 @@ class Solver:
                                               _ptr(b), nb, isol, _ptr(out["amas"]), _ptr(out["bdmp"]),
                                               _ptr(out["exfc"]), _ptr(mx), self.n))
         return out["amas"], out["bdmp"], out["exfc"][:nb], mx
+
+    def solve_sweep(self, v, wk, w1, h, wvn, betas, irsp=0, isol=1, nslots=1, out=None, want_potentials=False):
+        """Frequency sweep over arrays v, wk, w1 (and wvn rows for finite depth)
+        on nslots concurrent solve slots (hg_solve_sweep).
+
+        Returns (amas[nfreq, nd, nd], bdmp, exfc[nfreq, nbeta, nd], latency_ms[nfreq],
+        mxpot[nfreq, n, nd + nbeta] or None)."""
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        wk = np.ascontiguousarray(wk, dtype=np.float64)
+        w1 = np.ascontiguousarray(w1, dtype=np.float64)
+        nf = len(v)
+        nd = 6 * self.nbody
+        b = np.ascontiguousarray(betas, dtype=np.float64)
+        nb = len(b)
+        w = None
+        nk = 0
+        if h > 0 and wvn is not None:
+            w = np.ascontiguousarray(wvn, dtype=np.float64).reshape(nf, -1)
+            nk = w.shape[1]
+        if out is None:
+            out = {"amas": np.zeros((nf, nd, nd)), "bdmp": np.zeros((nf, nd, nd)),
+                   "exfc": np.zeros((nf, nd, max(nb, 1)), dtype=np.complex128),
+                   "lat": np.zeros(nf, dtype=np.float32),
+                   "mxpot": np.zeros((nf, nd + nb, self.n), dtype=np.complex128) if want_potentials else None}
+        mx = out.get("mxpot")
+        self._check(self.L.hg_solve_sweep(self.h, nf, _ptr(v), _ptr(wk), _ptr(w1), float(h), _ptr(w), nk, irsp,
+                                          _ptr(b), nb, isol, nslots, _ptr(out["amas"]), _ptr(out["bdmp"]),
+                                          _ptr(out["exfc"]), _ptr(mx), self.n, _ptr(out["lat"])))
+        # per frequency the arrays are column-major (Fortran): transpose the last two axes
+        amas = out["amas"].transpose(0, 2, 1)
+        bdmp = out["bdmp"].transpose(0, 2, 1)
+        exfc = out["exfc"].transpose(0, 2, 1)[:, :nb, :]
+        return amas, bdmp, exfc, out["lat"], None if mx is None else mx.transpose(0, 2, 1)
 
     def green_points(self, pts, flags):
         p = np.ascontiguousarray(pts, dtype=np.float64)

@@ -129,6 +129,33 @@ int hg_solve_frequency(hg_ctx *ctx, double v, double wk, double w1, double h, co
                        int irsp, const double *betas, int nbeta, int isol, double *amas, double *bdmp,
                        double *exfc, double *mxpot, int ldm);
 
+/*
+ * A frequency sweep: the frequency loop of HAMS_Prog (src/HAMS_Prog.f90:255-304
+ * single body, :613-704 multi-body) over nfreq frequencies of one mesh, depth,
+ * heading set and irsp, each frequency the work of hg_solve_frequency.
+ * Frequencies are independent, so nslots solve slots (child contexts holding
+ * their own copy of the mesh, device buffers and CUDA stream, created on the
+ * first call and kept) take them in turn from one queue and run concurrently
+ * on the device: one slot's latency-bound LU panels share the GPU with
+ * another's Green fill and tensor-core updates.  nslots = 1 runs them in order.
+ *   v, wk, w1[nfreq]    wave state per frequency (as hg_set_frequency)
+ *   wvn[nk * nfreq]     dispersion roots per frequency (finite depth only)
+ *   amas, bdmp          (6nb x 6nb) x nfreq, column-major per frequency
+ *   exfc                (nbeta x 6nb COMPLEX*16) x nfreq
+ *   mxpot               optional (NULL: none): potentials, (ldm x (6nb + nbeta)
+ *                       COMPLEX*16) x nfreq, radiation modes then headings
+ *   latency_ms[nfreq]   optional: host wall time of each frequency-solve
+ * Each slot holds about 5 n^2 x 8 bytes of device memory in the mixed form
+ * (16 bytes per entry in the FP64 form).  On an error in any frequency the
+ * other slots stop taking new frequencies and the call returns that error
+ * (frequency and slot in hg_last_error).  The device work of the sweep is
+ * ordered after earlier work on ctx's stream, and later work on ctx's stream
+ * (e.g. hg_mark) after the sweep.
+ */
+int hg_solve_sweep(hg_ctx *ctx, int nfreq, const double *v, const double *wk, const double *w1, double h,
+                   const double *wvn, int nk, int irsp, const double *betas, int nbeta, int isol, int nslots,
+                   double *amas, double *bdmp, double *exfc, double *mxpot, int ldm, float *latency_ms);
+
 /* Diagnostics for tests: copy the tn x n influence matrix (which = 0, before
  * factorisation) or single-layer matrix (which = 1) of the last fill to host
  * memory (COMPLEX*16, leading dimension ld >= tn).  Requires hg_fill_factor
