@@ -57,6 +57,7 @@ struct hg_ctx {
   std::string err;
   // mesh
   int n = 0, nl = 0, tn = 0, tnf = 0, ntnd = 0, nbody = 0;  // tn: rows of the current solve, tnf: n + nl
+  double ox = 0, oy = 0;  // horizontal centre of the hull centroids (origin of the FP32 pair coordinates)
   bool mesh_set = false;
   std::vector<int> bstart, bend;
   DevBuf<double> nodes, xyz_p, ds, pnsz, dxyz, rec, fx, betas;
@@ -72,6 +73,7 @@ struct hg_ctx {
   DevBuf<unsigned char> rws;             // workspace of the double-float residual
   DevBuf<unsigned char> luws;            // packed operands of the tensor-core LU updates
   DevBuf<double> amas, bdmp;
+  DevBuf<double> nrm;                    // column norms of the refinement (2 x columns)
   int irsp = 0;
   bool factored = false;
   bool keep = false;
@@ -218,14 +220,19 @@ int solve_cols(hg_ctx* c, int c0, int c1) {
   else CK(cudaMemcpy2DAsync(Rh, (size_t)n * sizeof(double2), Bc, (size_t)tn * sizeof(double2), (size_t)n * sizeof(double2),
                             nc, cudaMemcpyDeviceToDevice, c->st));
   // norms of the square-system right-hand side
-  DevBuf<double> nb;
+  DevBuf<double>& nb = c->nrm;
   CK(nb.ensure(2 * (size_t)nc));
   k_colmax<<<nc, 256, 0, c->st>>>(n, Rh, n, nb.p);
   std::vector<double> bnorm(nc), rnorm(nc);
   CK(cudaMemcpyAsync(bnorm.data(), nb.p, nc * sizeof(double), cudaMemcpyDeviceToHost, c->st));
   // x0 = M^{-1} b in complex64
+  const bool inv = hg::lu_has_inverses(n, c->o.lu_tensor, c->luws.cap);
+  auto lu_solve = [&](float2* rhs) -> cudaError_t {
+    if (inv) return hg::getrs_inv(c->st, n, nc, LU, ldlu, c->ipiv.p, rhs, n, c->luws.p);
+    return hg::getrs<float>(c->st, n, nc, LU, ldlu, c->ipiv.p, rhs, n);
+  };
   CK(hg::convert_z2c_2d(c->st, n, nc, Rh, n, Bf, n));
-  CK(hg::getrs<float>(c->st, n, nc, LU, ldlu, c->ipiv.p, Bf, n));
+  CK(lu_solve(Bf));
   CK(cudaMemsetAsync(Xc, 0, (size_t)n * nc * sizeof(double2), c->st));
   CK(hg::add_c2z_2d(c->st, n, nc, Bf, n, Xc, n));
   int sweep = 0;
@@ -247,11 +254,10 @@ int solve_cols(hg_ctx* c, int c0, int c1) {
     if (worst <= c->o.refine_tol || sweep >= c->o.max_refine) break;
     // x += M^{-1} r (complex64 correction)
     CK(hg::convert_z2c_2d(c->st, n, nc, Rh, n, Bf, n));
-    CK(hg::getrs<float>(c->st, n, nc, LU, ldlu, c->ipiv.p, Bf, n));
+    CK(lu_solve(Bf));
     CK(hg::add_c2z_2d(c->st, n, nc, Bf, n, Xc, n));
     ++sweep;
   }
-  nb.release();
   c->sweeps = sweep;
   c->resid = worst;
   return 0;
@@ -332,6 +338,7 @@ void hg_destroy(hg_ctx* c) {
   DevBuf<double>* dbs[] = {&c->nodes, &c->xyz_p, &c->ds, &c->pnsz, &c->dxyz, &c->rec, &c->fx, &c->betas,
                            &c->wvn, &c->amas, &c->bdmp};
   for (auto* b : dbs) b->release();
+  c->nrm.release();
   DevBuf<int>* ibs[] = {&c->ncon, &c->ncn, &c->body_of, &c->body_start, &c->body_end, &c->ipiv, &c->status, &c->info};
   for (auto* b : ibs) b->release();
   DevBuf<double2>* zbs[] = {&c->A, &c->S, &c->C, &c->A64, &c->B, &c->X, &c->R, &c->R2, &c->W, &c->Wz, &c->part, &c->exfc, &c->gws};
@@ -435,6 +442,12 @@ int hg_set_mesh(hg_ctx* c, int n, int ntnd, const double* nodes, const int* ncon
   if (nl > 0) c->h_lid.assign(lid_xyz_p, lid_xyz_p + (size_t)nl * 3);
   else c->h_lid.clear();
   c->h_ranges.assign(body_ranges, body_ranges + 2 * nbody);
+  {
+    double sx = 0, sy = 0;
+    for (int e = 0; e < n; ++e) { sx += xyz_p[e]; sy += xyz_p[e + (size_t)n]; }
+    c->ox = sx / n;
+    c->oy = sy / n;
+  }
   c->slots_mesh = false;
   c->mesh_set = true;
   c->factored = false;
@@ -505,7 +518,8 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
     CK(c->Sf.ensure((size_t)tn * n));
     const bool special = std::fabs(c->v) < (double)1.e-8f || std::fabs(c->v + 1.0) < (double)1.e-8f;
     if (deep && !special && c->o.grn_kind == 8)
-      CK(hg::launch_green_fill_mixed(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, c->v, c->Af.p, c->Sf.p, tn, c->status.p));
+      CK(hg::launch_green_fill_mixed(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, c->v, c->ox, c->oy, c->Af.p, c->Sf.p, tn,
+                                     c->status.p));
     else
       CK(hg::launch_green_fill<float2>(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, deep, c->o.grn_kind, c->Af.p,
                                        c->Sf.p, tn, c->status.p));
@@ -811,6 +825,7 @@ int hg_gesv(hg_ctx* c, int precision, int n, int nrhs, double* a, int lda, int* 
   const size_t nn = (size_t)n * n, nb = (size_t)n * (nrhs > 0 ? nrhs : 1);
   DevBuf<double2> dA, dB, dX, dR, ws;
   DevBuf<float2> dAf, dBf;
+  DevBuf<unsigned char> luws;
   DevBuf<int> dpiv, dinfo;
   DevBuf<double> norms;
   const double2 one = make_double2(1, 0), mone = make_double2(-1, 0);
@@ -834,10 +849,14 @@ int hg_gesv(hg_ctx* c, int precision, int n, int nrhs, double* a, int lda, int* 
     CK(ws.ensure((size_t)16 * nb));
     CK(norms.ensure(2 * (size_t)(nrhs > 0 ? nrhs : 1)));
     CK(hg::convert_z2c(c->st, (long)nn, dA.p, dAf.p));
-    DevBuf<unsigned char> luws;
     const size_t lwb = hg::lu_work_bytes(n, c->o.lu_tensor);
     if (lwb) CK(luws.ensure(lwb));
     CK(hg::getrf<float>(c->st, n, dAf.p, n, dpiv.p, dinfo.p, luws.p, lwb, c->o.lu_tensor));
+    const bool inv = hg::lu_has_inverses(n, c->o.lu_tensor, luws.cap);
+    auto lu_solve = [&](float2* rhs) -> cudaError_t {
+      if (inv) return hg::getrs_inv(c->st, n, nrhs, dAf.p, n, dpiv.p, rhs, n, luws.p);
+      return hg::getrs<float>(c->st, n, nrhs, dAf.p, n, dpiv.p, rhs, n);
+    };
     CK(cudaMemcpyAsync(&inf, dinfo.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
     if (inf < 0) return fail(c, HG_ERR_DEVICE, "LU panel: a bounded cluster wait ran out (info %d)", inf);
@@ -850,7 +869,7 @@ int hg_gesv(hg_ctx* c, int precision, int n, int nrhs, double* a, int lda, int* 
       k_colmax<<<nrhs, 256, 0, c->st>>>(n, dB.p, n, norms.p);
       CK(cudaMemcpyAsync(bn.data(), norms.p, nrhs * sizeof(double), cudaMemcpyDeviceToHost, c->st));
       CK(hg::convert_z2c(c->st, (long)nb, dB.p, dBf.p));
-      CK(hg::getrs<float>(c->st, n, nrhs, dAf.p, n, dpiv.p, dBf.p, n));
+      CK(lu_solve(dBf.p));
       CK(hg::convert_c2z(c->st, (long)nb, dBf.p, dX.p));
       bool ok = false;
       for (int sweep = 0;; ++sweep) {
@@ -865,7 +884,7 @@ int hg_gesv(hg_ctx* c, int precision, int n, int nrhs, double* a, int lda, int* 
         if (worst <= c->o.refine_tol) { ok = true; it = sweep; break; }
         if (sweep >= c->o.max_refine) break;
         CK(hg::convert_z2c(c->st, (long)nb, dR.p, dBf.p));
-        CK(hg::getrs<float>(c->st, n, nrhs, dAf.p, n, dpiv.p, dBf.p, n));
+        CK(lu_solve(dBf.p));
         CK(hg::add_c2z_2d(c->st, n, nrhs, dBf.p, n, dX.p, n));
       }
       if (ok) {

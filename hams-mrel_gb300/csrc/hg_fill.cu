@@ -180,15 +180,23 @@ static cudaError_t upload_cheb_constants() {
   return e;
 }
 
-constexpr int kPanelFloats = 24;  // ui, uj, uk, ksi, eta, l (3+3+3+4+4+4) + nv, ds, n0..n2
-
+// Single-precision pair loop of the mixed form.  Per pair only FP32
+// arithmetic, except (a) the pairs within 4 panel sizes (0.08 of the
+// 50-panel-size FLAG radius), whose Newman integrals stay in FP64 with FP64
+// coordinates, and (b) the rare pairs whose FP32 squared distance lies within
+// 1e-3 of the FLAG radius, where FLAG is decided again in FP64 exactly as
+// CALGREEN does (dist <= 50 PNSZ).  Horizontal coordinates enter FP32
+// relative to the mesh centre (ox, oy) so that their rounding is that of the
+// array's size, not of its position; depths stay absolute (the image
+// distance zp + zq needs them).
 __global__ void __launch_bounds__(FILL_ROWS)
 k_green_fill_mixed(const double* __restrict__ rec, const double* __restrict__ fx, int ldf, int n, int tn, float vf,
-                   float2* __restrict__ A, float2* __restrict__ S, long lda, int* status) {
+                   double ox, double oy, float2* __restrict__ A, float2* __restrict__ S, long lda, int* status) {
   __shared__ alignas(128) double tile[FILL_COLS * PR_SIZE];
   __shared__ alignas(8) uint64_t bar;
   __shared__ PanelF pfs[FILL_COLS];
   __shared__ float pds[FILL_COLS][4];  // area, normal
+  __shared__ float pxs[FILL_COLS][8];  // xq, yq, zq (relative), FLAG radius squared, Newman origin (relative)
   const int col0 = blockIdx.y * FILL_COLS;
   const int ncol = min(FILL_COLS, n - col0);
   if (threadIdx.x == 0) {
@@ -214,31 +222,48 @@ k_green_fill_mixed(const double* __restrict__ rec, const double* __restrict__ fx
     q.nv = (int)pr[PR_NCN];
     pds[threadIdx.x][0] = (float)pr[PR_DS];
     for (int k = 0; k < 3; ++k) pds[threadIdx.x][1 + k] = (float)pr[PR_N + k];
+    float* px = pxs[threadIdx.x];
+    px[0] = (float)(pr[PR_XQ] - ox);
+    px[1] = (float)(pr[PR_XQ + 1] - oy);
+    px[2] = (float)pr[PR_XQ + 2];
+    px[3] = (float)(pr[PR_FLAGD] * pr[PR_FLAGD]);
+    px[4] = (float)(pr[PR_PO] - ox);
+    px[5] = (float)(pr[PR_PO + 1] - oy);
+    px[6] = (float)pr[PR_PO + 2];
+    px[7] = 0.f;
   }
   __syncthreads();
   const int i = blockIdx.x * FILL_ROWS + threadIdx.x;
   if (i >= tn) return;
   const double xp = fx[i], yp = fx[i + ldf], zp = fx[i + 2 * (size_t)ldf];
+  const float xpf = (float)(xp - ox), ypf = (float)(yp - oy), zpf = (float)zp;
   for (int jj = 0; jj < ncol; ++jj) {
-    const double* pr = tile + jj * PR_SIZE;
+    const float* px = pxs[jj];
     const int j = col0 + jj;
-    const double dx = pr[PR_XQ] - xp, dy = pr[PR_XQ + 1] - yp, zq = pr[PR_XQ + 2];
-    const double dist = sqrt(dx * dx + dy * dy + (zp - zq) * (zp - zq));
-    const double flagd = pr[PR_FLAGD];
-    const int flag = (dist <= flagd) ? 1 : 0;
+    const float dxf = px[0] - xpf, dyf = px[1] - ypf, zqf = px[2];
+    const float dzf = zpf - zqf;
+    const float d2f = dxf * dxf + dyf * dyf + dzf * dzf;
+    const float fl2 = px[3];
+    int flag;
+    if (fabsf(d2f - fl2) > 1e-3f * fl2) {
+      flag = d2f < fl2 ? 1 : 0;
+    } else {
+      const double* pr = tile + jj * PR_SIZE;
+      const double dx = pr[PR_XQ] - xp, dy = pr[PR_XQ + 1] - yp, dz = zp - pr[PR_XQ + 2];
+      flag = (sqrt(dx * dx + dy * dy + dz * dz) <= pr[PR_FLAGD]) ? 1 : 0;
+    }
     float sij = 0.f, d0 = 0.f, d1 = 0.f, d2 = 0.f;
     if (flag) {
-      if (dist <= 0.08 * flagd) {
+      if (d2f <= 0.0064f * fl2) {
         double s64, e0, e1, e2;
-        newman_pair(pr, xp, yp, zp, s64, e0, e1, e2);
+        newman_pair(tile + jj * PR_SIZE, xp, yp, zp, s64, e0, e1, e2);
         sij = (float)s64; d0 = (float)e0; d1 = (float)e1; d2 = (float)e2;
       } else {
-        newman_pair_f(pfs[jj], (float)(xp - pr[PR_PO]), (float)(yp - pr[PR_PO + 1]), (float)(zp - pr[PR_PO + 2]),
-                      sij, d0, d1, d2);
+        newman_pair_f(pfs[jj], xpf - px[4], ypf - px[5], zpf - px[6], sij, d0, d1, d2);
       }
     }
     float2 g[4];
-    inf_green_f((float)dx, (float)dy, (float)(zp + zq), (float)(zp - zq), vf, flag, g);
+    inf_green_f(dxf, dyf, zpf + zqf, dzf, vf, flag, g);
     const float ear = pds[jj][0], n0 = pds[jj][1], n1 = pds[jj][2], n2 = pds[jj][3];
     float ar, ai, sr;
     if (flag) {
@@ -257,11 +282,11 @@ k_green_fill_mixed(const double* __restrict__ rec, const double* __restrict__ fx
 }
 
 cudaError_t launch_green_fill_mixed(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
-                                    double v, float2* A, float2* S, long lda, int* status) {
+                                    double v, double ox, double oy, float2* A, float2* S, long lda, int* status) {
   cudaError_t e = upload_cheb_constants();
   if (e != cudaSuccess) return e;
   dim3 grid((tn + FILL_ROWS - 1) / FILL_ROWS, (n + FILL_COLS - 1) / FILL_COLS);
-  k_green_fill_mixed<<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, (float)v, A, S, lda, status);
+  k_green_fill_mixed<<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, (float)v, ox, oy, A, S, lda, status);
   return cudaGetLastError();
 }
 template cudaError_t launch_green_fill<double2>(cudaStream_t, const double*, const double*, int, int, int,

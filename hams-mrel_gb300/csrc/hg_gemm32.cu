@@ -225,19 +225,20 @@ cudaError_t launch_wide(cudaStream_t st, int m, int n, int k, float2 alpha, cons
 }
 
 // ---------------------------------------------------------------------------
-// Skinny products, N <= 40 (the blocked triangular solves' updates
-// B2 -= L21 X1 with all right-hand sides at once): 32 rows x CW = 4*CPT
-// columns per CTA, 128 threads (one row x CPT columns each), 32-deep stages
-// double-buffered by cp.async.  Small tiles give enough CTAs to fill the GPU
-// without splitting K.
+// Skinny products, N <= 48 (the blocked triangular solves' updates
+// B2 -= L21 X1 with all right-hand sides at once): 32 rows x CW = 8*CPT
+// columns per CTA, 256 threads (one row x CPT columns each; eight warps so
+// that an SM holding one or two CTAs still has enough warps to issue), 32-deep
+// stages double-buffered by cp.async.  Small tiles give enough CTAs to
+// fill the GPU without splitting K.
 // ---------------------------------------------------------------------------
-constexpr int kSRows = 32, kSK = 32, kSThreads = 128, kSMaxCW = 40;
+constexpr int kSRows = 32, kSK = 32, kSThreads = 256, kSMaxCW = 48, kSStages = 2;
 
 template <int CPT, bool VEC>
 __device__ __forceinline__ void skinny_stage(float2* As, float2* Bs, const float2* __restrict__ A, long lda,
                                              const float2* __restrict__ B, long ldb, int m, int n, int k, int m0,
                                              int k0, int tid) {
-  constexpr int CW = 4 * CPT;
+  constexpr int CW = 8 * CPT;
   if (VEC) {
 #pragma unroll
     for (int it = 0; it < kSK * kSRows / 2 / kSThreads; ++it) {
@@ -270,23 +271,27 @@ template <int CPT, bool VEC>
 __global__ void __launch_bounds__(kSThreads)
 k_cgemm_skinny(int m, int n, int k, float2 alpha, const float2* __restrict__ A, long lda,
                const float2* __restrict__ B, long ldb, float2 beta, float2* __restrict__ C, long ldc) {
-  constexpr int CW = 4 * CPT;
-  __shared__ __align__(16) float2 As[2][kSK * kSRows];
-  __shared__ __align__(16) float2 Bs[2][kSK * CW];
+  constexpr int CW = 8 * CPT;
+  __shared__ __align__(16) float2 As[kSStages][kSK * kSRows];
+  __shared__ __align__(16) float2 Bs[kSStages][kSK * CW];
   const int tid = threadIdx.x, tx = tid & 31, cg = tid >> 5;
   const int m0 = blockIdx.x * kSRows;
   float ar[CPT], ai[CPT];
 #pragma unroll
   for (int j = 0; j < CPT; ++j) { ar[j] = 0.f; ai[j] = 0.f; }
   const int nst = (k + kSK - 1) / kSK;
-  skinny_stage<CPT, VEC>(As[0], Bs[0], A, lda, B, ldb, m, n, k, m0, 0, tid);
-  cp_async_commit();
-  for (int s = 0; s < nst; ++s) {
-    const int b = s & 1;
-    if (s + 1 < nst) skinny_stage<CPT, VEC>(As[b ^ 1], Bs[b ^ 1], A, lda, B, ldb, m, n, k, m0, (s + 1) * kSK, tid);
+#pragma unroll
+  for (int s = 0; s < kSStages - 1; ++s) {
+    if (s < nst) skinny_stage<CPT, VEC>(As[s], Bs[s], A, lda, B, ldb, m, n, k, m0, s * kSK, tid);
     cp_async_commit();
-    cp_async_wait<1>();
-    __syncthreads();
+  }
+  for (int s = 0; s < nst; ++s) {
+    const int b = s % kSStages;
+    cp_async_wait<kSStages - 2>();
+    __syncthreads();  // stage s landed; the buffer of stage s - 1 is free again
+    const int sn = s + kSStages - 1;
+    if (sn < nst) skinny_stage<CPT, VEC>(As[sn % kSStages], Bs[sn % kSStages], A, lda, B, ldb, m, n, k, m0, sn * kSK, tid);
+    cp_async_commit();
     const float2* as = As[b];
     const float2* bs = Bs[b] + cg * CPT;
 #pragma unroll 4
@@ -305,7 +310,6 @@ k_cgemm_skinny(int m, int n, int k, float2 alpha, const float2* __restrict__ A, 
         ai[j + 1] = fmaf(a.y, bb.z, ai[j + 1]);
       }
     }
-    __syncthreads();
   }
   const int row = m0 + tx;
   if (row >= m) return;
@@ -339,12 +343,10 @@ cudaError_t cgemm_skinny(cudaStream_t st, int m, int n, int k, float2 alpha, con
   if (m <= 0 || n <= 0) return cudaSuccess;
   if (n > kSMaxCW) return cudaErrorInvalidValue;
   const bool vec = (reinterpret_cast<uintptr_t>(A) % 16 == 0) && (lda % 2 == 0);
-  const int per = (n + 3) / 4;
+  const int per = (n + 7) / 8;
   if (per <= 2) return launch_skinny<2>(st, vec, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
   if (per <= 4) return launch_skinny<4>(st, vec, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
-  if (per <= 6) return launch_skinny<6>(st, vec, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
-  if (per <= 8) return launch_skinny<8>(st, vec, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
-  return launch_skinny<10>(st, vec, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  return launch_skinny<6>(st, vec, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
 }
 
 cudaError_t cgemm_wide(cudaStream_t st, bool transa, int m, int n, int k, float2 alpha, const float2* A, long lda,

@@ -25,7 +25,7 @@ cudaError_t launch_green_points_fin(cudaStream_t st, int npts, const double* pts
                                     double* out);
 
 cudaError_t launch_green_fill_mixed(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
-                                    double v, float2* A, float2* S, long lda, int* status);
+                                    double v, double ox, double oy, float2* A, float2* S, long lda, int* status);
 
 cudaError_t launch_incident(cudaStream_t st, int n, const double* xyz_p, const double* dxyz_p, int nbeta,
                             const double* betas, double v, double wk, double w1, double h, double2* w);

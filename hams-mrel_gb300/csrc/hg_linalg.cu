@@ -200,9 +200,9 @@ cudaError_t gemm<float>(cudaStream_t st, bool transa, int m, int n, int k, float
                         long lda, const float2* B, long ldb, float2 beta, float2* C, long ldc, void* ws,
                         size_t ws_bytes) {
   // Split-K (a workspace and a deep K) keeps the older kernel; otherwise
-  // the cp.async kernels: skinny (N <= 40) or wide.
+  // the cp.async kernels: skinny (N <= 48) or wide.
   const bool splitk = ws && k >= 1024;
-  if (!transa && n <= 40 && !splitk) return cgemm_skinny(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  if (!transa && n <= 48 && !splitk) return cgemm_skinny(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
   if (n <= 64)
     return launch_gemm<float, 64, 32, 8, 4, 2>(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, ws, ws_bytes);
   return cgemm_wide(st, transa, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
@@ -366,11 +366,31 @@ constexpr int kOuterNB = 256;
 // Below this order the one-level loop is used (few outer panels to amortise).
 constexpr int kTcMinN = 1024;
 
-// Workspace: the tensor-core GEMM's packed operands, then the 256 x 256
-// block I - L11^-1 used to form U12 by a GEMM.
+// Workspace of the two-level LU (complex64, tensor cores), in order:
+//   tc    the tensor-core GEMM's packed operands
+//   minv  I - L11^-1 of the current outer panel (256 x 256), to form U12 by a GEMM
+//   linv  L_kk^-1 of every 256-wide diagonal block (256 x 256 each, kept for getrs_inv)
+//   uinv  U_kk^-1 of every diagonal block
+//   y     the intermediate solution of getrs_inv (n x kSolveChunk)
+constexpr int kSolveChunk = 64;
+struct LuWork {
+  size_t tc, minv, linv, uinv, y, total;
+  explicit LuWork(int n) {
+    const size_t blk = (size_t)kOuterNB * kOuterNB * sizeof(float2);
+    const size_t nblk = (size_t)((n + kOuterNB - 1) / kOuterNB);
+    auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+    tc = 0;
+    minv = up(cgemm_tc_work_bytes(n, n, kOuterNB));
+    linv = minv + blk;
+    uinv = linv + nblk * blk;
+    y = uinv + nblk * blk;
+    total = y + up((size_t)n * kSolveChunk * sizeof(float2));
+  }
+};
+
 size_t lu_work_bytes(int n, int tc_passes) {
   if (tc_passes == 0 || n < kTcMinN) return 0;
-  return cgemm_tc_work_bytes(n, n, kOuterNB) + (size_t)kOuterNB * kOuterNB * sizeof(float2) + 256;
+  return LuWork(n).total;
 }
 
 namespace {
@@ -411,19 +431,64 @@ cudaError_t factor_columns(cudaStream_t st, bool use_cluster, int n, typename cx
   return cudaGetLastError();
 }
 
-__global__ void k_set_eye(int nb, float2* X) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
-  if (r < nb) X[r + (long)c * nb] = make_float2(r == c ? 1.f : 0.f, 0.f);
-}
-// X <- I - X
-__global__ void k_eye_minus(int nb, float2* X) {
+// Y <- I - X
+__global__ void k_eye_minus(int nb, const float2* X, int ldx, float2* Y, int ldy) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
   if (r < nb) {
-    float2 v = X[r + (long)c * nb];
+    float2 v = X[r + (long)c * ldx];
     v.x = (r == c ? 1.f : 0.f) - v.x;
     v.y = -v.y;
-    X[r + (long)c * nb] = v;
+    Y[r + (long)c * ldy] = v;
   }
+}
+
+// Y[0:jb, 0:nc] = M[0:jb, 0:jb] X[0:jb, 0:nc] for one diagonal block's
+// inverse M (leading dimension 256).  It sits on the serial chain of the
+// blocked solve, so it is cut into many short CTAs: a 32 x 8 output tile per
+// CTA, the 256-deep inner dimension split over the 8 warps (lane = row, 32
+// independent loads of M per thread in flight), X's 256 x 8 slice staged in
+// shared memory, and the 8 partial tiles added in shared memory.
+__global__ void __launch_bounds__(256)
+k_apply_inv(int jb, int nc, const float2* __restrict__ M, const float2* __restrict__ X, long ldx,
+            float2* __restrict__ Y, long ldy) {
+  __shared__ float2 xs[kOuterNB][8];
+  __shared__ float2 red[8][32][9];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 8;
+  for (int e = threadIdx.x; e < kOuterNB * 8; e += 256) {
+    const int p = e % kOuterNB, c = e / kOuterNB;
+    xs[p][c] = (p < jb && c0 + c < nc) ? X[p + (long)(c0 + c) * ldx] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const int r = r0 + lane;
+  float ar[8], ai[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) { ar[j] = 0.f; ai[j] = 0.f; }
+  const int p0 = w * 32;
+  if (r < jb) {
+#pragma unroll 8
+    for (int q = 0; q < 32; ++q) {
+      const int p = p0 + q;
+      const float2 m = (p < jb) ? M[r + (long)p * kOuterNB] : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const float2 x = xs[p][j];
+        ar[j] = fmaf(m.x, x.x, fmaf(-m.y, x.y, ar[j]));
+        ai[j] = fmaf(m.x, x.y, fmaf(m.y, x.x, ai[j]));
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j) red[w][lane][j] = make_float2(ar[j], ai[j]);
+  __syncthreads();
+  const int rr = threadIdx.x & 31, cc = threadIdx.x >> 5;  // one output per thread
+  float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    acc.x += red[k][rr][cc].x;
+    acc.y += red[k][rr][cc].y;
+  }
+  if (r0 + rr < jb && c0 + cc < nc) Y[(r0 + rr) + (long)(c0 + cc) * ldy] = acc;
 }
 
 }  // namespace
@@ -443,20 +508,27 @@ cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* i
   // L11^-1 from one column-parallel triangular solve of the identity (the
   // GEMM packs its B operand, here A12, before it overwrites A12).
   typedef typename cx<R>::T T;
-  const size_t tcb = cgemm_tc_work_bytes(n, n, kOuterNB);
-  float2* Minv = reinterpret_cast<float2*>(static_cast<char*>(work) + ((tcb + 255) / 256) * 256);
+  const LuWork lw(n);
+  const size_t tcb = lw.minv;
+  char* wb = static_cast<char*>(work);
+  float2* Minv = reinterpret_cast<float2*>(wb + lw.minv);
+  const size_t blk = (size_t)kOuterNB * kOuterNB;
   for (int K = 0; K < n; K += kOuterNB) {
     const int jbo = (n - K < kOuterNB) ? n - K : kOuterNB;
     e = factor_columns<R>(st, use_cluster, n, A, lda, K, K + jbo, ipiv, info);
     if (e != cudaSuccess) return e;
     k_laswp<T><<<(n + 127) / 128, 128, 0, st>>>(A, lda, n, ipiv, K, K + jbo, K, K + jbo);
+    // inverse of this diagonal block's unit-lower triangle (for U12 here and
+    // for getrs_inv); the upper triangles' inverses follow after the loop
+    float2* Linv_all = reinterpret_cast<float2*>(wb + lw.linv);
+    const float2* Linv = Linv_all + (size_t)(K / kOuterNB) * blk;
+    e = trsm_inverse_blocks<float>(st, false, reinterpret_cast<const float2*>(A), lda, n, kOuterNB, Linv_all, kOuterNB,
+                                   K / kOuterNB, 1);
+    if (e != cudaSuccess) return e;
+    const dim3 eg((jbo + 127) / 128, jbo);
     const int rest = n - K - jbo;
     if (rest > 0) {
-      const dim3 eg((jbo + 127) / 128, jbo);
-      k_set_eye<<<eg, 128, 0, st>>>(jbo, Minv);
-      e = trsm_cols<float>(st, false, reinterpret_cast<const float2*>(A + K + (long)K * lda), lda, jbo, Minv, jbo, jbo);
-      if (e != cudaSuccess) return e;
-      k_eye_minus<<<eg, 128, 0, st>>>(jbo, Minv);
+      k_eye_minus<<<eg, 128, 0, st>>>(jbo, Linv, kOuterNB, Minv, jbo);
       float2* A12 = reinterpret_cast<float2*>(A + K + (long)(K + jbo) * lda);
       e = cgemm_tc(st, tc_passes, jbo, rest, jbo, Minv, jbo, A12, lda, A12, lda, work, tcb, info);
       if (e != cudaSuccess) return e;
@@ -465,10 +537,57 @@ cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* i
       if (e != cudaSuccess) return e;
     }
   }
-  return cudaGetLastError();
+  // U_kk^-1 of every diagonal block, in one launch
+  return trsm_inverse_blocks<float>(st, true, reinterpret_cast<const float2*>(A), lda, n, kOuterNB,
+                                    reinterpret_cast<float2*>(wb + lw.uinv), kOuterNB, 0, (n + kOuterNB - 1) / kOuterNB);
 }
 
 constexpr int kSolveNB = 256;
+
+bool lu_has_inverses(int n, int tc_passes, size_t work_bytes) {
+  return tc_passes != 0 && n >= kTcMinN && work_bytes >= lu_work_bytes(n, tc_passes) && cgemm_tc_supported();
+}
+
+// Triangular solves with the diagonal-block inverses getrf kept: per 256-row
+// block one small GEMM by the block inverse and one update GEMM of the rows
+// below (above), instead of a row-by-row substitution inside each block.
+//   forward:  Y_k = L_kk^-1 B_k;  B_(k+1:) -= L_(k+1:),k Y_k
+//   backward: X_k = U_kk^-1 Y_k;  Y_(:k)   -= U_(:k),k X_k   (X written into B)
+cudaError_t getrs_inv(cudaStream_t st, int n, int nrhs, const float2* LU, long lda, const int* ipiv, float2* B,
+                      long ldb, void* work) {
+  const LuWork lw(n);
+  char* wb = static_cast<char*>(work);
+  const float2* Linv = reinterpret_cast<const float2*>(wb + lw.linv);
+  const float2* Uinv = reinterpret_cast<const float2*>(wb + lw.uinv);
+  float2* Y = reinterpret_cast<float2*>(wb + lw.y);
+  const size_t blk = (size_t)kOuterNB * kOuterNB;
+  const float2 mone = make_float2(-1.f, 0.f), one = make_float2(1.f, 0.f);
+  const int nblk = (n + kOuterNB - 1) / kOuterNB;
+  k_laswp<float2><<<(nrhs + 127) / 128, 128, 0, st>>>(B, ldb, nrhs, ipiv, 0, n, 0, 0);
+  for (int c0 = 0; c0 < nrhs; c0 += kSolveChunk) {
+    const int nc = (nrhs - c0 < kSolveChunk) ? nrhs - c0 : kSolveChunk;
+    float2* Bc = B + (long)c0 * ldb;
+    for (int b = 0; b < nblk; ++b) {
+      const int K = b * kOuterNB, jb = (n - K < kOuterNB) ? n - K : kOuterNB;
+      k_apply_inv<<<dim3((jb + 31) / 32, (nc + 7) / 8), 256, 0, st>>>(jb, nc, Linv + b * blk, Bc + K, ldb, Y + K, n);
+      const int rest = n - K - jb;
+      if (rest > 0) {
+        cudaError_t e = gemm<float>(st, false, rest, nc, jb, mone, LU + (K + jb) + (long)K * lda, lda, Y + K, n, one,
+                                    Bc + K + jb, ldb);
+        if (e != cudaSuccess) return e;
+      }
+    }
+    for (int b = nblk - 1; b >= 0; --b) {
+      const int K = b * kOuterNB, jb = (n - K < kOuterNB) ? n - K : kOuterNB;
+      k_apply_inv<<<dim3((jb + 31) / 32, (nc + 7) / 8), 256, 0, st>>>(jb, nc, Uinv + b * blk, Y + K, n, Bc + K, ldb);
+      if (K > 0) {
+        cudaError_t e = gemm<float>(st, false, K, nc, jb, mone, LU + (long)K * lda, lda, Bc + K, ldb, one, Y, n);
+        if (e != cudaSuccess) return e;
+      }
+    }
+  }
+  return cudaGetLastError();
+}
 
 template <typename R>
 cudaError_t getrs(cudaStream_t st, int n, int nrhs, const typename cx<R>::T* LU, long lda, const int* ipiv,

@@ -37,7 +37,7 @@ cudaError_t resid_df(cudaStream_t st, bool transa, int m, int nc, int k, const f
                      long ldy, const double2* Bin, long ldb, double sign, double2* out, long ldo, void* ws,
                      size_t ws_bytes, bool exact = true);
 
-// Complex64 GEMM for N <= 40 untransposed (hg_gemm32.cu), without split-K.
+// Complex64 GEMM for N <= 48 untransposed (hg_gemm32.cu), without split-K.
 cudaError_t cgemm_skinny(cudaStream_t st, int m, int n, int k, float2 alpha, const float2* A, long lda,
                          const float2* B, long ldb, float2 beta, float2* C, long ldc);
 
@@ -59,6 +59,13 @@ cudaError_t getrs(cudaStream_t st, int n, int nrhs, const typename cx<R>::T* LU,
                   typename cx<R>::T* B, long ldb);
 
 size_t lu_work_bytes(int n, int tc_passes);
+
+// getrs for the complex64 factors of a two-level getrf (tc_passes != 0):
+// uses the inverses of the 256 x 256 diagonal blocks that getrf kept in its
+// workspace.  lu_has_inverses tells whether getrf took that path.
+bool lu_has_inverses(int n, int tc_passes, size_t work_bytes);
+cudaError_t getrs_inv(cudaStream_t st, int n, int nrhs, const float2* LU, long lda, const int* ipiv, float2* B,
+                      long ldb, void* work);
 
 // Complex64 C -= A B on the tcgen05 tensor cores (hg_tc.cu): A m x k (lda),
 // B k x n (ldb), C m x n (ldc), column-major.  passes 3: split-TF32 products
@@ -84,6 +91,14 @@ bool panel_cluster_supported(int m);
 template <typename R>
 cudaError_t trsm_cols(cudaStream_t st, bool upper, const typename cx<R>::T* A, long lda, int jb,
                       typename cx<R>::T* X, long ldx, int ncols);
+
+// Inverses of the diagonal nb x nb blocks nblk_first .. nblk_first + nblk - 1
+// of the n x n factor A (unit lower triangle, or upper triangle), in one
+// launch: block b's inverse goes to X + b nb ldx (an nb x nb block with
+// leading dimension ldx; the last block of order n - b nb if smaller).
+template <typename R>
+cudaError_t trsm_inverse_blocks(cudaStream_t st, bool upper, const typename cx<R>::T* A, long lda, int n, int nb,
+                                typename cx<R>::T* X, long ldx, int nblk_first, int nblk);
 
 // Elementwise conversions between complex128 and complex64 buffers.
 cudaError_t convert_z2c(cudaStream_t st, long count, const double2* src, float2* dst);

@@ -515,27 +515,41 @@ __device__ __forceinline__ void trsm_stage(T* buf, const T* __restrict__ A, long
   }
 }
 
+// Batched form (gridDim.y > 1): block b solves with the diagonal block at
+// A + b a_bstride (order min(jb, ntot - b jb)) for X + b x_bstride.
+// ident: X is taken as the identity (not read), so the solve produces the
+// inverse; sub-blocks where column `col` of the result is known to be zero
+// (above the diagonal for lower, below it for upper) are skipped.
 template <typename T, bool UPPER>
 __global__ void __launch_bounds__(kTrsmBlock)
-k_trsm_col(const T* __restrict__ A, long lda, int jb, T* __restrict__ X, long ldx) {
+k_trsm_col(const T* __restrict__ A, long lda, int jb, T* __restrict__ X, long ldx, long a_bstride, long x_bstride,
+           int ntot, int ident) {
   constexpr int SB = TrsmSub<T>::SB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* bufs = reinterpret_cast<T*>(smem_raw);  // 2 x [SB][kTrsmBlock]
   __shared__ T x[kTrsmBlock];
   const int col = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  A += blockIdx.y * a_bstride;
+  X += blockIdx.y * x_bstride;
+  jb = min(jb, ntot - (int)blockIdx.y * jb);
+  if (ident && col >= jb) return;  // whole CTA: the inverse of a smaller last block has fewer columns
   T* xc = X + (long)col * ldx;
   T zero;
   zero.x = 0; zero.y = 0;
   const int nsb = (jb + SB - 1) / SB;
-  if (tid < jb) x[tid] = xc[tid];
-  int s = UPPER ? nsb - 1 : 0;
+  if (tid < jb) {
+    if (ident) { x[tid] = zero; if (tid == col) x[tid].x = 1; }
+    else x[tid] = xc[tid];
+  }
+  int s = ident ? col / SB : (UPPER ? nsb - 1 : 0);
+  const int iters = UPPER ? s + 1 : nsb - s;
   trsm_stage<T, UPPER>(bufs, A, lda, jb, s, tid);
   cp_async_commit();
-  for (int it = 0; it < nsb; ++it, s += (UPPER ? -1 : 1)) {
+  for (int it = 0; it < iters; ++it, s += (UPPER ? -1 : 1)) {
     T* cur = bufs + (it & 1) * SB * kTrsmBlock;
     cp_async_wait<0>();
     __syncthreads();  // sub-block landed; x and the other buffer are free
-    if (it + 1 < nsb)
+    if (it + 1 < iters)
       trsm_stage<T, UPPER>(bufs + ((it + 1) & 1) * SB * kTrsmBlock, A, lda, jb, s + (UPPER ? -1 : 1), tid);
     cp_async_commit();
     const int c0 = s * SB, w = min(SB, jb - c0);
@@ -580,10 +594,28 @@ cudaError_t trsm_cols(cudaStream_t st, bool upper, const typename cx<R>::T* A, l
   auto kern = upper ? k_trsm_col<T, true> : k_trsm_col<T, false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  kern<<<ncols, kTrsmBlock, smem, st>>>(A, lda, jb, X, ldx);
+  kern<<<ncols, kTrsmBlock, smem, st>>>(A, lda, jb, X, ldx, 0, 0, jb, 0);
   return cudaGetLastError();
 }
 template cudaError_t trsm_cols<float>(cudaStream_t, bool, const float2*, long, int, float2*, long, int);
 template cudaError_t trsm_cols<double>(cudaStream_t, bool, const double2*, long, int, double2*, long, int);
+
+template <typename R>
+cudaError_t trsm_inverse_blocks(cudaStream_t st, bool upper, const typename cx<R>::T* A, long lda, int n, int nb,
+                                typename cx<R>::T* X, long ldx, int nblk_first, int nblk) {
+  typedef typename cx<R>::T T;
+  if (nb > kTrsmBlock) return cudaErrorInvalidValue;
+  if (nblk <= 0) return cudaSuccess;
+  const int smem = 2 * TrsmSub<T>::SB * kTrsmBlock * (int)sizeof(T);
+  auto kern = upper ? k_trsm_col<T, true> : k_trsm_col<T, false>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  const long k0 = (long)nblk_first * nb;
+  kern<<<dim3(nb, nblk), kTrsmBlock, smem, st>>>(A + k0 + k0 * lda, lda, nb, X + (long)nblk_first * nb * ldx, ldx,
+                                                 (long)nb * (1 + lda), (long)nb * ldx, n - (int)k0, 1);
+  return cudaGetLastError();
+}
+template cudaError_t trsm_inverse_blocks<float>(cudaStream_t, bool, const float2*, long, int, int, float2*, long, int,
+                                                int);
 
 }  // namespace hg

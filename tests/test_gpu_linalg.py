@@ -6,7 +6,9 @@ routines are the checker here.  The shapes cover the library's code paths:
 an odd leading dimension (8-byte operand staging), an even one (16-byte
 staging), more than 64 right-hand sides (the wide GEMM with a 256-deep inner
 dimension in the blocked solves) and a matrix small enough to skip the wide
-GEMM altogether.
+GEMM altogether; orders >= 1024 take the complex64 two-level LU with
+tensor-core updates and the block-inverse triangular solves (one and two
+64-column chunks of right-hand sides).
 """
 import numpy as np
 import pytest
@@ -47,7 +49,7 @@ def solver(pkg):
     s.close()
 
 
-SHAPES = [(701, 3), (768, 70), (50, 4), (1030, 38)]
+SHAPES = [(701, 3), (768, 70), (50, 4), (1030, 38), (1100, 70)]
 
 
 @pytest.mark.parametrize("n,nrhs", SHAPES)
