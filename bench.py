@@ -219,7 +219,8 @@ def ours(args, dist, rank, world, local):
         vals = [_frequency_inputs(pkg, w) for w in ws]
         return (np.array([x[0] for x in vals]), np.array([x[1] for x in vals]), np.array([x[2] for x in vals]))
 
-    s = hg.Solver(precision=prec, device=local)
+    sopts = dict(lu_tensor=args.lu_tensor, refine_method=1 if args.refine == "gmres" else 0)
+    s = hg.Solver(precision=prec, device=local, **sopts)
     s.set_mesh(mesh.nodes, mesh.ncon, mesh.ncn, mesh.xyz_p, mesh.ds, mesh.pnsz, mesh.dxyz_p, mesh.body_ranges)
     # warm-up: at least one frequency per slot, so that every slot has its buffers
     warm = max(args.warmup, nslots)
@@ -244,7 +245,7 @@ def ours(args, dist, rank, world, local):
 
     # ---- end to end through the C ABI with host buffers: new context, mesh upload,
     #      the sweep, forces and all potentials read back to host memory ----
-    s2 = hg.Solver(precision=prec, device=local)
+    s2 = hg.Solver(precision=prec, device=local, **sopts)
     _barrier(dist)
     t0 = time.perf_counter()
     s2.set_mesh(mesh.nodes, mesh.ncon, mesh.ncn, mesh.xyz_p, mesh.ds, mesh.pnsz, mesh.dxyz_p, mesh.body_ranges)
@@ -293,7 +294,8 @@ def ours(args, dist, rank, world, local):
             "scaling": "weak", "vs_baseline": None,
             "dtype": "complex64+fp64-refine" if prec == hg.HG_PREC_MIXED else "complex128",
             "data": "synthetic",
-            "config": dict(CONFIG, precision=args.precision, parallelism=f"replicas{world}", slots=nslots),
+            "config": dict(CONFIG, precision=args.precision, parallelism=f"replicas{world}", slots=nslots,
+                           refine=args.refine, lu_tensor=args.lu_tensor),
             "latency_ms": {"p50": lat_sorted[len(lat) // 2], "p99": lat_sorted[min(len(lat) - 1,
                                                                                   int(0.99 * len(lat)))],
                            "what": f"host wall time per frequency-solve with {nslots} solves in flight"},
@@ -369,6 +371,10 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--slots", type=int, default=4, help="frequency-solves in flight (hg_solve_sweep slots)")
+    ap.add_argument("--refine", default="classical", choices=["classical", "gmres"],
+                    help="mixed-form refinement: classical iterative refinement or GMRES-IR")
+    ap.add_argument("--lu-tensor", type=int, default=3, choices=[0, 1, 3],
+                    help="LU trailing updates: 3 split-TF32 tensor cores, 1 TF32, 0 FP32 SIMT")
     args = ap.parse_args()
     if args.impl == "reference":
         rank = int(os.environ.get("RANK", "0"))

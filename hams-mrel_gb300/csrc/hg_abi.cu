@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <complex>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -74,6 +75,9 @@ struct hg_ctx {
   DevBuf<unsigned char> luws;            // packed operands of the tensor-core LU updates
   DevBuf<double> amas, bdmp;
   DevBuf<double> nrm;                    // column norms of the refinement (2 x columns)
+  DevBuf<double2> gV, gZ, gW, gH, gY;    // GMRES refinement: Krylov basis, preconditioned basis, work, Hessenberg, y
+  DevBuf<double> gN;
+  int inner_its = 0;                     // GMRES iterations of the last solve
   int irsp = 0;
   bool factored = false;
   bool keep = false;
@@ -185,6 +189,165 @@ __global__ void k_colmax(int rows, const double2* __restrict__ M, long ld, doubl
   }
 }
 
+// y = M z for the square system of the mixed form (M = A, or A^T A for
+// irsp = 1), FP64-accurate products with the complex64 matrix (hg_resid.cu).
+int apply_op(hg_ctx* c, int c0, int nc, const float2* A0, const double2* Z, double2* out) {
+  const int n = c->n, tn = c->tn;
+  if (c->irsp == 1) {
+    double2* R1 = c->R.p + (size_t)c0 * tn;
+    CK(hg::resid_df(c->st, false, tn, nc, n, A0, tn, Z, n, nullptr, 0, 1.0, R1, tn, c->rws.p, c->rws.cap));
+    CK(hg::resid_df(c->st, true, n, nc, tn, A0, tn, R1, tn, nullptr, 0, 1.0, out, n, c->rws.p, c->rws.cap));
+  } else {
+    CK(hg::resid_df(c->st, false, n, nc, n, A0, tn, Z, n, nullptr, 0, 1.0, out, n, c->rws.p, c->rws.cap));
+  }
+  return 0;
+}
+
+// GMRES-based iterative refinement (Carson and Higham's GMRES-IR) built on
+// the restarted GMRES of IterativeSolvers.f90:324-488: per outer step the
+// FP64 residual r = b - M x, then GMRES on M d = r right-preconditioned by
+// the complex64 LU (z = LU^-1 v), x += d.  All right-hand-side columns run
+// together (each column its own Krylov basis, Hessenberg matrix and Givens
+// rotations, the latter on the host as in ZGIVENS_ROTATION); the inner
+// GMRES stops per column at a residual reduction of 1e-4 (the reference's
+// GMRES tolerance) or after kGmresRestart iterations, the outer loop when
+// max|r| / max|b| <= refine_tol for every column or after max_refine steps.
+constexpr int kGmresRestart = 8;
+constexpr double kGmresInnerTol = 1e-4;
+
+template <typename Solve>
+int refine_gmres(hg_ctx* c, int c0, int c1, const float2* LU, long ldlu, const float2* A0, const double2* Bc,
+                 double2* Xc, double2* Rh, const std::vector<double>& bnorm, Solve& lu_solve, int* sweeps_out,
+                 double* worst_out) {
+  (void)LU;
+  (void)ldlu;
+  const int n = c->n, nc = c1 - c0, m = kGmresRestart;
+  const size_t blk = (size_t)n * nc;
+  float2* Bf = c->Bf.p + (size_t)c0 * n;
+  CK(c->gV.ensure(blk * (m + 1)));
+  CK(c->gZ.ensure(blk * m));
+  CK(c->gW.ensure(blk));
+  CK(c->gH.ensure((size_t)2 * (m + 1) * nc));
+  CK(c->gY.ensure((size_t)m * nc));
+  CK(c->gN.ensure(nc));
+  double2* V = c->gV.p;
+  double2* Z = c->gZ.p;
+  double2* W = c->gW.p;
+  double2* H1 = c->gH.p;
+  double2* H2 = c->gH.p + (size_t)(m + 1) * nc;
+  std::vector<double> rnorm(nc), beta(nc), hn(nc);
+  std::vector<double2> hcol((size_t)(m + 1) * nc), hc2((size_t)(m + 1) * nc);
+  // per column: Hessenberg (column-major (m+1) x m), rotations, g
+  typedef std::complex<double> zd;
+  std::vector<zd> Hh((size_t)nc * (m + 1) * m), cs((size_t)nc * m), sn((size_t)nc * m), g((size_t)nc * (m + 1));
+  std::vector<double2> yh((size_t)m * nc);
+  double worst = 0.0;
+  int outer = 0, inner_total = 0;
+  for (;;) {
+    // r = b - M x
+    if (c->irsp == 1) {
+      double2* R1 = c->R.p + (size_t)c0 * c->tn;
+      CK(hg::resid_df(c->st, false, c->tn, nc, n, A0, c->tn, Xc, n, Bc, c->tn, -1.0, R1, c->tn, c->rws.p, c->rws.cap));
+      CK(hg::resid_df(c->st, true, n, nc, c->tn, A0, c->tn, R1, c->tn, nullptr, 0, 1.0, Rh, n, c->rws.p, c->rws.cap));
+    } else {
+      CK(hg::resid_df(c->st, false, n, nc, n, A0, c->tn, Xc, n, Bc, c->tn, -1.0, Rh, n, c->rws.p, c->rws.cap));
+    }
+    k_colmax<<<nc, 256, 0, c->st>>>(n, Rh, n, c->nrm.p + nc);
+    CK(cudaMemcpyAsync(rnorm.data(), c->nrm.p + nc, nc * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(hg::col_norm2(c->st, n, nc, Rh, n, c->gN.p));
+    CK(cudaMemcpyAsync(beta.data(), c->gN.p, nc * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    worst = 0.0;
+    for (int k = 0; k < nc; ++k) worst = std::fmax(worst, bnorm[k] > 0 ? rnorm[k] / bnorm[k] : rnorm[k]);
+    if (worst <= c->o.refine_tol || outer >= c->o.max_refine) break;
+    ++outer;
+    // GMRES on M d = r, d0 = 0: V_0 = r / ||r||
+    CK(hg::col_scale(c->st, n, nc, Rh, n, c->gN.p, V, n));
+    std::fill(Hh.begin(), Hh.end(), zd(0, 0));
+    std::fill(g.begin(), g.end(), zd(0, 0));
+    for (int k = 0; k < nc; ++k) g[(size_t)k * (m + 1)] = zd(beta[k], 0);
+    int mact = 0;
+    for (int j = 0; j < m; ++j) {
+      // Z_j = LU^-1 V_j (complex64 solve), W = M Z_j
+      CK(hg::convert_z2c_2d(c->st, n, nc, V + j * blk, n, Bf, n));
+      CK(lu_solve(Bf));
+      CK(hg::convert_c2z_2d(c->st, n, nc, Bf, n, Z + j * blk, n));
+      int r = apply_op(c, c0, nc, A0, Z + j * blk, W);
+      if (r) return r;
+      // two passes of classical Gram-Schmidt against V_0..V_j
+      CK(hg::col_dots(c->st, n, nc, j + 1, V, n, (long)blk, W, n, H1, m + 1));
+      CK(hg::col_axpy(c->st, n, nc, j + 1, V, n, (long)blk, H1, m + 1, W, n, -1.0));
+      CK(hg::col_dots(c->st, n, nc, j + 1, V, n, (long)blk, W, n, H2, m + 1));
+      CK(hg::col_axpy(c->st, n, nc, j + 1, V, n, (long)blk, H2, m + 1, W, n, -1.0));
+      CK(hg::col_norm2(c->st, n, nc, W, n, c->gN.p));
+      CK(hg::col_scale(c->st, n, nc, W, n, c->gN.p, V + (j + 1) * blk, n));
+      CK(cudaMemcpyAsync(hcol.data(), H1, (size_t)(m + 1) * nc * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+      CK(cudaMemcpyAsync(hc2.data(), H2, (size_t)(m + 1) * nc * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+      CK(cudaMemcpyAsync(hn.data(), c->gN.p, nc * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+      ++inner_total;
+      mact = j + 1;
+      bool all = true;
+      for (int k = 0; k < nc; ++k) {
+        zd* Hk = &Hh[(size_t)k * (m + 1) * m];
+        zd* ck = &cs[(size_t)k * m];
+        zd* sk = &sn[(size_t)k * m];
+        zd* gk = &g[(size_t)k * (m + 1)];
+        zd* h = Hk + (size_t)j * (m + 1);
+        for (int i = 0; i <= j; ++i) {
+          const double2 a = hcol[i + (size_t)k * (m + 1)], b = hc2[i + (size_t)k * (m + 1)];
+          h[i] = zd(a.x + b.x, a.y + b.y);
+        }
+        h[j + 1] = zd(hn[k], 0);
+        for (int i = 0; i < j; ++i) {  // previous rotations
+          const zd t = ck[i] * h[i] + sk[i] * h[i + 1];
+          h[i + 1] = -std::conj(sk[i]) * h[i] + std::conj(ck[i]) * h[i + 1];
+          h[i] = t;
+        }
+        // new rotation zeroing h[j+1] (ZGIVENS_ROTATION)
+        const zd a = h[j], b = h[j + 1];
+        zd cv(1, 0), sv(0, 0);
+        if (std::abs(b) < 1e-300) {
+        } else if (std::abs(a) < 1e-300) {
+          cv = zd(0, 0);
+          sv = zd(1, 0);
+        } else {
+          const double den = std::sqrt(std::norm(a) + std::norm(b));
+          cv = std::abs(a) / den;
+          sv = (a / std::abs(a)) * std::conj(b) / den;
+        }
+        ck[j] = cv;
+        sk[j] = sv;
+        h[j] = cv * a + sv * b;
+        h[j + 1] = 0;
+        const zd t = cv * gk[j] + sv * gk[j + 1];
+        gk[j + 1] = -std::conj(sv) * gk[j] + std::conj(cv) * gk[j + 1];
+        gk[j] = t;
+        if (beta[k] > 0 && std::abs(gk[j + 1]) > kGmresInnerTol * beta[k]) all = false;
+      }
+      if (all) break;
+    }
+    // y = H^-1 g per column, then x += sum_j y_j Z_j
+    for (int k = 0; k < nc; ++k) {
+      const zd* Hk = &Hh[(size_t)k * (m + 1) * m];
+      const zd* gk = &g[(size_t)k * (m + 1)];
+      std::vector<zd> y(gk, gk + mact);
+      for (int i = mact - 1; i >= 0; --i) {
+        const zd d = Hk[i + (size_t)i * (m + 1)];
+        y[i] = (std::abs(d) < 1e-300) ? zd(0, 0) : y[i] / d;
+        for (int q = 0; q < i; ++q) y[q] -= Hk[q + (size_t)i * (m + 1)] * y[i];
+      }
+      for (int i = 0; i < m; ++i) yh[i + (size_t)k * m] = i < mact ? make_double2(y[i].real(), y[i].imag()) : make_double2(0, 0);
+    }
+    CK(cudaMemcpyAsync(c->gY.p, yh.data(), (size_t)m * nc * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+    CK(hg::col_axpy(c->st, n, nc, mact, Z, n, (long)blk, c->gY.p, m, Xc, n, 1.0));
+  }
+  *sweeps_out = outer;
+  *worst_out = worst;
+  c->inner_its = inner_total;
+  return 0;
+}
+
 // Solve M X[:, c0:c1] = rhs for the current factorisation.  rhs is B (tn
 // rows) for irsp = 0, or the normal-equation right-hand side A^T B for irsp = 1.
 int solve_cols(hg_ctx* c, int c0, int c1) {
@@ -237,6 +400,14 @@ int solve_cols(hg_ctx* c, int c0, int c1) {
   CK(hg::add_c2z_2d(c->st, n, nc, Bf, n, Xc, n));
   int sweep = 0;
   double worst = 0.0;
+  c->inner_its = 0;
+  if (c->o.refine_method == 1) {
+    const int r = refine_gmres(c, c0, c1, LU, ldlu, A0, Bc, Xc, Rh, bnorm, lu_solve, &sweep, &worst);
+    if (r) return r;
+    c->sweeps = sweep;
+    c->resid = worst;
+    return 0;
+  }
   for (;;) {
     // r = b - M x in FP64 (M = A, or A^T A applied as A^T (B - A x))
     if (c->irsp == 1) {
@@ -302,6 +473,7 @@ void hg_default_opts(hg_opts* o) {
   o->grn_kind = 8;
   o->max_refine = 10;
   o->refine_tol = 1e-10;
+  o->refine_method = 0;
   o->rho = 1000.0;
   o->g = 9.80665;
   o->lu_tensor = 3;
@@ -317,6 +489,7 @@ int hg_create(hg_ctx** out, const hg_opts* opts) {
   if (c->o.precision != HG_PREC_FP64 && c->o.precision != HG_PREC_MIXED) { delete c; return -2; }
   if (c->o.grn_kind != 4 && c->o.grn_kind != 8) { delete c; return -2; }
   if (c->o.lu_tensor != 0 && c->o.lu_tensor != 1 && c->o.lu_tensor != 3) { delete c; return -2; }
+  if (c->o.refine_method != 0 && c->o.refine_method != 1) { delete c; return -2; }
   cudaError_t e = cudaSetDevice(c->o.device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
   for (int k = 0; k < 5 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
@@ -807,6 +980,12 @@ int hg_refine_info(const hg_ctx* c, int* sweeps, double* residual) {
   if (!c) return -1;
   if (sweeps) *sweeps = c->sweeps;
   if (residual) *residual = c->resid;
+  return 0;
+}
+
+int hg_gmres_iterations(const hg_ctx* c, int* iterations) {
+  if (!c) return -1;
+  if (iterations) *iterations = c->inner_its;
   return 0;
 }
 

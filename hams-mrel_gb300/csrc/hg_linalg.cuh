@@ -100,6 +100,20 @@ template <typename R>
 cudaError_t trsm_inverse_blocks(cudaStream_t st, bool upper, const typename cx<R>::T* A, long lda, int n, int nb,
                                 typename cx<R>::T* X, long ldx, int nblk_first, int nblk);
 
+// Column-batched FP64 vector kernels of the GMRES refinement (hg_gmres.cu).
+// Blocks V_i = V + i vstride are n x nc (leading dimension ldv).
+//   col_dots:  H[i + c ldh] = V_i[:, c]^H W[:, c], i < nv
+//   col_axpy:  W[:, c] += sign sum_{i < nv} H[i + c ldh] V_i[:, c]
+//   col_norm2: out[c] = ||W[:, c]||_2;  col_scale: out[:, c] = W[:, c] / s[c]
+cudaError_t col_dots(cudaStream_t st, int n, int nc, int nv, const double2* V, long ldv, long vstride, const double2* W,
+                     long ldw, double2* H, int ldh);
+cudaError_t col_axpy(cudaStream_t st, int n, int nc, int nv, const double2* V, long ldv, long vstride,
+                     const double2* H, int ldh, double2* W, long ldw, double sign);
+cudaError_t col_norm2(cudaStream_t st, int n, int nc, const double2* W, long ldw, double* out);
+cudaError_t col_scale(cudaStream_t st, int n, int nc, const double2* W, long ldw, const double* s, double2* out,
+                      long ldo);
+cudaError_t convert_c2z_2d(cudaStream_t st, int rows, int cols, const float2* src, long lds, double2* dst, long ldd);
+
 // Elementwise conversions between complex128 and complex64 buffers.
 cudaError_t convert_z2c(cudaStream_t st, long count, const double2* src, float2* dst);
 cudaError_t convert_c2z(cudaStream_t st, long count, const float2* src, double2* dst);

@@ -24,14 +24,14 @@ EXPORTS = [
     "hg_solve_frequency", "hg_keep_matrices", "hg_get_matrix", "hg_green_points", "hg_refine_info",
     "hg_stage_times", "hg_dispersion", "hg_wave_properties", "hg_panel_geometry", "hg_mark", "hg_elapsed",
     "hg_bench_gemm", "hg_green_points_noalloc", "hg_gesv", "hg_gemm_check",
-    "hg_solve_sweep",
+    "hg_solve_sweep", "hg_gmres_iterations",
 ]
 
 
 class HgOpts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("precision", ctypes.c_int), ("grn_kind", ctypes.c_int),
                 ("max_refine", ctypes.c_int), ("refine_tol", ctypes.c_double), ("rho", ctypes.c_double),
-                ("g", ctypes.c_double), ("lu_tensor", ctypes.c_int)]
+                ("g", ctypes.c_double), ("lu_tensor", ctypes.c_int), ("refine_method", ctypes.c_int)]
 
 
 _LIB = None
@@ -79,6 +79,7 @@ def load(build_if_missing: bool = True):
     L.hg_get_matrix.argtypes = [c_void_p, c_int, c_void_p, c_int]
     L.hg_green_points.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p]
     L.hg_refine_info.argtypes = [c_void_p, P(c_int), P(c_double)]
+    L.hg_gmres_iterations.argtypes = [c_void_p, P(c_int)]
     L.hg_stage_times.argtypes = [c_void_p, P(ctypes.c_float)]
     L.hg_green_points_noalloc.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p]
     L.hg_gesv.argtypes = [c_void_p, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_void_p, c_int, P(c_int),
@@ -146,13 +147,14 @@ class Solver:
 
     def __init__(self, precision: int = HG_PREC_FP64, device: int = 0, grn_kind: int = 8,
                  max_refine: int = 10, refine_tol: float = 1e-10, rho: float = 1000.0, g: float = 9.80665,
-                 lu_tensor: int = 3):
+                 lu_tensor: int = 3, refine_method: int = 0):
         self.L = load()
         opts = HgOpts()
         self.L.hg_default_opts(ctypes.byref(opts))
         opts.device, opts.precision, opts.grn_kind = device, precision, grn_kind
         opts.max_refine, opts.refine_tol, opts.rho, opts.g = max_refine, refine_tol, rho, g
         opts.lu_tensor = lu_tensor
+        opts.refine_method = refine_method
         h = ctypes.c_void_p()
         rc = self.L.hg_create(ctypes.byref(h), ctypes.byref(opts))
         if rc != 0:
@@ -326,6 +328,11 @@ class Solver:
         ms = ctypes.c_float()
         self._check(self.L.hg_bench_gemm(self.h, variant, m, n, k, iters, ctypes.byref(ms)))
         return ms.value
+
+    def gmres_iterations(self):
+        it = ctypes.c_int()
+        self.L.hg_gmres_iterations(self.h, ctypes.byref(it))
+        return it.value
 
     def refine_info(self):
         s = ctypes.c_int(); r = ctypes.c_double()

@@ -49,6 +49,10 @@ typedef struct {
                             tensor cores, 3 = split TF32 (three products, single-precision
                             quality; default), 1 = TF32 (one product, more refinement sweeps),
                             0 = FP32 SIMT kernels only */
+    int refine_method;   /* mixed form: 0 = classical iterative refinement (x += LU^-1 r per
+                            sweep; default), 1 = GMRES-based refinement (restarted GMRES of
+                            src/IterativeSolvers.f90:324-488 on A d = r, right-preconditioned by
+                            the complex64 LU); both stop on refine_tol / max_refine */
 } hg_opts;
 
 /* Fill opts with the defaults above (device 0, FP64, GRN_KIND 8, rho 1000, g 9.80665, lu_tensor 3). */
@@ -216,6 +220,9 @@ int hg_gesv(hg_ctx *ctx, int precision, int n, int nrhs, double *a, int lda, int
 
 /* Refinement sweeps taken and final relative residual of the last mixed-form solve. */
 int hg_refine_info(const hg_ctx *ctx, int *sweeps, double *residual);
+/* GMRES iterations (preconditioned operator applications) of the last mixed-form solve
+ * with refine_method = 1 (0 otherwise). */
+int hg_gmres_iterations(const hg_ctx *ctx, int *iterations);
 
 /* CUDA events on the context's stream, for callers that time a sequence of
  * calls on the device: hg_mark records event slot (0..15); hg_elapsed waits
