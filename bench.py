@@ -320,11 +320,13 @@ def _launch_count(n, prec, sweeps=1, nd=30, nbeta=8):
         return 2 * p + 2 * (p - 1)
     if prec == 1 and n >= 1024:
         outer = (n + nbo - 1) // nbo
-        lu = sum(inner(min(nbo, n - k)) for k in range(0, n, nbo)) + outer + 9 * (outer - 1)
+        # per outer panel: pivots to the other columns, L_kk^-1; where columns remain: I - L_kk^-1 and two
+        # tensor-core GEMMs (U12, trailing update) with their operand packing; then one batched U_kk^-1
+        lu = sum(inner(min(nbo, n - k)) for k in range(0, n, nbo)) + 2 * outer + 7 * (outer - 1) + 1
     else:
         lu = inner(n)
     blocks = (n + nbo - 1) // nbo
-    getrs = 1 + 2 * (2 * blocks - 1)                # laswp + (trsm, gemm) down and up
+    getrs = 1 + 2 * (2 * blocks - 1)                # laswp + (trsm or block-inverse product, gemm) down and up
     fill = 1
     forces = 1
     if prec == 0:

@@ -983,6 +983,27 @@ int hg_refine_info(const hg_ctx* c, int* sweeps, double* residual) {
   return 0;
 }
 
+size_t hg_solve_footprint(int precision, int n, int nl, int nbody, int nbeta, int irsp, int lu_tensor) {
+  if (n <= 0 || nbody <= 0 || nbeta < 0) return 0;
+  const size_t tn = (size_t)n + (irsp == 1 ? (size_t)(nl > 0 ? nl : 0) : 0);
+  const size_t nn = (size_t)n, nc = (size_t)6 * nbody + (size_t)nbeta;
+  size_t b = 0;
+  // mesh: node and panel arrays, 288-byte panel records, field points
+  b += nn * (4 * sizeof(int) + 12 * sizeof(double) + 36 * sizeof(double)) + (nn + nl) * 3 * sizeof(double);
+  // right-hand sides, solutions, source weights, split-K workspace
+  b += sizeof(double2) * (tn * nc + nn * nc + nn * (nbeta > 0 ? nbeta : 1) + 16 * tn * nc);
+  b += hg::rhs_work_bytes(n, (int)tn, nbody, nbeta);
+  if (precision == HG_PREC_MIXED) {
+    b += sizeof(float2) * (tn * nn * (irsp == 1 ? 2 : 3) + (irsp == 1 ? nn * nn : 0) + nn * nc);
+    b += sizeof(double2) * (tn * nc + nn * nc);
+    b += hg::resid_work_bytes((int)tn, (int)nc, (int)tn);
+    b += hg::lu_work_bytes(n, lu_tensor);
+  } else {
+    b += sizeof(double2) * (2 * tn * nn + (irsp == 1 ? nn * nn + nn * nc : 0));
+  }
+  return b;
+}
+
 int hg_gmres_iterations(const hg_ctx* c, int* iterations) {
   if (!c) return -1;
   if (iterations) *iterations = c->inner_its;

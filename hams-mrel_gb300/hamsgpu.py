@@ -24,7 +24,8 @@ EXPORTS = [
     "hg_solve_frequency", "hg_keep_matrices", "hg_get_matrix", "hg_green_points", "hg_refine_info",
     "hg_stage_times", "hg_dispersion", "hg_wave_properties", "hg_panel_geometry", "hg_mark", "hg_elapsed",
     "hg_bench_gemm", "hg_green_points_noalloc", "hg_gesv", "hg_gemm_check",
-    "hg_solve_sweep", "hg_gmres_iterations",
+    "hg_solve_sweep", "hg_gmres_iterations", "hg_solve_footprint", "hg_server_create", "hg_server_submit",
+    "hg_server_wait", "hg_server_stats", "hg_server_last_error", "hg_server_destroy",
 ]
 
 
@@ -32,6 +33,16 @@ class HgOpts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("precision", ctypes.c_int), ("grn_kind", ctypes.c_int),
                 ("max_refine", ctypes.c_int), ("refine_tol", ctypes.c_double), ("rho", ctypes.c_double),
                 ("g", ctypes.c_double), ("lu_tensor", ctypes.c_int), ("refine_method", ctypes.c_int)]
+
+
+class HgRequest(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int), ("ntnd", ctypes.c_int), ("nodes", ctypes.c_void_p), ("ncon", ctypes.c_void_p),
+                ("ncn", ctypes.c_void_p), ("xyz_p", ctypes.c_void_p), ("ds", ctypes.c_void_p),
+                ("pnsz", ctypes.c_void_p), ("dxyz_p", ctypes.c_void_p), ("nl", ctypes.c_int),
+                ("lid_xyz_p", ctypes.c_void_p), ("nbody", ctypes.c_int), ("body_ranges", ctypes.c_void_p),
+                ("h", ctypes.c_double), ("nfreq", ctypes.c_int), ("v", ctypes.c_void_p), ("wk", ctypes.c_void_p),
+                ("w1", ctypes.c_void_p), ("wvn", ctypes.c_void_p), ("nk", ctypes.c_int), ("irsp", ctypes.c_int),
+                ("isol", ctypes.c_int), ("nbeta", ctypes.c_int), ("betas", ctypes.c_void_p)]
 
 
 _LIB = None
@@ -87,6 +98,16 @@ def load(build_if_missing: bool = True):
     L.hg_solve_sweep.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_int, c_int,
                                  c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
                                  c_void_p]
+    L.hg_solve_footprint.argtypes = [c_int, c_int, c_int, c_int, c_int, c_int, c_int]
+    L.hg_solve_footprint.restype = ctypes.c_size_t
+    L.hg_server_create.argtypes = [P(c_void_p), P(HgOpts), c_int, c_double]
+    L.hg_server_submit.argtypes = [c_void_p, P(HgRequest), P(ctypes.c_longlong)]
+    L.hg_server_wait.argtypes = [c_void_p, ctypes.c_longlong, c_double, c_void_p, c_void_p, c_void_p, c_void_p]
+    L.hg_server_stats.argtypes = [c_void_p, c_void_p]
+    L.hg_server_last_error.argtypes = [c_void_p]
+    L.hg_server_last_error.restype = ctypes.c_char_p
+    L.hg_server_destroy.argtypes = [c_void_p]
+    L.hg_server_destroy.restype = None
     L.hg_bench_gemm.argtypes = [c_void_p, c_int, c_int, c_int, c_int, c_int, P(ctypes.c_float)]
     L.hg_gemm_check.argtypes = [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_void_p,
                                 c_int]
@@ -351,3 +372,88 @@ class Solver:
         a = (ctypes.c_float * 4)()
         self.L.hg_stage_times(self.h, a)
         return list(a)
+
+
+def solve_footprint(precision, n, nl, nbody, nbeta, irsp=0, lu_tensor=3):
+    """Device bytes one frequency-solve of this size holds (hg_solve_footprint)."""
+    return int(load().hg_solve_footprint(precision, n, nl, nbody, nbeta, irsp, lu_tensor))
+
+
+class Server:
+    """Request server: continuous batching of frequency-solve requests (hg_server_*)."""
+
+    def __init__(self, nslots=4, budget_bytes=150e9, precision=HG_PREC_MIXED, device=0, **opts_kw):
+        self.L = load()
+        opts = HgOpts()
+        self.L.hg_default_opts(ctypes.byref(opts))
+        opts.device, opts.precision = device, precision
+        for k, v in opts_kw.items():
+            setattr(opts, k, v)
+        h = ctypes.c_void_p()
+        rc = self.L.hg_server_create(ctypes.byref(h), ctypes.byref(opts), nslots, float(budget_bytes))
+        if rc != 0:
+            raise HamsGpuError(rc, "hg_server_create failed")
+        self.h = h
+        self._pending = {}
+
+    def submit(self, mesh, h, v, wk, w1, wvn, betas, irsp=0, isol=1):
+        """Queue one request (mesh as meshgen.Mesh; per-frequency wave state). Returns a ticket."""
+        f = lambda a, t=np.float64: np.asfortranarray(a, dtype=t)  # noqa: E731
+        keep = [f(mesh.nodes), f(mesh.ncon, np.int32), np.ascontiguousarray(mesh.ncn, dtype=np.int32), f(mesh.xyz_p),
+                np.ascontiguousarray(mesh.ds, dtype=np.float64), np.ascontiguousarray(mesh.pnsz, dtype=np.float64),
+                f(mesh.dxyz_p)]
+        lid = mesh.lid_xyz_p if irsp == 1 else None
+        lid = None if lid is None or len(lid) == 0 else f(lid)
+        br = np.ascontiguousarray(np.asarray(mesh.body_ranges, dtype=np.int32).reshape(-1))
+        vv = np.ascontiguousarray(v, dtype=np.float64)
+        kk = np.ascontiguousarray(wk, dtype=np.float64)
+        ww = np.ascontiguousarray(w1, dtype=np.float64)
+        b = np.ascontiguousarray(betas, dtype=np.float64)
+        wv = None
+        nk = 0
+        if h > 0 and wvn is not None:
+            wv = np.ascontiguousarray(wvn, dtype=np.float64).reshape(len(vv), -1)
+            nk = wv.shape[1]
+        q = HgRequest(len(keep[2]), len(keep[0]), _ptr(keep[0]), _ptr(keep[1]), _ptr(keep[2]), _ptr(keep[3]),
+                      _ptr(keep[4]), _ptr(keep[5]), _ptr(keep[6]), 0 if lid is None else len(lid), _ptr(lid),
+                      len(br) // 2, _ptr(br), float(h), len(vv), _ptr(vv), _ptr(kk), _ptr(ww), _ptr(wv), nk, irsp,
+                      isol, len(b), _ptr(b))
+        t = ctypes.c_longlong()
+        rc = self.L.hg_server_submit(self.h, ctypes.byref(q), ctypes.byref(t))
+        if rc != 0:
+            raise HamsGpuError(rc, self.L.hg_server_last_error(self.h).decode())
+        self._pending[t.value] = (len(vv), len(br) // 2, len(b))
+        return t.value
+
+    def wait(self, ticket, timeout_s=0.0):
+        """(amas[nfreq, nd, nd], bdmp, exfc[nfreq, nbeta, nd], latency_ms, admit_wait_ms), or None on timeout."""
+        nf, nbody, nb = self._pending[ticket]
+        nd = 6 * nbody
+        amas = np.zeros((nf, nd, nd)); bdmp = np.zeros((nf, nd, nd))
+        exfc = np.zeros((nf, nd, max(nb, 1)), dtype=np.complex128)
+        lat = np.zeros(2)
+        rc = self.L.hg_server_wait(self.h, ticket, float(timeout_s), _ptr(amas), _ptr(bdmp), _ptr(exfc), _ptr(lat))
+        if rc == 1:
+            return None
+        del self._pending[ticket]
+        if rc != 0:
+            raise HamsGpuError(rc, self.L.hg_server_last_error(self.h).decode())
+        return (amas.transpose(0, 2, 1), bdmp.transpose(0, 2, 1), exfc.transpose(0, 2, 1)[:, :nb, :], lat[0], lat[1])
+
+    def stats(self):
+        st = np.zeros(8)
+        self.L.hg_server_stats(self.h, _ptr(st))
+        keys = ["requests_done", "solves_done", "reserved_bytes", "peak_reserved_bytes", "max_admitted",
+                "queued", "admitted", "budget_bytes"]
+        return dict(zip(keys, st.tolist()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.hg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -20,6 +20,8 @@
 #ifndef HAMSGPU_H
 #define HAMSGPU_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -159,6 +161,62 @@ int hg_solve_frequency(hg_ctx *ctx, double v, double wk, double w1, double h, co
 int hg_solve_sweep(hg_ctx *ctx, int nfreq, const double *v, const double *wk, const double *w1, double h,
                    const double *wvn, int nk, int irsp, const double *betas, int nbeta, int isol, int nslots,
                    double *amas, double *bdmp, double *exfc, double *mxpot, int ldm, float *latency_ms);
+
+/*
+ * Device bytes one frequency-solve of this size holds in a context (matrices,
+ * factor workspace, right-hand sides, refinement buffers, mesh): what the
+ * serving loop below reserves per solve in flight.  0 for invalid sizes.
+ */
+size_t hg_solve_footprint(int precision, int n, int nl, int nbody, int nbeta, int irsp, int lu_tensor);
+
+/*
+ * Serving: continuous batching of frequency-solve requests (the serving form
+ * of this path; the reference runs one request per process, HAMS_Prog).  A
+ * request is a mesh (as hg_set_mesh), a depth, nfreq frequencies (wave state
+ * per frequency as hg_set_frequency; wvn nk x nfreq for finite depth) and
+ * nbeta headings.  hg_server_submit copies the request and returns at once;
+ * nslots solve slots (contexts with their own stream and host thread) run
+ * the frequencies of all admitted requests as slots free up, so requests
+ * that arrive while others run join the mix and their solves overlap on the
+ * device.  Admission: requests are admitted in arrival order while the
+ * reserved device memory, min(nslots, nfreq) x hg_solve_footprint + mesh per
+ * admitted request, stays within budget_bytes; a request larger than the
+ * budget is rejected by hg_server_submit (-3).  Each result equals that of
+ * hg_solve_frequency on a single context (same kernels, same order).
+ *   hg_server_wait: blocks (timeout_s <= 0) or waits up to timeout_s seconds
+ *     (returns 1 if the request is not finished); copies amas, bdmp
+ *     ((6nb)^2 x nfreq), exfc (nbeta x 6nb COMPLEX*16 x nfreq) and
+ *     latency_ms[2] = (submit to done, submit to admission); a ticket can be
+ *     collected once.  A failed request returns its first error.
+ *   hg_server_stats: stats[8] = requests done, frequency-solves done,
+ *     reserved bytes, peak reserved bytes, most requests admitted at once,
+ *     queued requests, admitted requests, budget.
+ * hg_server_destroy stops the slots (unfinished requests are dropped).
+ */
+typedef struct hg_server hg_server;
+typedef struct {
+    int n, ntnd;
+    const double *nodes;
+    const int *ncon, *ncn;
+    const double *xyz_p, *ds, *pnsz, *dxyz_p;
+    int nl;
+    const double *lid_xyz_p;
+    int nbody;
+    const int *body_ranges;
+    double h;
+    int nfreq;
+    const double *v, *wk, *w1, *wvn;
+    int nk, irsp, isol, nbeta;
+    const double *betas;
+} hg_request;
+
+int hg_server_create(hg_server **srv, const hg_opts *opts, int nslots, double budget_bytes);
+int hg_server_submit(hg_server *srv, const hg_request *req, long long *ticket);
+int hg_server_wait(hg_server *srv, long long ticket, double timeout_s, double *amas, double *bdmp, double *exfc,
+                   double *latency_ms);
+int hg_server_stats(hg_server *srv, double *stats);
+const char *hg_server_last_error(const hg_server *srv);
+void hg_server_destroy(hg_server *srv);
 
 /* Diagnostics for tests: copy the tn x n influence matrix (which = 0, before
  * factorisation) or single-layer matrix (which = 1) of the last fill to host
