@@ -311,6 +311,77 @@ def ours(args, dist, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
+def _request_inputs(hg, freqs, h):
+    vals = [hg.wave_properties(3, float(w), h) for w in freqs]
+    v = np.array([x[0] for x in vals]); wk = np.array([x[1] for x in vals]); w1 = np.array([x[2] for x in vals])
+    wvn = np.stack([x[3] for x in vals]) if h > 0 else None
+    return v, wk, w1, wvn
+
+
+def served(args):
+    """Batching and serving forms through the request server (hg_server_*).
+
+    batch: `requests` independent single-frequency solves (1-4 cylinders,
+      N log-uniform 300-4000, deep water with p = 0.5 else h ~ U(30, 200) m,
+      1-4 headings), all submitted at once.
+    serve: `requests` requests (1-6 bodies, N log-uniform 500-12000, 20-100
+      frequencies, 1-8 headings) arriving as a Poisson stream whose rate is
+      set from a calibration run of the same stream submitted at once (0.8 of
+      the measured request throughput, i.e. about 80 % device utilisation).
+    """
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    hg, mg = pkg.hamsgpu, pkg.meshgen
+    rng = np.random.default_rng(4 if args.workload == "batch" else 5)
+    reqs = []
+    for _ in range(args.requests):
+        if args.workload == "batch":
+            mesh, h, w, heads = mg.batch_case(rng)
+            freqs = np.array([w])
+        else:
+            mesh, h, freqs, heads = mg.serving_case(rng)
+        v, wk, w1, wvn = _request_inputs(hg, freqs, h)
+        reqs.append((mesh, h, v, wk, w1, wvn, np.array(heads) * math.pi / 180.0))
+    nsolves = sum(len(r[2]) for r in reqs)
+
+    def run(arrivals):
+        srv = hg.Server(nslots=args.slots, budget_bytes=150e9)
+        t0 = time.perf_counter()
+        tickets = []
+        for r, ta in zip(reqs, arrivals):
+            dt = ta - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            tickets.append(srv.submit(*r))
+        lat = []
+        for t in tickets:
+            lat.append(srv.wait(t)[3])
+        total = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        return total, sorted(lat), st
+
+    with ClockSampler(0) as clk:
+        total, lat, st = run([0.0] * len(reqs))
+        rate = None
+        if args.workload == "serve":
+            rate = 0.8 * len(reqs) / total  # requests per second at ~80 % of the measured capacity
+            gaps = rng.exponential(1.0 / rate, size=len(reqs))
+            total, lat, st = run(np.cumsum(gaps) - gaps[0])
+    p = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))]  # noqa: E731
+    line = {"metric": "freq-solves/s (%s form, mixed precision); p50/p99 request latency" % args.workload,
+            "value": nsolves / total, "unit": "freq-solves/s", "n_gpus": 1, "steps": nsolves, "warmup": 0,
+            "ms_per_step": 1e3 * total / nsolves, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "complex64+fp64-refine", "data": "synthetic",
+            "config": {"workload": args.workload, "requests": len(reqs), "freq_solves": nsolves,
+                       "panels_min_max": [min(r[0].n for r in reqs), max(r[0].n for r in reqs)],
+                       "slots": args.slots, "hbm_budget_bytes": 150e9,
+                       "arrival_rate_per_s": rate, "timing": "host wall clock, submission to last result"},
+            "latency_ms": {"p50": p(0.5), "p99": p(0.99)},
+            "server": st, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def _launch_count(n, prec, sweeps=1, nd=30, nbeta=8):
     """Kernels the library launches per frequency-solve, from its launch
     sequence (checked against the ncu launch list of one solve)."""
@@ -377,11 +448,21 @@ def main():
                     help="mixed-form refinement: classical iterative refinement or GMRES-IR")
     ap.add_argument("--lu-tensor", type=int, default=3, choices=[0, 1, 3],
                     help="LU trailing updates: 3 split-TF32 tensor cores, 1 TF32, 0 FP32 SIMT")
+    ap.add_argument("--workload", default="array", choices=["array", "batch", "serve"],
+                    help="array: the 6048-panel frequency sweep (headline); batch / serve: the request server")
+    ap.add_argument("--requests", type=int, default=None, help="batch / serve: number of requests")
     args = ap.parse_args()
     if args.impl == "reference":
         rank = int(os.environ.get("RANK", "0"))
         world = int(os.environ.get("WORLD_SIZE", "1"))
         cpu_reference(args.steps, args.warmup, rank, world)
+        return
+    if args.workload != "array":
+        if args.requests is None:
+            args.requests = 512 if args.workload == "batch" else 24
+        if args.slots == 4:
+            args.slots = 8
+        served(args)
         return
     dist, rank, world, local = _dist()
     try:

@@ -63,6 +63,7 @@ struct hg_ctx {
   std::vector<int> bstart, bend;
   DevBuf<double> nodes, xyz_p, ds, pnsz, dxyz, rec, fx, betas;
   DevBuf<int> ncon, ncn, body_of, body_start, body_end, ipiv, status, info;
+  DevBuf<int> bins;                      // finite depth: pairs binned by the cost of their Green function
   // frequency
   double v = 0, wk = 0, w1 = 0, h = -1, nm0 = 0;
   int nk = 0;
@@ -671,8 +672,13 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
   if (!mixed(c)) {
     CK(c->A.ensure((size_t)tn * n));
     CK(c->S.ensure((size_t)tn * n));
+    int* bins = nullptr;  // pair indices are ints: the binned fill needs tn * n < 2^31
+    if (!deep && (long long)tn * n < 2147483647LL) {
+      CK(c->bins.ensure(hg::fin_bins_ints(n, tn)));
+      bins = c->bins.p;
+    }
     CK(hg::launch_green_fill<double2>(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, deep, c->o.grn_kind, c->A.p, c->S.p, tn,
-                                      c->status.p));
+                                      c->status.p, bins));
     if (c->keep && irsp == 0) {
       CK(c->A64.ensure((size_t)tn * n));
       CK(cudaMemcpyAsync(c->A64.p, c->A.p, (size_t)tn * n * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
@@ -690,7 +696,12 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
     CK(c->Af.ensure((size_t)tn * n));
     CK(c->Sf.ensure((size_t)tn * n));
     const bool special = std::fabs(c->v) < (double)1.e-8f || std::fabs(c->v + 1.0) < (double)1.e-8f;
-    if (deep && !special && c->o.grn_kind == 8)
+    if (!deep) {
+      const bool binned = (long long)tn * n < 2147483647LL;
+      if (binned) CK(c->bins.ensure(hg::fin_bins_ints(n, tn)));
+      CK(hg::launch_green_fill_fin_fma(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, c->o.grn_kind, c->Af.p, c->Sf.p, tn,
+                                       c->status.p, binned ? c->bins.p : nullptr));
+    } else if (!special && c->o.grn_kind == 8)
       CK(hg::launch_green_fill_mixed(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, c->v, c->ox, c->oy, c->Af.p, c->Sf.p, tn,
                                      c->status.p));
     else
@@ -990,6 +1001,8 @@ size_t hg_solve_footprint(int precision, int n, int nl, int nbody, int nbeta, in
   size_t b = 0;
   // mesh: node and panel arrays, 288-byte panel records, field points
   b += nn * (4 * sizeof(int) + 12 * sizeof(double) + 36 * sizeof(double)) + (nn + nl) * 3 * sizeof(double);
+  // finite depth: one int per pair for the cost-binned fill
+  b += sizeof(int) * tn * nn;
   // right-hand sides, solutions, source weights, split-K workspace
   b += sizeof(double2) * (tn * nc + nn * nc + nn * (nbeta > 0 ? nbeta : 1) + 16 * tn * nc);
   b += hg::rhs_work_bytes(n, (int)tn, nbody, nbeta);

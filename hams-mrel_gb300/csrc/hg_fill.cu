@@ -104,25 +104,22 @@ __global__ void k_prep_panels(int n, int ntnd, const double* __restrict__ nodes 
 
 // ---------------------------------------------------------------------------
 // Deep-water pair kernel instantiations (the finite-depth ones live in
-// hg_fill_fin.cu, compiled without FMA contraction).
+// hg_fill_fin.cu, compiled without FMA contraction, and, for the mixed form,
+// hg_fill_fin_fma.cu).
 // ---------------------------------------------------------------------------
 template <typename OUT>
 cudaError_t launch_green_fill(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
-                              const FinState& fs, bool deep, int grn_kind, OUT* A, OUT* S, long lda, int* status) {
-  if (!deep) return launch_green_fill_fin<OUT>(st, rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, status);
+                              const FinState& fs, bool deep, int grn_kind, OUT* A, OUT* S, long lda, int* status,
+                              int* bins) {
+  if (!deep) return launch_green_fill_fin<OUT>(st, rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, status, bins);
   dim3 grid((tn + FILL_ROWS - 1) / FILL_ROWS, (n + FILL_COLS - 1) / FILL_COLS);
   k_green_fill<true, OUT><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, status);
   return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
-// Mixed form, deep water: the pair kernel in single precision.
-//   - FLAG (dist <= 50 PNSZ) is decided in double exactly as in the plain
-//     kernel, so both forms integrate the same pairs analytically;
-//   - pairs closer than 4 PNSZ (self and adjacent panels) keep the
-//     double-precision Newman integral;
-//   - coordinate differences are formed in double, everything else (Green
-//     function, far Newman integrals, assembly) in single precision.
+// Mixed form, deep water: the pair kernel in single precision (the kernel
+// k_green_fill_mixed below says which parts stay in double).
 // ---------------------------------------------------------------------------
 // Monomial coefficients in rho of the Wu-Noblesse local-flow polynomials
 // A, B, C, D (InfGreen_Appr.f90:298-416) and A', B', C' (:494-580).
@@ -290,9 +287,9 @@ cudaError_t launch_green_fill_mixed(cudaStream_t st, const double* rec, const do
   return cudaGetLastError();
 }
 template cudaError_t launch_green_fill<double2>(cudaStream_t, const double*, const double*, int, int, int,
-                                                const FinState&, bool, int, double2*, double2*, long, int*);
+                                                const FinState&, bool, int, double2*, double2*, long, int*, int*);
 template cudaError_t launch_green_fill<float2>(cudaStream_t, const double*, const double*, int, int, int,
-                                               const FinState&, bool, int, float2*, float2*, long, int*);
+                                               const FinState&, bool, int, float2*, float2*, long, int*, int*);
 
 cudaError_t launch_prep_panels(cudaStream_t st, int n, int ntnd, const double* nodes, const int* ncon, const int* ncn,
                                const double* xyz_p, const double* ds, const double* pnsz, const double* dxyz_p,

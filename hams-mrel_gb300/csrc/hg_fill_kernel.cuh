@@ -17,7 +17,46 @@ namespace hg {
 constexpr int FILL_ROWS = 128;
 constexpr int FILL_COLS = 16;
 
+// One (field i, source j) pair of the fill: FLAG, Newman integral, Green
+// function, assembly of A(i, j) and S(i, j) (the loop body of k_green_fill).
 template <bool DEEP, typename OUT>
+__device__ __forceinline__ void fill_pair(const double* __restrict__ pr, double xp, double yp, double zp, int i, int j,
+                                          const FinState& fs, int grn_kind, OUT* __restrict__ A,
+                                          OUT* __restrict__ S, long lda) {
+  const double xq = pr[PR_XQ], yq = pr[PR_XQ + 1], zq = pr[PR_XQ + 2];
+  const double dist = sqrt((xp - xq) * (xp - xq) + (yp - yq) * (yp - yq) + (zp - zq) * (zp - zq));
+  const int flag = (dist <= pr[PR_FLAGD]) ? 1 : 0;
+  double sij = 0.0, d0 = 0.0, d1 = 0.0, d2 = 0.0;
+  if (flag) newman_pair(pr, xp, yp, zp, sij, d0, d1, d2);
+  double2 g[4];
+  if (DEEP) inf_green(xq, yq, zq, xp, yp, zp, fs.v, flag, g);
+  else fin_green(fs, xq, yq, zq, xp, yp, zp, flag, g);
+  if (grn_kind == 4) {
+    sij = (float)sij; d0 = (float)d0; d1 = (float)d1; d2 = (float)d2;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) g[k] = make_double2((float)g[k].x, (float)g[k].y);
+  }
+  const double ear = pr[PR_DS], n0 = pr[PR_N], n1 = pr[PR_N + 1], n2 = pr[PR_N + 2];
+  double ar, ai, sr, si;
+  if (flag) {
+    ar = (d0 + g[1].x * ear) * n0 + (d1 + g[2].x * ear) * n1 + (d2 + g[3].x * ear) * n2;
+    ai = (g[1].y * ear) * n0 + (g[2].y * ear) * n1 + (g[3].y * ear) * n2;
+    sr = sij + g[0].x * ear;
+  } else {
+    ar = (g[1].x * n0 + g[2].x * n1 + g[3].x * n2) * ear;
+    ai = (g[1].y * n0 + g[2].y * n1 + g[3].y * n2) * ear;
+    sr = g[0].x * ear;
+  }
+  si = g[0].y * ear;
+  if (i == j) ar += 2.0 * HG_PI;
+  store_c(A + i + (long)j * lda, ar, ai);
+  store_c(S + i + (long)j * lda, sr, si);
+}
+
+// FAST distinguishes the instantiation compiled with fused multiply-adds
+// (the mixed form's finite-depth fill) from the one compiled without; the
+// code is the same.
+template <bool DEEP, typename OUT, int FAST = 0>
 __global__ void __launch_bounds__(FILL_ROWS)
 k_green_fill(const double* __restrict__ rec, const double* __restrict__ fx /* ldf x 3 col-major */, int ldf, int n, int tn,
              FinState fs, int grn_kind, OUT* __restrict__ A, OUT* __restrict__ S, long lda, int* status) {
@@ -39,38 +78,118 @@ k_green_fill(const double* __restrict__ rec, const double* __restrict__ fx /* ld
   const int i = blockIdx.x * FILL_ROWS + threadIdx.x;
   if (i >= tn) return;
   const double xp = fx[i], yp = fx[i + ldf], zp = fx[i + 2 * (size_t)ldf];
-  for (int jj = 0; jj < ncol; ++jj) {
-    const double* pr = tile + jj * PR_SIZE;
-    const int j = col0 + jj;
-    const double xq = pr[PR_XQ], yq = pr[PR_XQ + 1], zq = pr[PR_XQ + 2];
-    const double dist = sqrt((xp - xq) * (xp - xq) + (yp - yq) * (yp - yq) + (zp - zq) * (zp - zq));
-    const int flag = (dist <= pr[PR_FLAGD]) ? 1 : 0;
-    double sij = 0.0, d0 = 0.0, d1 = 0.0, d2 = 0.0;
-    if (flag) newman_pair(pr, xp, yp, zp, sij, d0, d1, d2);
-    double2 g[4];
-    if (DEEP) inf_green(xq, yq, zq, xp, yp, zp, fs.v, flag, g);
-    else fin_green(fs, xq, yq, zq, xp, yp, zp, flag, g);
-    if (grn_kind == 4) {
-      sij = (float)sij; d0 = (float)d0; d1 = (float)d1; d2 = (float)d2;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) g[k] = make_double2((float)g[k].x, (float)g[k].y);
-    }
-    const double ear = pr[PR_DS], n0 = pr[PR_N], n1 = pr[PR_N + 1], n2 = pr[PR_N + 2];
-    double ar, ai, sr, si;
-    if (flag) {
-      ar = (d0 + g[1].x * ear) * n0 + (d1 + g[2].x * ear) * n1 + (d2 + g[3].x * ear) * n2;
-      ai = (g[1].y * ear) * n0 + (g[2].y * ear) * n1 + (g[3].y * ear) * n2;
-      sr = sij + g[0].x * ear;
-    } else {
-      ar = (g[1].x * n0 + g[2].x * n1 + g[3].x * n2) * ear;
-      ai = (g[1].y * n0 + g[2].y * n1 + g[3].y * n2) * ear;
-      sr = g[0].x * ear;
-    }
-    si = g[0].y * ear;
-    if (i == j) ar += 2.0 * HG_PI;
-    store_c(A + i + (long)j * lda, ar, ai);
-    store_c(S + i + (long)j * lda, sr, si);
+  for (int jj = 0; jj < ncol; ++jj)
+    fill_pair<DEEP, OUT>(tile + jj * PR_SIZE, xp, yp, zp, i, col0 + jj, fs, grn_kind, A, S, lda);
+}
+
+// ---------------------------------------------------------------------------
+// Finite depth, pairs binned by cost.  FINGREEN3D (FinGreen3D.f90:81-155)
+// branches per pair on R/h into methods whose costs differ by orders of
+// magnitude (LINTON's adaptive quadrature, PIDCOCK's and EIGENE's 10-100-term
+// series with Wynn extrapolation, EIGEN's <= 10 terms).  In the tiled kernel
+// one expensive pair holds up the 31 other threads of its warp; here the
+// pairs are first sorted into kFinBins bins by method and series length
+// (counting pass, scan, scatter pass), and the evaluation kernel then walks
+// the bins in order, one pair per thread, so that a warp's pairs cost about
+// the same.  Each result goes to its own (i, j), so the order inside a bin
+// (set by atomics) does not affect the matrices.
+// ---------------------------------------------------------------------------
+constexpr int kFinBins = 16;
+
+__device__ __forceinline__ int fin_bin(const FinState& fs, double rr) {
+  const double v = fs.v;
+  if (fabs(v) < SPD(1.e-8) || fabs(v + 1.0) < SPD(1.e-8)) return kFinBins - 1;  // closed forms
+  const double rhp = fabs(rr / fs.h);
+  if (rhp < 0.0005) return 0;                                                    // LINTON
+  if (rhp < 0.05) {                                                              // PIDCOCK, 50-100 terms
+    const int nt = (int)(SPD(-1010.10) * rhp + SPD(100.50));
+    return 1 + min(6, max(0, (100 - nt) / 8));
   }
+  if (rhp < 0.5) {                                                               // EIGENE, 10-50 terms
+    const int nt = (int)(SPD(-88.89) * rhp + SPD(54.45));
+    return 8 + min(5, max(0, (54 - nt) / 8));
+  }
+  return 14;                                                                     // EIGEN
+}
+
+// Pass 1 (scatter = false): bin counts; pass 2 (scatter = true): pair index
+// i + j * tn appended to its bin at cursor[bin] (warp-aggregated atomics).
+template <bool SCATTER>
+__global__ void k_fin_bins(const double* __restrict__ rec, const double* __restrict__ fx, int ldf, int n, int tn,
+                           FinState fs, int* __restrict__ counts, int* __restrict__ list) {
+  __shared__ int hist[kFinBins];
+  if (!SCATTER && threadIdx.x < kFinBins) hist[threadIdx.x] = 0;
+  if (!SCATTER) __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  const bool ok = i < tn;
+  int b = 0;
+  if (ok) {
+    const double* pr = rec + (size_t)j * PR_SIZE;
+    const double dx = pr[PR_XQ] - fx[i], dy = pr[PR_XQ + 1] - fx[i + ldf];
+    b = fin_bin(fs, sqrt(dx * dx + dy * dy));
+  }
+  const unsigned act = __ballot_sync(0xffffffffu, ok);
+  if (ok) {
+    const unsigned peers = __match_any_sync(act, b);
+    const int leader = __ffs(peers) - 1, lane = threadIdx.x & 31;
+    const int rank = __popc(peers & ((1u << lane) - 1u));
+    if (!SCATTER) {
+      if (lane == leader) atomicAdd(&hist[b], __popc(peers));
+    } else {
+      int base = 0;
+      if (lane == leader) base = atomicAdd(&counts[b], __popc(peers));
+      base = __shfl_sync(peers, base, leader);
+      list[base + rank] = i + j * tn;
+    }
+  }
+  if (!SCATTER) {
+    __syncthreads();
+    if (threadIdx.x < kFinBins && hist[threadIdx.x]) atomicAdd(&counts[threadIdx.x], hist[threadIdx.x]);
+  }
+}
+
+// counts -> cursors (exclusive prefix sums), one thread.
+static __global__ void k_fin_scan(int* __restrict__ counts) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    int acc = 0;
+    for (int b = 0; b < kFinBins; ++b) {
+      const int c = counts[b];
+      counts[b] = acc;
+      acc += c;
+    }
+  }
+}
+
+template <typename OUT, int FAST>
+__global__ void __launch_bounds__(128)
+k_green_fill_binned(const double* __restrict__ rec, const double* __restrict__ fx, int ldf, int tn, long npairs,
+                    const int* __restrict__ list, FinState fs, int grn_kind, OUT* __restrict__ A,
+                    OUT* __restrict__ S, long lda) {
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < npairs; k += (long)gridDim.x * blockDim.x) {
+    const int p = list[k];
+    const int i = p % tn, j = p / tn;
+    fill_pair<false, OUT>(rec + (size_t)j * PR_SIZE, fx[i], fx[i + ldf], fx[i + 2 * (size_t)ldf], i, j, fs, grn_kind,
+                          A, S, lda);
+  }
+}
+
+template <typename OUT, int FAST>
+cudaError_t launch_fin_binned(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
+                              const FinState& fs, int grn_kind, OUT* A, OUT* S, long lda, int* bins) {
+  int* counts = bins;
+  int* list = bins + kFinBins;
+  cudaError_t e = cudaMemsetAsync(counts, 0, kFinBins * sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  const dim3 cg((tn + 127) / 128, n);
+  k_fin_bins<false><<<cg, 128, 0, st>>>(rec, fx, ldf, n, tn, fs, counts, list);
+  k_fin_scan<<<1, 32, 0, st>>>(counts);
+  k_fin_bins<true><<<cg, 128, 0, st>>>(rec, fx, ldf, n, tn, fs, counts, list);
+  const long np = (long)tn * n;
+  long blocks = (np + 127) / 128;
+  if (blocks > 152L * 64) blocks = 152L * 64;
+  k_green_fill_binned<OUT, FAST><<<(unsigned)blocks, 128, 0, st>>>(rec, fx, ldf, tn, np, list, fs, grn_kind, A, S, lda);
+  return cudaGetLastError();
 }
 
 // Green function at arbitrary points (kernel-level parity tests of every

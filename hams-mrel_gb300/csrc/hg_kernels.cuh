@@ -16,11 +16,19 @@ cudaError_t launch_prep_panels(cudaStream_t st, int n, int ntnd, const double* n
 
 template <typename OUT>
 cudaError_t launch_green_fill(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
-                              const FinState& fs, bool deep, int grn_kind, OUT* A, OUT* S, long lda, int* status);
+                              const FinState& fs, bool deep, int grn_kind, OUT* A, OUT* S, long lda, int* status,
+                              int* bins = nullptr);
 
 template <typename OUT>
 cudaError_t launch_green_fill_fin(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
-                                  const FinState& fs, int grn_kind, OUT* A, OUT* S, long lda, int* status);
+                                  const FinState& fs, int grn_kind, OUT* A, OUT* S, long lda, int* status,
+                                  int* bins);
+// Finite depth, complex64 output, compiled with FMA contraction (mixed form).
+cudaError_t launch_green_fill_fin_fma(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
+                                      const FinState& fs, int grn_kind, float2* A, float2* S, long lda, int* status,
+                                      int* bins);
+// Scratch ints of the cost-binned finite-depth fill: bin cursors + one pair index per pair.
+inline size_t fin_bins_ints(int n, int tn) { return 16 + (size_t)n * tn; }
 cudaError_t launch_green_points_fin(cudaStream_t st, int npts, const double* pts, const int* flags, const FinState& fs,
                                     double* out);
 

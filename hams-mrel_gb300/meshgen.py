@@ -290,3 +290,57 @@ def scaled_array(n_target, seed=0) -> Mesh:
         x, y = 30.0 * (k % 4) + rng.uniform(-3, 3), 30.0 * (k // 4) + rng.uniform(-3, 3)
         bodies.append(cylinder(4.0, 8.0, 48, 22, 8, cx=x, cy=y))
     return combine(bodies)
+
+
+def _cylinder_for(n_target, radius, draft, n_az, cx, cy):
+    """Cylinder with about n_target panels at n_az azimuthal divisions."""
+    rows = max(2, round(n_target / n_az))
+    n_ring = max(1, round(rows * radius / (radius + draft)))
+    n_vert = max(1, rows - n_ring)
+    return cylinder(radius, draft, n_az, n_vert, n_ring, cx=cx, cy=cy)
+
+
+def _box_for(n_target, lx, ly, draft, cx, cy):
+    """Box with about n_target panels of equal size."""
+    area = 2.0 * lx * draft + 2.0 * ly * draft + lx * ly
+    return box(lx, ly, draft, math.sqrt(area / max(n_target, 6)), cx=cx, cy=cy)
+
+
+def batch_case(rng) -> tuple:
+    """One solve of the batching workload: 1-4 cylinders (R ~ U(2, 8) m,
+    T ~ U(2, 10) m, azimuthal count ~ U{16..48}) sized so that the panel count
+    is log-uniform on 300-4000; returns (mesh, depth, w, headings_deg)."""
+    n_target = math.exp(rng.uniform(math.log(300.0), math.log(4000.0)))
+    nb = int(rng.integers(1, 5))
+    bodies = []
+    for k in range(nb):
+        r, t = rng.uniform(2.0, 8.0), rng.uniform(2.0, 10.0)
+        n_az = int(rng.integers(16, 49))
+        bodies.append(_cylinder_for(n_target / nb, r, t, n_az, 25.0 * k, 0.0))
+    h = -1.0 if rng.uniform() < 0.5 else float(rng.uniform(30.0, 200.0))
+    w = float(rng.uniform(0.1, 3.0))
+    heads = list(np.linspace(0.0, 90.0, int(rng.integers(1, 5))))
+    return combine(bodies), h, w, heads
+
+
+def serving_case(rng) -> tuple:
+    """One request of the serving workload: 1-6 bodies (cylinders and boxes) on
+    a 30 m grid, panel count log-uniform on 500-12000, depth infinite or
+    U(30, 200) m, 20-100 frequencies in 0.1-3.0 rad/s and 1-8 headings;
+    returns (mesh, depth, frequencies, headings_deg)."""
+    n_target = math.exp(rng.uniform(math.log(500.0), math.log(12000.0)))
+    nb = int(rng.integers(1, 7))
+    bodies = []
+    for k in range(nb):
+        x, y = 30.0 * (k % 3) + rng.uniform(-3, 3), 30.0 * (k // 3) + rng.uniform(-3, 3)
+        if rng.uniform() < 0.6:
+            bodies.append(_cylinder_for(n_target / nb, rng.uniform(2.0, 8.0), rng.uniform(2.0, 10.0),
+                                        int(rng.integers(16, 49)), x, y))
+        else:
+            bodies.append(_box_for(n_target / nb, rng.uniform(6.0, 14.0), rng.uniform(4.0, 8.0),
+                                   rng.uniform(2.0, 6.0), x, y))
+    h = -1.0 if rng.uniform() < 0.5 else float(rng.uniform(30.0, 200.0))
+    nf = int(rng.integers(20, 101))
+    freqs = np.linspace(0.1, 3.0, nf)
+    heads = list(np.linspace(0.0, 315.0, int(rng.integers(1, 9))))
+    return combine(bodies), h, freqs, heads

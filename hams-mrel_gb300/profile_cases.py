@@ -14,6 +14,8 @@ repository root, e.g.
                              triangular solves, refinement residuals
   step [PREC]                one frequency-solve of the 6048-panel 5-body
                              benchmark array (fill, LU, solves, forces)
+  fill N H PREC              one Green fill + LU of a cylinder array of about N
+                             panels at depth H metres (H <= 0: deep water)
 """
 from __future__ import annotations
 
@@ -66,6 +68,21 @@ def case_step(prec=1):
     s.close()
 
 
+def case_fill(n, h, prec):
+    import meshgen
+    mesh = meshgen.scaled_array(n)
+    s = hamsgpu.Solver(precision=prec)
+    s.set_mesh(mesh.nodes, mesh.ncon, mesh.ncn, mesh.xyz_p, mesh.ds, mesh.pnsz, mesh.dxyz_p, mesh.body_ranges)
+    hh = float(h) if h > 0 else -1.0
+    v, wk, w1, wvn = hamsgpu.wave_properties(3, 1.0, hh)
+    s.set_frequency(v, wk, w1, hh, wvn)
+    s.fill_factor(0)
+    t = s.stage_times()
+    print(f"fill n={len(mesh.ncn)} h={hh} prec={prec}: fill {t[0]:.2f} ms ({len(mesh.ncn) ** 2 / t[0] / 1e3:.3f} "
+          f"Mpairs/s), lu {t[1]:.2f} ms")
+    s.close()
+
+
 def main(argv):
     if not argv:
         print(__doc__)
@@ -77,6 +94,8 @@ def main(argv):
         case_gesv(*args)
     elif cmd == "step":
         case_step(*args)
+    elif cmd == "fill":
+        case_fill(*args)
     else:
         print(__doc__)
         return 2

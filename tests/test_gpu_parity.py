@@ -277,3 +277,16 @@ def test_mixed_solve_irr_within_tolerance(pkg, oracle, example5):
     assert max_norm_err(amas, ref.amas) < MIXED_TOL
     assert max_norm_err(bdmp, ref.bdmp) < MIXED_TOL
     assert max_norm_err(exfc, ref.exfc) < MIXED_TOL
+
+
+def test_mixed_solve_finite_depth_within_tolerance(pkg, oracle, config1):
+    """Finite depth in the mixed form (the FMA-contracted FP64 Green function, complex64 LU)."""
+    s = gpu_solver(pkg, config1, precision=1)
+    w = config1.ctl.wvnb[2]
+    amas, bdmp, exfc, mx = gpu_frequency(pkg, s, config1, w)
+    ref = _oracle_solve(oracle, config1, w)
+    s.close()
+    assert max_norm_err(amas, ref.amas) < MIXED_TOL
+    assert max_norm_err(bdmp, ref.bdmp) < MIXED_TOL
+    assert max_norm_err(exfc, ref.exfc) < MIXED_TOL
+
