@@ -178,9 +178,10 @@ static cudaError_t upload_cheb_constants() {
 }
 
 // Single-precision pair loop of the mixed form.  Per pair only FP32
-// arithmetic, except (a) the pairs within 4 panel sizes (0.08 of the
-// 50-panel-size FLAG radius), whose Newman integrals stay in FP64 with FP64
-// coordinates, and (b) the rare pairs whose FP32 squared distance lies within
+// arithmetic, except (a) the self and adjacent pairs, within 2 panel sizes
+// (0.04 of the 50-panel-size FLAG radius), whose Newman integrals stay in
+// FP64 with FP64 coordinates, and (b) the rare pairs whose FP32 squared
+// distance lies within
 // 1e-3 of the FLAG radius, where FLAG is decided again in FP64 exactly as
 // CALGREEN does (dist <= 50 PNSZ).  Horizontal coordinates enter FP32
 // relative to the mesh centre (ox, oy) so that their rounding is that of the
@@ -251,7 +252,7 @@ k_green_fill_mixed(const double* __restrict__ rec, const double* __restrict__ fx
     }
     float sij = 0.f, d0 = 0.f, d1 = 0.f, d2 = 0.f;
     if (flag) {
-      if (d2f <= 0.0064f * fl2) {
+      if (d2f <= 0.0016f * fl2) {
         double s64, e0, e1, e2;
         newman_pair(tile + jj * PR_SIZE, xp, yp, zp, s64, e0, e1, e2);
         sij = (float)s64; d0 = (float)e0; d1 = (float)e1; d2 = (float)e2;
