@@ -405,8 +405,9 @@ def _launch_count(n, prec, sweeps=1, nd=30, nbeta=8):
     # mixed: RHS (incident, source columns, S W as a split product: 3 kernels);
     # 1 + sweeps solves, each followed by a residual check (product, split,
     # reduce) and bracketed by conversions; column norms of B and of each residual
+    # (later sweeps update the residual with the correction: one more conversion each)
     s1 = 1 + sweeps
-    return fill + lu + 5 + s1 * getrs + 3 * s1 + (1 + s1) + 2 * s1 + forces
+    return fill + lu + 5 + s1 * getrs + 3 * s1 + (1 + s1) + 2 * s1 + sweeps + forces
 
 
 def _roofline(s, n, prec, hg):

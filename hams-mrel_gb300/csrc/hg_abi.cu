@@ -409,14 +409,27 @@ int solve_cols(hg_ctx* c, int c0, int c1) {
     c->resid = worst;
     return 0;
   }
+  // After the first sweep (irsp = 0) the residual is updated instead of
+  // recomputed: r_(k+1) = r_k - A d_k for the complex64 correction d_k.
+  // |d_k| is ~1e-5 |x|, so the product needs only single-precision relative
+  // accuracy (the compensated single-product mode, ~1e-7 of sum |a||d|) to
+  // keep r FP64-accurate (~1e-12 |b|), at a fifth of the cost of the exact
+  // double-float product that the first residual b - A x0 needs.
+  const bool incremental = c->irsp == 0;
+  if (incremental) CK(c->gW.ensure((size_t)n * nc));
   for (;;) {
     // r = b - M x in FP64 (M = A, or A^T A applied as A^T (B - A x))
     if (c->irsp == 1) {
       double2* R1 = c->R.p + (size_t)c0 * tn;
       CK(hg::resid_df(c->st, false, tn, nc, n, A0, tn, Xc, n, Bc, tn, -1.0, R1, tn, rws, rws_bytes));
       CK(hg::resid_df(c->st, true, n, nc, tn, A0, tn, R1, tn, nullptr, 0, 1.0, Rh, n, rws, rws_bytes));
-    } else {
+    } else if (sweep == 0) {
       CK(hg::resid_df(c->st, false, n, nc, n, A0, tn, Xc, n, Bc, tn, -1.0, Rh, n, rws, rws_bytes));
+    } else {
+      double2* D = c->R.p;  // tn x nc >= n x nc, unused for irsp = 0
+      CK(hg::convert_c2z_2d(c->st, n, nc, Bf, n, D, n));
+      CK(hg::resid_df(c->st, false, n, nc, n, A0, tn, D, n, Rh, n, -1.0, c->gW.p, n, rws, rws_bytes, false));
+      CK(cudaMemcpyAsync(Rh, c->gW.p, (size_t)n * nc * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
     }
     k_colmax<<<nc, 256, 0, c->st>>>(n, Rh, n, nb.p + nc);
     CK(cudaMemcpyAsync(rnorm.data(), nb.p + nc, nc * sizeof(double), cudaMemcpyDeviceToHost, c->st));
