@@ -21,6 +21,7 @@
 #include "hg_green.cuh"
 #include "hg_kernels.cuh"
 #include "hg_linalg.cuh"
+#include "hg_fintab.cuh"
 
 using hg::FinState;
 
@@ -59,11 +60,13 @@ struct hg_ctx {
   // mesh
   int n = 0, nl = 0, tn = 0, tnf = 0, ntnd = 0, nbody = 0;  // tn: rows of the current solve, tnf: n + nl
   double ox = 0, oy = 0;  // horizontal centre of the hull centroids (origin of the FP32 pair coordinates)
+  double rmax = 0;        // largest horizontal distance between centroids (hull and lid)
   bool mesh_set = false;
   std::vector<int> bstart, bend;
   DevBuf<double> nodes, xyz_p, ds, pnsz, dxyz, rec, fx, betas;
   DevBuf<int> ncon, ncn, body_of, body_start, body_end, ipiv, status, info;
   DevBuf<int> bins;                      // finite depth: pairs binned by the cost of their Green function
+  DevBuf<float> tab;                     // finite depth, mixed form: tabulated Green function
   // frequency
   double v = 0, wk = 0, w1 = 0, h = -1, nm0 = 0;
   int nk = 0;
@@ -488,6 +491,7 @@ void hg_default_opts(hg_opts* o) {
   o->max_refine = 10;
   o->refine_tol = 1e-10;
   o->refine_method = 0;
+  o->fin_table = -1;
   o->rho = 1000.0;
   o->g = 9.80665;
   o->lu_tensor = 3;
@@ -504,6 +508,7 @@ int hg_create(hg_ctx** out, const hg_opts* opts) {
   if (c->o.grn_kind != 4 && c->o.grn_kind != 8) { delete c; return -2; }
   if (c->o.lu_tensor != 0 && c->o.lu_tensor != 1 && c->o.lu_tensor != 3) { delete c; return -2; }
   if (c->o.refine_method != 0 && c->o.refine_method != 1) { delete c; return -2; }
+  if (c->o.fin_table < -1 || c->o.fin_table > 1) { delete c; return -2; }
   cudaError_t e = cudaSetDevice(c->o.device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
   for (int k = 0; k < 5 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
@@ -630,10 +635,19 @@ int hg_set_mesh(hg_ctx* c, int n, int ntnd, const double* nodes, const int* ncon
   else c->h_lid.clear();
   c->h_ranges.assign(body_ranges, body_ranges + 2 * nbody);
   {
-    double sx = 0, sy = 0;
-    for (int e = 0; e < n; ++e) { sx += xyz_p[e]; sy += xyz_p[e + (size_t)n]; }
+    double sx = 0, sy = 0, x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300;
+    for (int e = 0; e < n; ++e) {
+      const double x = xyz_p[e], y = xyz_p[e + (size_t)n];
+      sx += x; sy += y;
+      x0 = std::min(x0, x); x1 = std::max(x1, x); y0 = std::min(y0, y); y1 = std::max(y1, y);
+    }
+    for (int e = 0; e < nl; ++e) {
+      const double x = lid_xyz_p[e], y = lid_xyz_p[e + (size_t)nl];
+      x0 = std::min(x0, x); x1 = std::max(x1, x); y0 = std::min(y0, y); y1 = std::max(y1, y);
+    }
     c->ox = sx / n;
     c->oy = sy / n;
+    c->rmax = std::sqrt((x1 - x0) * (x1 - x0) + (y1 - y0) * (y1 - y0));
   }
   c->slots_mesh = false;
   c->mesh_set = true;
@@ -709,7 +723,15 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
     CK(c->Af.ensure((size_t)tn * n));
     CK(c->Sf.ensure((size_t)tn * n));
     const bool special = std::fabs(c->v) < (double)1.e-8f || std::fabs(c->v + 1.0) < (double)1.e-8f;
-    if (!deep) {
+    const bool table = !deep && !special && c->o.grn_kind == 8 &&
+                       (c->o.fin_table == 1 || (c->o.fin_table < 0 && (long long)tn * n >= 4000000LL));
+    if (table) {
+      CK(c->tab.ensure(hg::fintab_floats()));
+      hg::FinTab tab;
+      CK(hg::fintab_build(c->st, fs, 1.02 * c->rmax + 1.0, c->tab.p, &tab));
+      CK(hg::launch_green_fill_mixed_fin(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, tab, c->ox, c->oy, c->Af.p,
+                                         c->Sf.p, tn, c->status.p));
+    } else if (!deep) {
       const bool binned = (long long)tn * n < 2147483647LL;
       if (binned) CK(c->bins.ensure(hg::fin_bins_ints(n, tn)));
       CK(hg::launch_green_fill_fin_fma(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, c->o.grn_kind, c->Af.p, c->Sf.p, tn,

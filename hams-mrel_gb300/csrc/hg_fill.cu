@@ -15,6 +15,7 @@
 #include "hg_tma.cuh"
 #include "hg_fill_kernel.cuh"
 #include "hg_green32.cuh"
+#include "hg_fintab.cuh"
 #include <cmath>
 
 namespace hg {
@@ -186,10 +187,14 @@ static cudaError_t upload_cheb_constants() {
 // CALGREEN does (dist <= 50 PNSZ).  Horizontal coordinates enter FP32
 // relative to the mesh centre (ox, oy) so that their rounding is that of the
 // array's size, not of its position; depths stay absolute (the image
-// distance zp + zq needs them).
+// distance zp + zq needs them).  FIN: finite depth, the Green function from
+// the tables of hg_fintab.cuh plus FINGREEN3D's Rankine pair (FinGreen3D.f90
+// :120-150) in FP32; otherwise deep water (inf_green_f).
+template <bool FIN>
 __global__ void __launch_bounds__(FILL_ROWS)
 k_green_fill_mixed(const double* __restrict__ rec, const double* __restrict__ fx, int ldf, int n, int tn, float vf,
-                   double ox, double oy, float2* __restrict__ A, float2* __restrict__ S, long lda, int* status) {
+                   double ox, double oy, FinTab tab, FinState fs, float2* __restrict__ A, float2* __restrict__ S,
+                   long lda, int* status) {
   __shared__ alignas(128) double tile[FILL_COLS * PR_SIZE];
   __shared__ alignas(8) uint64_t bar;
   __shared__ PanelF pfs[FILL_COLS];
@@ -261,7 +266,42 @@ k_green_fill_mixed(const double* __restrict__ rec, const double* __restrict__ fx
       }
     }
     float2 g[4];
-    inf_green_f(dxf, dyf, zpf + zqf, dzf, vf, flag, g);
+    if (!FIN) {
+      inf_green_f(dxf, dyf, zpf + zqf, dzf, vf, flag, g);
+    } else {
+      const float rr = sqrtf(dxf * dxf + dyf * dyf);
+      float f[6];
+      if (d2f > 1e-10f) {
+        fintab_eval(tab, rr, zqf, zpf, f);
+      } else {
+        // coincident centroids (the diagonal): LINTON drops its direct term at
+        // r < 1e-6 (FinGreen3D.f90, Linton's image sums) instead of taking the
+        // limit, so these pairs take the reference's FP64 value, not the tables'
+        const double* pr = tile + jj * PR_SIZE;
+        const double dx = pr[PR_XQ] - xp, dy = pr[PR_XQ + 1] - yp;
+        double fd[6];
+        fin_regions(fs, sqrt(dx * dx + dy * dy), pr[PR_XQ + 2], zp, fd);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) f[q] = (float)fd[q];
+      }
+      g[0] = make_float2(f[0], f[1]);
+      g[3] = make_float2(f[4], f[5]);
+      if (rr > 1e-6f) {
+        const float cx = dxf / rr, cy = dyf / rr;
+        g[1] = make_float2(f[2] * cx, f[3] * cx);
+        g[2] = make_float2(f[2] * cy, f[3] * cy);
+      } else {
+        g[1] = make_float2(0.f, 0.f);
+        g[2] = g[1];
+      }
+      const float zs = zqf + zpf;
+      const float ir1 = rsqrtf(rr * rr + zs * zs), ir13 = ir1 * ir1 * ir1;
+      g[0].x += ir1; g[1].x -= dxf * ir13; g[2].x -= dyf * ir13; g[3].x -= zs * ir13;
+      if (flag == 0) {
+        const float ir = rsqrtf(d2f), ir3 = ir * ir * ir;
+        g[0].x += ir; g[1].x -= dxf * ir3; g[2].x -= dyf * ir3; g[3].x += dzf * ir3;  // (zq - zp) = -dzf
+      }
+    }
     const float ear = pds[jj][0], n0 = pds[jj][1], n1 = pds[jj][2], n2 = pds[jj][3];
     float ar, ai, sr;
     if (flag) {
@@ -284,7 +324,19 @@ cudaError_t launch_green_fill_mixed(cudaStream_t st, const double* rec, const do
   cudaError_t e = upload_cheb_constants();
   if (e != cudaSuccess) return e;
   dim3 grid((tn + FILL_ROWS - 1) / FILL_ROWS, (n + FILL_COLS - 1) / FILL_COLS);
-  k_green_fill_mixed<<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, (float)v, ox, oy, A, S, lda, status);
+  FinTab none = {};
+  FinState nfs = {};
+  k_green_fill_mixed<false><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, (float)v, ox, oy, none, nfs, A, S, lda,
+                                                         status);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_green_fill_mixed_fin(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
+                                        const FinState& fs, const FinTab& tab, double ox, double oy, float2* A,
+                                        float2* S, long lda, int* status) {
+  dim3 grid((tn + FILL_ROWS - 1) / FILL_ROWS, (n + FILL_COLS - 1) / FILL_COLS);
+  k_green_fill_mixed<true><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, (float)fs.v, ox, oy, tab, fs, A, S,
+                                                        lda, status);
   return cudaGetLastError();
 }
 template cudaError_t launch_green_fill<double2>(cudaStream_t, const double*, const double*, int, int, int,

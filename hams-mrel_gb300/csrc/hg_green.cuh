@@ -833,6 +833,22 @@ HGD inline void d_linton(const FinState& st, double r, double zf, double zp, dou
   g[4] = -p4 * re2; g[5] = -p4 * im2;
 }
 
+// FINGREEN3D_R dispatch (FinGreen3D.f90:160-226): the Green function minus
+// its Rankine pair 1/r + 1/r1 and its derivatives, f = [G, dG/dR, dG/dzq]
+// as (re, im) pairs, at horizontal distance rr, source depth zq, field depth zp.
+// method: -1 by R/h as the reference; 0 LINTON, 1 PIDCOCK, 2 EIGENE, 3 EIGEN.
+HGD inline void fin_regions(const FinState& st, double rr, double zq, double zp, double f[6], int method = -1) {
+  if (method < 0) {
+    const double rhp = fabs(rr / st.h);
+    method = (rhp < 0.0005) ? 0 : (rhp < 0.05) ? 1 : (rhp < 0.5) ? 2 : 3;
+  }
+  if (method == 0) d_linton(st, rr, zq, zp, f);
+  else if (method == 1) d_series_eps(st, rr, zq, zp, f, true);
+  else if (method == 2) d_series_eps(st, rr, zq, zp, f, false);
+  else d_eigen(st, rr, zq, zp, f);
+  if (rr == 0.0) { f[2] = 0.0; f[3] = 0.0; }
+}
+
 // FINGREEN3D (FinGreen3D.f90:81-155) for source (xq,yq,zq) and field (xp,yp,zp).
 HGD inline void fin_green(const FinState& st, double xq, double yq, double zq, double xp,
                                  double yp, double zp, int flag, double2 g[4]) {
@@ -850,12 +866,7 @@ HGD inline void fin_green(const FinState& st, double xq, double yq, double zq, d
   }
   if (!(fabs(v) < SPD(1.e-8))) {
     double f[6];
-    const double rhp = fabs(rr / st.h);
-    if (rhp < 0.0005) d_linton(st, rr, zq, zp, f);
-    else if (rhp < 0.05) d_series_eps(st, rr, zq, zp, f, true);
-    else if (rhp < 0.5) d_series_eps(st, rr, zq, zp, f, false);
-    else d_eigen(st, rr, zq, zp, f);
-    if (rr == 0.0) { f[2] = 0.0; f[3] = 0.0; }
+    fin_regions(st, rr, zq, zp, f);
     if (rr > SPD(1.e-6)) {
       const double cx = xpq / rr, cy = ypq / rr;
       g[1] = make_double2(f[2] * cx, f[3] * cx);

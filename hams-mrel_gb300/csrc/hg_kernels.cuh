@@ -27,6 +27,15 @@ cudaError_t launch_green_fill_fin(cudaStream_t st, const double* rec, const doub
 cudaError_t launch_green_fill_fin_fma(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
                                       const FinState& fs, int grn_kind, float2* A, float2* S, long lda, int* status,
                                       int* bins);
+// Tabulated finite-depth Green function of the mixed form (hg_fintab.cu):
+// fintab_floats() floats of device scratch; rmax = largest horizontal
+// distance between a field point and a source.
+struct FinTab;
+size_t fintab_floats();
+cudaError_t fintab_build(cudaStream_t st, const FinState& fs, double rmax, float* buf, FinTab* out);
+cudaError_t launch_green_fill_mixed_fin(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
+                                        const FinState& fs, const FinTab& tab, double ox, double oy, float2* A,
+                                        float2* S, long lda, int* status);
 // Scratch ints of the cost-binned finite-depth fill: bin cursors + one pair index per pair.
 inline size_t fin_bins_ints(int n, int tn) { return 16 + (size_t)n * tn; }
 cudaError_t launch_green_points_fin(cudaStream_t st, int npts, const double* pts, const int* flags, const FinState& fs,

@@ -32,7 +32,8 @@ EXPORTS = [
 class HgOpts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("precision", ctypes.c_int), ("grn_kind", ctypes.c_int),
                 ("max_refine", ctypes.c_int), ("refine_tol", ctypes.c_double), ("rho", ctypes.c_double),
-                ("g", ctypes.c_double), ("lu_tensor", ctypes.c_int), ("refine_method", ctypes.c_int)]
+                ("g", ctypes.c_double), ("lu_tensor", ctypes.c_int), ("refine_method", ctypes.c_int),
+                ("fin_table", ctypes.c_int)]
 
 
 class HgRequest(ctypes.Structure):
@@ -168,7 +169,7 @@ class Solver:
 
     def __init__(self, precision: int = HG_PREC_FP64, device: int = 0, grn_kind: int = 8,
                  max_refine: int = 10, refine_tol: float = 1e-10, rho: float = 1000.0, g: float = 9.80665,
-                 lu_tensor: int = 3, refine_method: int = 0):
+                 lu_tensor: int = 3, refine_method: int = 0, fin_table: int = -1):
         self.L = load()
         opts = HgOpts()
         self.L.hg_default_opts(ctypes.byref(opts))
@@ -176,6 +177,7 @@ class Solver:
         opts.max_refine, opts.refine_tol, opts.rho, opts.g = max_refine, refine_tol, rho, g
         opts.lu_tensor = lu_tensor
         opts.refine_method = refine_method
+        opts.fin_table = fin_table
         h = ctypes.c_void_p()
         rc = self.L.hg_create(ctypes.byref(h), ctypes.byref(opts))
         if rc != 0:
