@@ -724,13 +724,13 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
     CK(c->Sf.ensure((size_t)tn * n));
     const bool special = std::fabs(c->v) < (double)1.e-8f || std::fabs(c->v + 1.0) < (double)1.e-8f;
     const bool table = !deep && !special && c->o.grn_kind == 8 &&
-                       (c->o.fin_table == 1 || (c->o.fin_table < 0 && (long long)tn * n >= 4000000LL));
+                       (c->o.fin_table == 1 || (c->o.fin_table < 0 && (long long)tn * n >= 1000000LL));
     if (table) {
-      CK(c->tab.ensure(hg::fintab_floats()));
+      CK(c->tab.ensure(hg::fintab_floats() + (size_t)6 * n));
       hg::FinTab tab;
       CK(hg::fintab_build(c->st, fs, 1.02 * c->rmax + 1.0, c->tab.p, &tab));
-      CK(hg::launch_green_fill_mixed_fin(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, tab, c->ox, c->oy, c->Af.p,
-                                         c->Sf.p, tn, c->status.p));
+      CK(hg::launch_green_fill_mixed_fin(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, tab, c->ox, c->oy,
+                                         c->tab.p + hg::fintab_floats(), c->Af.p, c->Sf.p, tn, c->status.p));
     } else if (!deep) {
       const bool binned = (long long)tn * n < 2147483647LL;
       if (binned) CK(c->bins.ensure(hg::fin_bins_ints(n, tn)));

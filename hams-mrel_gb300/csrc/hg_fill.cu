@@ -193,8 +193,8 @@ static cudaError_t upload_cheb_constants() {
 template <bool FIN>
 __global__ void __launch_bounds__(FILL_ROWS)
 k_green_fill_mixed(const double* __restrict__ rec, const double* __restrict__ fx, int ldf, int n, int tn, float vf,
-                   double ox, double oy, FinTab tab, FinState fs, float2* __restrict__ A, float2* __restrict__ S,
-                   long lda, int* status) {
+                   double ox, double oy, FinTab tab, const float* __restrict__ diag, float2* __restrict__ A,
+                   float2* __restrict__ S, long lda, int* status) {
   __shared__ alignas(128) double tile[FILL_COLS * PR_SIZE];
   __shared__ alignas(8) uint64_t bar;
   __shared__ PanelF pfs[FILL_COLS];
@@ -276,13 +276,10 @@ k_green_fill_mixed(const double* __restrict__ rec, const double* __restrict__ fx
       } else {
         // coincident centroids (the diagonal): LINTON drops its direct term at
         // r < 1e-6 (FinGreen3D.f90, Linton's image sums) instead of taking the
-        // limit, so these pairs take the reference's FP64 value, not the tables'
-        const double* pr = tile + jj * PR_SIZE;
-        const double dx = pr[PR_XQ] - xp, dy = pr[PR_XQ + 1] - yp;
-        double fd[6];
-        fin_regions(fs, sqrt(dx * dx + dy * dy), pr[PR_XQ + 2], zp, fd);
+        // limit, so these pairs take the reference's FP64 value at
+        // (R = 0, zq = zp), computed beforehand per source panel (k_fin_diag)
 #pragma unroll
-        for (int q = 0; q < 6; ++q) f[q] = (float)fd[q];
+        for (int q = 0; q < 6; ++q) f[q] = diag[6 * j + q];
       }
       g[0] = make_float2(f[0], f[1]);
       g[3] = make_float2(f[4], f[5]);
@@ -325,17 +322,27 @@ cudaError_t launch_green_fill_mixed(cudaStream_t st, const double* rec, const do
   if (e != cudaSuccess) return e;
   dim3 grid((tn + FILL_ROWS - 1) / FILL_ROWS, (n + FILL_COLS - 1) / FILL_COLS);
   FinTab none = {};
-  FinState nfs = {};
-  k_green_fill_mixed<false><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, (float)v, ox, oy, none, nfs, A, S, lda,
-                                                         status);
+  k_green_fill_mixed<false><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, (float)v, ox, oy, none, nullptr, A, S,
+                                                         lda, status);
   return cudaGetLastError();
 }
 
+// F at R = 0, zq = zp = z_j for every source panel j (the coincident pairs).
+__global__ void k_fin_diag(int n, const double* __restrict__ rec, FinState fs, float* __restrict__ diag) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const double z = rec[(size_t)j * PR_SIZE + PR_XQ + 2];
+  double f[6];
+  fin_regions(fs, 0.0, z, z, f);
+  for (int q = 0; q < 6; ++q) diag[6 * j + q] = (float)f[q];
+}
+
 cudaError_t launch_green_fill_mixed_fin(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
-                                        const FinState& fs, const FinTab& tab, double ox, double oy, float2* A,
-                                        float2* S, long lda, int* status) {
+                                        const FinState& fs, const FinTab& tab, double ox, double oy, float* diag,
+                                        float2* A, float2* S, long lda, int* status) {
+  k_fin_diag<<<(n + 31) / 32, 32, 0, st>>>(n, rec, fs, diag);
   dim3 grid((tn + FILL_ROWS - 1) / FILL_ROWS, (n + FILL_COLS - 1) / FILL_COLS);
-  k_green_fill_mixed<true><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, (float)fs.v, ox, oy, tab, fs, A, S,
+  k_green_fill_mixed<true><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, (float)fs.v, ox, oy, tab, diag, A, S,
                                                         lda, status);
   return cudaGetLastError();
 }

@@ -167,7 +167,7 @@ __device__ __forceinline__ void fintab_eval(const FinTab& T, float R, float zq, 
 
 // Grid sizes: R nodes per segment (LINTON, PIDCOCK, EIGENE, EIGEN), W and U
 // nodes; the build costs (sum of R nodes) x (W + 2 U) evaluations.
-constexpr int kFinSegN[kFinSegs] = {4, 96, 100, 64};
-constexpr int kFinTabR = 4 + 96 + 100 + 64, kFinTabW = 240, kFinTabU = 300;
+constexpr int kFinSegN[kFinSegs] = {2, 64, 72, 64};
+constexpr int kFinTabR = 2 + 64 + 72 + 64, kFinTabW = 160, kFinTabU = 200;
 
 }  // namespace hg

@@ -33,9 +33,10 @@ cudaError_t launch_green_fill_fin_fma(cudaStream_t st, const double* rec, const 
 struct FinTab;
 size_t fintab_floats();
 cudaError_t fintab_build(cudaStream_t st, const FinState& fs, double rmax, float* buf, FinTab* out);
+// diag: device scratch of 6 n floats (the coincident pairs' FP64 values).
 cudaError_t launch_green_fill_mixed_fin(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
-                                        const FinState& fs, const FinTab& tab, double ox, double oy, float2* A,
-                                        float2* S, long lda, int* status);
+                                        const FinState& fs, const FinTab& tab, double ox, double oy, float* diag,
+                                        float2* A, float2* S, long lda, int* status);
 // Scratch ints of the cost-binned finite-depth fill: bin cursors + one pair index per pair.
 inline size_t fin_bins_ints(int n, int tn) { return 16 + (size_t)n * tn; }
 cudaError_t launch_green_points_fin(cudaStream_t st, int npts, const double* pts, const int* flags, const FinState& fs,

@@ -60,7 +60,7 @@ typedef struct {
                             and (R, zq+zp), bicubic interpolation in FP32; ~50x faster than FP64
                             per pair from a few thousand panels; A, B, F within 1e-5..6e-4 of the
                             FP64 form, the worst where PIDCOCK's near-surface values are noisy):
-                            1 on, 0 off (FP64 per pair), -1 automatic (on from 4e6 pairs; default) */
+                            1 on, 0 off (FP64 per pair), -1 automatic (on from 1e6 pairs; default) */
 } hg_opts;
 
 /* Fill opts with the defaults above (device 0, FP64, GRN_KIND 8, rho 1000, g 9.80665, lu_tensor 3). */
