@@ -382,6 +382,62 @@ def served(args):
     print(json.dumps(line), flush=True)
 
 
+def three_bodies(args):
+    """The plain FP64 form on three cylinders in line (R 3 m, T 6 m, 15 m apart,
+    32 x 12 + 32 x 4 panels each, 32 x 4 lid panels each: 1536 + 384), depth
+    40 m, irregular-frequency removal (IRSP = 1), headings 0/45/90 deg, 18
+    modes, frequencies from 0.2-3.0 rad/s; beside it the CPU oracle on one
+    frequency and the difference between the two on that frequency."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    hg, mg = pkg.hamsgpu, pkg.meshgen
+    mesh = mg.three_cylinders(with_lid=True)
+    h = 40.0
+    freqs = np.linspace(0.2, 3.0, 80)
+    betas_deg = [0.0, 45.0, 90.0]
+    betas = np.array(betas_deg) * math.pi / 180.0
+    prec = hg.HG_PREC_FP64 if args.precision == "fp64" else hg.HG_PREC_MIXED
+    sel = [freqs[(7 * k) % 80] for k in range(args.warmup + args.steps)]
+    v, wk, w1, wvn = _request_inputs(hg, sel, h)
+    s = hg.Solver(precision=prec)
+    s.set_mesh(mesh.nodes, mesh.ncon, mesh.ncn, mesh.xyz_p, mesh.ds, mesh.pnsz, mesh.dxyz_p, mesh.body_ranges,
+               mesh.lid_xyz_p)
+    W = args.warmup
+    s.solve_sweep(v[:W], wk[:W], w1[:W], h, wvn[:W], betas, irsp=1, nslots=args.slots)
+    with ClockSampler(0) as clk:
+        s.mark(0)
+        am, bm, fm, lat, _ = s.solve_sweep(v[W:], wk[W:], w1[W:], h, wvn[W:], betas, irsp=1, nslots=args.slots)
+        s.mark(1)
+        ms = s.elapsed_ms(0, 1)
+    s.close()
+    # the CPU oracle on the first timed frequency, all host cores
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle
+    from helpers import case_from_mesh, max_norm_err
+    case = case_from_mesh(oracle, mesh, h=h, headings_deg=betas_deg, irsp=1)
+    t0 = time.perf_counter()
+    ref = oracle.solve_frequency(case, sel[W], nthreads=os.cpu_count())
+    tcpu = time.perf_counter() - t0
+    lat = sorted(float(x) for x in lat)
+    form = "plain FP64" if prec == hg.HG_PREC_FP64 else "mixed"
+    line = {"metric": f"freq-solves/s ({form} form, 3 cylinders in line, finite depth, IRSP=1)",
+            "value": args.steps / (ms / 1e3), "unit": "freq-solves/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": W, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "complex128" if prec == hg.HG_PREC_FP64 else "complex64+fp64-refine",
+            "data": "synthetic",
+            "config": {"workload": "3 cylinders R 3 m T 6 m, 1536 hull + 384 lid panels, h 40 m, 3 headings, 18 modes",
+                       "slots": args.slots},
+            "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[-1]},
+            "vs_oracle_max_norm_err": {"A": max_norm_err(am[0], ref.amas), "B": max_norm_err(bm[0], ref.bdmp),
+                                       "F": max_norm_err(fm[0], ref.exfc)},
+            "cpu_baseline": {"value": 1.0 / tcpu, "unit": "freq-solves/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": "1 frequency-solve of this workload (C oracle, OpenMP over field rows, "
+                                       "OpenBLAS LU)"},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def _launch_count(n, prec, sweeps=1, nd=30, nbeta=8):
     """Kernels the library launches per frequency-solve, from its launch
     sequence (checked against the ncu launch list of one solve)."""
@@ -453,7 +509,7 @@ def main():
                     help="mixed-form refinement: classical iterative refinement or GMRES-IR")
     ap.add_argument("--lu-tensor", type=int, default=3, choices=[0, 1, 3],
                     help="LU trailing updates: 3 split-TF32 tensor cores, 1 TF32, 0 FP32 SIMT")
-    ap.add_argument("--workload", default="array", choices=["array", "batch", "serve"],
+    ap.add_argument("--workload", default="array", choices=["array", "batch", "serve", "three"],
                     help="array: the 6048-panel frequency sweep (headline); batch / serve: the request server")
     ap.add_argument("--requests", type=int, default=None, help="batch / serve: number of requests")
     args = ap.parse_args()
@@ -461,6 +517,9 @@ def main():
         rank = int(os.environ.get("RANK", "0"))
         world = int(os.environ.get("WORLD_SIZE", "1"))
         cpu_reference(args.steps, args.warmup, rank, world)
+        return
+    if args.workload == "three":
+        three_bodies(args)
         return
     if args.workload != "array":
         if args.requests is None:
