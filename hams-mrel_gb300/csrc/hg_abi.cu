@@ -149,8 +149,6 @@ FinState fin_state(const hg_ctx* c) {
 
 bool mixed(const hg_ctx* c) { return c->o.precision == HG_PREC_MIXED; }
 
-int ncols_total(const hg_ctx* c) { return 6 * c->nbody + c->nbeta; }
-
 // Ensure the B/X/R buffers hold 6*nbody + nbeta columns.
 int ensure_rhs(hg_ctx* c, int nbeta) {
   const int nc = 6 * c->nbody + nbeta;
