@@ -81,6 +81,10 @@ struct hg_ctx {
   DevBuf<double> nrm;                    // column norms of the refinement (2 x columns)
   DevBuf<double2> gV, gZ, gW, gH, gY;    // GMRES refinement: Krylov basis, preconditioned basis, work, Hessenberg, y
   DevBuf<double> gN;
+  // field points (hg_field_points): coordinates, on-body flags, DUM2 / DUM1 rows, weights, potentials
+  DevBuf<double> fpx;
+  DevBuf<int> fonb;
+  DevBuf<double2> fA, fS, fW, fout;
   int inner_its = 0;                     // GMRES iterations of the last solve
   int irsp = 0;
   bool factored = false;
@@ -853,6 +857,56 @@ int hg_forces(hg_ctx* c, int isol, double* amas, double* bdmp, double* exfc) {
         exfc[2 * (k + (size_t)d * nbeta) + 1] = f[(size_t)k * nd + d].y;
       }
   return 0;
+}
+
+int hg_field_points(hg_ctx* c, int npts, const double* xyz, int kind, int isol, double* out, int ldo) {
+  if (!c) return -1;
+  if (npts < 0) return fail(c, -2, "npts must be >= 0");
+  if (npts > 0 && !xyz) return fail(c, -3, "xyz is NULL");
+  if (kind < 0 || kind > 2) return fail(c, -4, "kind must be 0 (potential), 1 (pressure) or 2 (elevation)");
+  if (isol != 1 && isol != 2) return fail(c, -5, "isol must be 1 or 2");
+  if (npts > 0 && !out) return fail(c, -6, "out is NULL");
+  if (ldo < npts) return fail(c, -7, "ldo %d < npts %d", ldo, npts);
+  if (!c->rad_done) return fail(c, HG_ERR_STATE, "a radiation solve (hg_solve_frequency or hg_solve_radiation) must come first");
+  if (npts == 0) return 0;
+  cudaSetDevice(c->o.device);
+  const int n = c->n, nrad = 6 * c->nbody, nbeta = c->dif_done ? c->nbeta : 0, ncol = nrad + nbeta;
+  const bool deep = c->h < 0.0;
+  const FinState fs = fin_state(c);
+  // Field points in chunks of up to 2048 rows: two chunk x n complex128
+  // matrices (DUM2 and DUM1) at a time.
+  const int chunk = std::min(npts, 2048);
+  CK(c->fpx.ensure((size_t)chunk * 3));
+  CK(c->fonb.ensure(chunk));
+  CK(c->fA.ensure((size_t)chunk * n));
+  CK(c->fS.ensure((size_t)chunk * n));
+  CK(c->fW.ensure((size_t)n * ncol));
+  CK(c->fout.ensure((size_t)chunk * ncol));
+  const bool binned = !deep && (long long)chunk * n < 2147483647LL;
+  if (binned) CK(c->bins.ensure(hg::fin_bins_ints(n, chunk)));
+  // source weights [radiation modes | -grad phi_I . n of the solved headings]
+  CK(hg::launch_rhs_cols(c->st, n, c->dxyz.p, c->body_of.p, c->nbody, nbeta, c->W.p, c->fW.p, n));
+  std::vector<double> hx((size_t)chunk * 3);
+  const double2 one = make_double2(1, 0), mone = make_double2(-1, 0), zero = make_double2(0, 0);
+  for (int p0 = 0; p0 < npts; p0 += chunk) {
+    const int m = std::min(chunk, npts - p0);
+    for (int p = 0; p < m; ++p)
+      for (int k = 0; k < 3; ++k) hx[p + (size_t)k * m] = xyz[3 * (size_t)(p0 + p) + k];
+    CK(cudaMemcpyAsync(c->fpx.p, hx.data(), (size_t)m * 3 * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(hg::launch_field_on_body(c->st, m, c->fpx.p, m, n, c->ntnd, c->nodes.p, c->ncon.p, c->ncn.p, c->dxyz.p,
+                                c->pnsz.p, c->fonb.p));
+    // rows = field points, no free term: fA = DUM2, fS = DUM1 (FP64 in both forms)
+    CK(hg::launch_green_fill<double2>(c->st, c->rec.p, c->fpx.p, m, n, m, fs, deep, c->o.grn_kind, c->fA.p, c->fS.p, m,
+                                      c->status.p, binned ? c->bins.p : nullptr, 0));
+    CK(hg::gemm<double>(c->st, false, m, ncol, n, one, c->fS.p, m, c->fW.p, n, zero, c->fout.p, m, WS(c)));
+    CK(hg::gemm<double>(c->st, false, m, ncol, n, mone, c->fA.p, m, c->X.p, n, one, c->fout.p, m, WS(c)));
+    CK(hg::launch_field_finish(c->st, m, ncol, nrad, c->fout.p, m, c->fonb.p, c->fpx.p, m, c->betas.p, c->v, c->wk,
+                               c->w1, c->h, c->o.g, c->o.rho, isol, kind));
+    CK(cudaMemcpy2DAsync(out + 2 * (size_t)p0, (size_t)ldo * sizeof(double2), c->fout.p, (size_t)m * sizeof(double2),
+                         (size_t)m * sizeof(double2), ncol, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));  // hx is rewritten by the next chunk
+  }
+  return check_status(c);
 }
 
 int hg_solve_frequency(hg_ctx* c, double v, double wk, double w1, double h, const double* wvn, int nk, int irsp,

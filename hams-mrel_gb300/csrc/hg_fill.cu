@@ -111,10 +111,11 @@ __global__ void k_prep_panels(int n, int ntnd, const double* __restrict__ nodes 
 template <typename OUT>
 cudaError_t launch_green_fill(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
                               const FinState& fs, bool deep, int grn_kind, OUT* A, OUT* S, long lda, int* status,
-                              int* bins) {
-  if (!deep) return launch_green_fill_fin<OUT>(st, rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, status, bins);
+                              int* bins, int ndiag) {
+  if (ndiag < 0) ndiag = tn;
+  if (!deep) return launch_green_fill_fin<OUT>(st, rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, status, bins, ndiag);
   dim3 grid((tn + FILL_ROWS - 1) / FILL_ROWS, (n + FILL_COLS - 1) / FILL_COLS);
-  k_green_fill<true, OUT><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, status);
+  k_green_fill<true, OUT><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, status, ndiag);
   return cudaGetLastError();
 }
 
@@ -347,9 +348,11 @@ cudaError_t launch_green_fill_mixed_fin(cudaStream_t st, const double* rec, cons
   return cudaGetLastError();
 }
 template cudaError_t launch_green_fill<double2>(cudaStream_t, const double*, const double*, int, int, int,
-                                                const FinState&, bool, int, double2*, double2*, long, int*, int*);
+                                                const FinState&, bool, int, double2*, double2*, long, int*, int*,
+                                                int);
 template cudaError_t launch_green_fill<float2>(cudaStream_t, const double*, const double*, int, int, int,
-                                               const FinState&, bool, int, float2*, float2*, long, int*, int*);
+                                               const FinState&, bool, int, float2*, float2*, long, int*, int*,
+                                               int);
 
 cudaError_t launch_prep_panels(cudaStream_t st, int n, int ntnd, const double* nodes, const int* ncon, const int* ncn,
                                const double* xyz_p, const double* ds, const double* pnsz, const double* dxyz_p,

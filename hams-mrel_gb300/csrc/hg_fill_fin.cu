@@ -14,16 +14,17 @@ namespace hg {
 // hg_fill_kernel.cuh); without it the tiled kernel runs.
 template <typename OUT>
 cudaError_t launch_green_fill_fin(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
-                                  const FinState& fs, int grn_kind, OUT* A, OUT* S, long lda, int* status, int* bins) {
-  if (bins) return launch_fin_binned<OUT, 0>(st, rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, bins);
+                                  const FinState& fs, int grn_kind, OUT* A, OUT* S, long lda, int* status, int* bins,
+                                  int ndiag) {
+  if (bins) return launch_fin_binned<OUT, 0>(st, rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, bins, ndiag);
   dim3 grid((tn + FILL_ROWS - 1) / FILL_ROWS, (n + FILL_COLS - 1) / FILL_COLS);
-  k_green_fill<false, OUT><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, status);
+  k_green_fill<false, OUT><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, status, ndiag);
   return cudaGetLastError();
 }
 template cudaError_t launch_green_fill_fin<double2>(cudaStream_t, const double*, const double*, int, int, int,
-                                                    const FinState&, int, double2*, double2*, long, int*, int*);
+                                                    const FinState&, int, double2*, double2*, long, int*, int*, int);
 template cudaError_t launch_green_fill_fin<float2>(cudaStream_t, const double*, const double*, int, int, int,
-                                                   const FinState&, int, float2*, float2*, long, int*, int*);
+                                                   const FinState&, int, float2*, float2*, long, int*, int*, int);
 
 cudaError_t launch_green_points_fin(cudaStream_t st, int npts, const double* pts, const int* flags, const FinState& fs,
                                     double* out) {

@@ -12,9 +12,9 @@ namespace hg {
 cudaError_t launch_green_fill_fin_fma(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
                                       const FinState& fs, int grn_kind, float2* A, float2* S, long lda, int* status,
                                       int* bins) {
-  if (bins) return launch_fin_binned<float2, 1>(st, rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, bins);
+  if (bins) return launch_fin_binned<float2, 1>(st, rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, bins, tn);
   dim3 grid((tn + FILL_ROWS - 1) / FILL_ROWS, (n + FILL_COLS - 1) / FILL_COLS);
-  k_green_fill<false, float2, 1><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, status);
+  k_green_fill<false, float2, 1><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, status, tn);
   return cudaGetLastError();
 }
 

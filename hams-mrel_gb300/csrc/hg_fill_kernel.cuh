@@ -19,10 +19,12 @@ constexpr int FILL_COLS = 16;
 
 // One (field i, source j) pair of the fill: FLAG, Newman integral, Green
 // function, assembly of A(i, j) and S(i, j) (the loop body of k_green_fill).
+// ndiag: rows below it are collocation points (row i is panel i's centroid)
+// and get the free term 2 pi on the diagonal; field points (ndiag = 0) none.
 template <bool DEEP, typename OUT>
 __device__ __forceinline__ void fill_pair(const double* __restrict__ pr, double xp, double yp, double zp, int i, int j,
                                           const FinState& fs, int grn_kind, OUT* __restrict__ A,
-                                          OUT* __restrict__ S, long lda) {
+                                          OUT* __restrict__ S, long lda, int ndiag) {
   const double xq = pr[PR_XQ], yq = pr[PR_XQ + 1], zq = pr[PR_XQ + 2];
   const double dist = sqrt((xp - xq) * (xp - xq) + (yp - yq) * (yp - yq) + (zp - zq) * (zp - zq));
   const int flag = (dist <= pr[PR_FLAGD]) ? 1 : 0;
@@ -48,7 +50,7 @@ __device__ __forceinline__ void fill_pair(const double* __restrict__ pr, double 
     sr = g[0].x * ear;
   }
   si = g[0].y * ear;
-  if (i == j) ar += 2.0 * HG_PI;
+  if (i == j && i < ndiag) ar += 2.0 * HG_PI;
   store_c(A + i + (long)j * lda, ar, ai);
   store_c(S + i + (long)j * lda, sr, si);
 }
@@ -59,7 +61,7 @@ __device__ __forceinline__ void fill_pair(const double* __restrict__ pr, double 
 template <bool DEEP, typename OUT, int FAST = 0>
 __global__ void __launch_bounds__(FILL_ROWS)
 k_green_fill(const double* __restrict__ rec, const double* __restrict__ fx /* ldf x 3 col-major */, int ldf, int n, int tn,
-             FinState fs, int grn_kind, OUT* __restrict__ A, OUT* __restrict__ S, long lda, int* status) {
+             FinState fs, int grn_kind, OUT* __restrict__ A, OUT* __restrict__ S, long lda, int* status, int ndiag) {
   __shared__ alignas(128) double tile[FILL_COLS * PR_SIZE];
   __shared__ alignas(8) uint64_t bar;
   const int col0 = blockIdx.y * FILL_COLS;
@@ -79,7 +81,7 @@ k_green_fill(const double* __restrict__ rec, const double* __restrict__ fx /* ld
   if (i >= tn) return;
   const double xp = fx[i], yp = fx[i + ldf], zp = fx[i + 2 * (size_t)ldf];
   for (int jj = 0; jj < ncol; ++jj)
-    fill_pair<DEEP, OUT>(tile + jj * PR_SIZE, xp, yp, zp, i, col0 + jj, fs, grn_kind, A, S, lda);
+    fill_pair<DEEP, OUT>(tile + jj * PR_SIZE, xp, yp, zp, i, col0 + jj, fs, grn_kind, A, S, lda, ndiag);
 }
 
 // ---------------------------------------------------------------------------
@@ -165,18 +167,18 @@ template <typename OUT, int FAST>
 __global__ void __launch_bounds__(128)
 k_green_fill_binned(const double* __restrict__ rec, const double* __restrict__ fx, int ldf, int tn, long npairs,
                     const int* __restrict__ list, FinState fs, int grn_kind, OUT* __restrict__ A,
-                    OUT* __restrict__ S, long lda) {
+                    OUT* __restrict__ S, long lda, int ndiag) {
   for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < npairs; k += (long)gridDim.x * blockDim.x) {
     const int p = list[k];
     const int i = p % tn, j = p / tn;
     fill_pair<false, OUT>(rec + (size_t)j * PR_SIZE, fx[i], fx[i + ldf], fx[i + 2 * (size_t)ldf], i, j, fs, grn_kind,
-                          A, S, lda);
+                          A, S, lda, ndiag);
   }
 }
 
 template <typename OUT, int FAST>
 cudaError_t launch_fin_binned(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
-                              const FinState& fs, int grn_kind, OUT* A, OUT* S, long lda, int* bins) {
+                              const FinState& fs, int grn_kind, OUT* A, OUT* S, long lda, int* bins, int ndiag) {
   int* counts = bins;
   int* list = bins + kFinBins;
   cudaError_t e = cudaMemsetAsync(counts, 0, kFinBins * sizeof(int), st);
@@ -188,7 +190,8 @@ cudaError_t launch_fin_binned(cudaStream_t st, const double* rec, const double* 
   const long np = (long)tn * n;
   long blocks = (np + 127) / 128;
   if (blocks > 152L * 64) blocks = 152L * 64;
-  k_green_fill_binned<OUT, FAST><<<(unsigned)blocks, 128, 0, st>>>(rec, fx, ldf, tn, np, list, fs, grn_kind, A, S, lda);
+  k_green_fill_binned<OUT, FAST><<<(unsigned)blocks, 128, 0, st>>>(rec, fx, ldf, tn, np, list, fs, grn_kind, A, S, lda,
+                                                                  ndiag);
   return cudaGetLastError();
 }
 

@@ -17,12 +17,12 @@ cudaError_t launch_prep_panels(cudaStream_t st, int n, int ntnd, const double* n
 template <typename OUT>
 cudaError_t launch_green_fill(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
                               const FinState& fs, bool deep, int grn_kind, OUT* A, OUT* S, long lda, int* status,
-                              int* bins = nullptr);
+                              int* bins = nullptr, int ndiag = -1);  // ndiag: rows with the 2 pi free term (-1: all)
 
 template <typename OUT>
 cudaError_t launch_green_fill_fin(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
                                   const FinState& fs, int grn_kind, OUT* A, OUT* S, long lda, int* status,
-                                  int* bins);
+                                  int* bins, int ndiag);
 // Finite depth, complex64 output, compiled with FMA contraction (mixed form).
 cudaError_t launch_green_fill_fin_fma(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
                                       const FinState& fs, int grn_kind, float2* A, float2* S, long lda, int* status,
@@ -60,6 +60,16 @@ cudaError_t launch_rhs(cudaStream_t st, int n, int tn, const IN* S, long lds, co
 // B = S W then gives every right-hand side at once.
 cudaError_t launch_rhs_cols(cudaStream_t st, int n, const double* dxyz_p, const int* body_of, int nbody, int nbeta,
                             const double2* w, double2* W, long ldw);
+
+// Field points (hg_field.cu): onb[p] = 1 where point p (npts x 3 column-major,
+// leading dimension ldp) lies on a panel; the finishing pass of the field
+// potentials acc (npts x ncol, columns >= nrad are diffraction headings).
+cudaError_t launch_field_on_body(cudaStream_t st, int npts, const double* px, int ldp, int n, int ntnd,
+                                 const double* nodes, const int* ncon, const int* ncn, const double* dxyz,
+                                 const double* pnsz, int* onb);
+cudaError_t launch_field_finish(cudaStream_t st, int npts, int ncol, int nrad, double2* acc, long lda, const int* onb,
+                                const double* px, int ldp, const double* betas, double v, double wk, double w1,
+                                double h, double g, double rho, int isol, int kind);
 
 cudaError_t launch_forces(cudaStream_t st, int n, const double2* X, long ldx, const double* xyz_p, const double* ds,
                           const double* dxyz_p, const int* body_start, const int* body_end, int nbody, int nbeta,

@@ -25,7 +25,7 @@ EXPORTS = [
     "hg_stage_times", "hg_dispersion", "hg_wave_properties", "hg_panel_geometry", "hg_mark", "hg_elapsed",
     "hg_bench_gemm", "hg_green_points_noalloc", "hg_gesv", "hg_gemm_check",
     "hg_solve_sweep", "hg_gmres_iterations", "hg_solve_footprint", "hg_server_create", "hg_server_submit",
-    "hg_server_wait", "hg_server_stats", "hg_server_last_error", "hg_server_destroy",
+    "hg_server_wait", "hg_server_stats", "hg_server_last_error", "hg_server_destroy", "hg_field_points",
 ]
 
 
@@ -87,6 +87,7 @@ def load(build_if_missing: bool = True):
     L.hg_forces.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p]
     L.hg_solve_frequency.argtypes = [c_void_p, c_double, c_double, c_double, c_double, c_void_p, c_int, c_int,
                                      c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int]
+    L.hg_field_points.argtypes = [c_void_p, c_int, c_void_p, c_int, c_int, c_void_p, c_int]
     L.hg_keep_matrices.argtypes = [c_void_p, c_int]
     L.hg_get_matrix.argtypes = [c_void_p, c_int, c_void_p, c_int]
     L.hg_green_points.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p]
@@ -235,17 +236,20 @@ class Solver:
     def solve_radiation(self):
         out = np.zeros((self.n, 6 * self.nbody), dtype=np.complex128, order="F")
         self._check(self.L.hg_solve_radiation(self.h, _ptr(out), self.n))
+        self._ndif = 0
         return out
 
     def solve_all_headings(self, betas):
         b = np.ascontiguousarray(betas, dtype=np.float64)
         out = np.zeros((self.n, len(b)), dtype=np.complex128, order="F")
         self._check(self.L.hg_solve_all_headings(self.h, _ptr(b), len(b), _ptr(out), self.n))
+        self._ndif = len(b)
         return out
 
     def solve_diffraction(self, beta):
         out = np.zeros(self.n, dtype=np.complex128)
         self._check(self.L.hg_solve_diffraction(self.h, float(beta), _ptr(out)))
+        self._ndif = 1
         return out
 
     def forces(self, nbeta, isol=1):
@@ -271,7 +275,19 @@ class Solver:
         self._check(self.L.hg_solve_frequency(self.h, v, wk, w1, h, _ptr(w), 0 if w is None else len(w), irsp,
                                               _ptr(b), nb, isol, _ptr(out["amas"]), _ptr(out["bdmp"]),
                                               _ptr(out["exfc"]), _ptr(mx), self.n))
+        self._ndif = nb
         return out["amas"], out["bdmp"], out["exfc"][:nb], mx
+
+    FIELD_POTENTIAL, FIELD_PRESSURE, FIELD_ELEVATION = 0, 1, 2
+
+    def field_points(self, xyz, kind=0, isol=1):
+        """Potential (kind 0), pressure (1) or elevation (2) at field points
+        xyz (npts, 3) for every column of the last solve (hg_field_points):
+        returns (npts, 6 nbody + nbeta) complex128."""
+        x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros((len(x), 6 * self.nbody + getattr(self, "_ndif", 0)), dtype=np.complex128, order="F")
+        self._check(self.L.hg_field_points(self.h, len(x), _ptr(x), int(kind), int(isol), _ptr(out), max(len(x), 1)))
+        return out
 
     def solve_sweep(self, v, wk, w1, h, wvn, betas, irsp=0, isol=1, nslots=1, out=None, want_potentials=False):
         """Frequency sweep over arrays v, wk, w1 (and wvn rows for finite depth)

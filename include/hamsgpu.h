@@ -142,6 +142,25 @@ int hg_solve_frequency(hg_ctx *ctx, double v, double wk, double w1, double h, co
                        double *exfc, double *mxpot, int ldm);
 
 /*
+ * Potential, pressure or free-surface elevation at field points from the last
+ * solve of this context; replaces CalPotential / CalPressure / CalElevation
+ * (src/PressureElevation.f90:53-336) and CalPotentialMulti / CalPressureMulti /
+ * CalElevationMulti (src/PressureElevationMulti.f90:55-360), which the reference
+ * calls once per point and mode from WritePressureElevation
+ * (PressureElevation.f90:380-460): here every point and every solved column
+ * in one call.
+ *   xyz[npts*3]    field points XET(3, NPTS) (x, y, z of each point together)
+ *   kind           0 potential, 1 pressure (i w rho pot), 2 elevation (i w/g pot)
+ *   isol           1 adds the incident potential to the diffraction columns
+ *   out            COMPLEX*16 (ldo, 6*nbody + nbeta): columns as in mxpot of
+ *                  hg_solve_frequency (radiation mode 6b+m, then headings);
+ *                  the heading columns only after a diffraction solve
+ * SLD = 2 pi for points on a panel (the reference's on-surface test), 4 pi
+ * elsewhere.  Needs a radiation solve first (HG_ERR_STATE otherwise).
+ */
+int hg_field_points(hg_ctx *ctx, int npts, const double *xyz, int kind, int isol, double *out, int ldo);
+
+/*
  * A frequency sweep: the frequency loop of HAMS_Prog (src/HAMS_Prog.f90:255-304
  * single body, :613-704 multi-body) over nfreq frequencies of one mesh, depth,
  * heading set and irsp, each frequency the work of hg_solve_frequency.

@@ -120,6 +120,18 @@ void or_eforce(int i0, int i1, const double *xyz_p, const double *ds, const doub
                double w1, double beta, double v, double wk, double h, int isol,
                const zdouble *phi7, zdouble exfc[6]);
 
+/* CalPotential / CalPotentialMulti (PressureElevation.f90:53-250,
+ * PressureElevationMulti.f90:55-272), NSYS = 1: the potential at field points
+ * xf[npts][3] of every solved column c of mxpot (n rows, leading dimension
+ * ldm): c < 6 nbody radiation mode c % 6 of body c / 6 (source weight
+ * DXYZ_P(j, mode) on that body's panels), c >= 6 nbody diffraction for
+ * betas[c - 6 nbody] (weight -grad phi_I . n); pot = (sum_j DUM1 w - DUM2 phi)
+ * / SLD, SLD = 2 pi for a point on a body panel and 4 pi elsewhere, plus VINP
+ * for diffraction columns when isol = 1.  pot[p + c * npts]. */
+void or_field_potential(const or_mesh *m, int npts, const double *xf, double v, double wk, double w1,
+                        const double *wvn, int nk, double h, int nbody, const int *body_start, const int *body_end,
+                        int nbeta, const double *betas, int isol, const zdouble *mxpot, int ldm, zdouble *pot);
+
 #ifdef __cplusplus
 }
 #endif

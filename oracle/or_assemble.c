@@ -224,3 +224,96 @@ void or_green_point(double xq, double yq, double zq, double xp, double yp, doubl
     else or_fingreen3d(xq, xp, yq, yp, zq, zp, v, wvn, nk, h, g, flag);
     for (k = 0; k < 4; ++k) { out8[2 * k] = creal(g[k]); out8[2 * k + 1] = cimag(g[k]); }
 }
+
+/* CalPotential / CalPotentialMulti (src/PressureElevation.f90:53-250,
+ * src/PressureElevationMulti.f90:55-272) for NSYS = 1, every solved column at
+ * once; see hams_oracle.h. */
+static int on_body(const or_mesh *m, const double *p)
+{
+    int j;
+    for (j = 0; j < m->n; ++j) {
+        const double *en = m->dxyz_p + 6 * j;
+        const double tolp = fmax(1.0e-6, 1.0e-3 * m->pnsz[j]), tola = 1.0e-3 * m->pnsz[j] * m->pnsz[j];
+        const int ncv = m->ncn[j];
+        const double *va = m->nodes + 3 * (m->ncon[4 * j] - 1);
+        double dpln = (p[0] - va[0]) * en[0] + (p[1] - va[1]) * en[1] + (p[2] - va[2]) * en[2];
+        double smin = 1.0e30, smax = -1.0e30;
+        int kk;
+        if (fabs(dpln) > tolp) continue;
+        for (kk = 0; kk < ncv; ++kk) {
+            const double *a = m->nodes + 3 * (m->ncon[4 * j + kk] - 1);
+            const double *b = m->nodes + 3 * (m->ncon[4 * j + (kk + 1 < ncv ? kk + 1 : 0)] - 1);
+            const double ev[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+            const double wv[3] = {p[0] - a[0], p[1] - a[1], p[2] - a[2]};
+            const double cx = ev[1] * wv[2] - ev[2] * wv[1], cy = ev[2] * wv[0] - ev[0] * wv[2],
+                         cz = ev[0] * wv[1] - ev[1] * wv[0];
+            const double sv = cx * en[0] + cy * en[1] + cz * en[2];
+            smin = fmin(smin, sv);
+            smax = fmax(smax, sv);
+        }
+        if (smin >= -tola || smax <= tola) return 1;
+    }
+    return 0;
+}
+
+void or_field_potential(const or_mesh *m, int npts, const double *xf, double v, double wk, double w1,
+                        const double *wvn, int nk, double h, int nbody, const int *body_start, const int *body_end,
+                        int nbeta, const double *betas, int isol, const zdouble *mxpot, int ldm, zdouble *pot)
+{
+    const int n = m->n, ncol = 6 * nbody + nbeta;
+    zdouble *dinc = (zdouble *)malloc(sizeof(zdouble) * (size_t)n * (nbeta > 0 ? nbeta : 1));
+    int p, j, k;
+    for (k = 0; k < nbeta; ++k)
+        for (j = 0; j < n; ++j) {
+            const double *xq = m->xyz_p + 3 * j, *env = m->dxyz_p + 6 * j;
+            zdouble dx, dy, dz;
+            or_dinp(xq[0], xq[1], xq[2], betas[k], v, wk, w1, h, &dx, &dy, &dz);
+            dinc[(size_t)k * n + j] = dx * env[0] + dy * env[1] + dz * env[2];
+        }
+#pragma omp parallel for schedule(dynamic, 4)
+    for (p = 0; p < npts; ++p) {
+        const double *x = xf + 3 * p;
+        zdouble *acc = (zdouble *)calloc((size_t)ncol, sizeof(zdouble));
+        int jj, c, b;
+        for (jj = 0; jj < n; ++jj) {
+            double rkn[4], ear = m->ds[jj];
+            const double *env = m->dxyz_p + 6 * jj;
+            zdouble grn[4], dum1, dum2;
+            int flag;
+            pair_terms(m, x, jj, v, wvn, nk, h, 8, &flag, rkn, grn);
+            if (flag == 1) {
+                dum1 = rkn[0] + grn[0] * ear;
+                dum2 = (rkn[1] + grn[1] * ear) * env[0] + (rkn[2] + grn[2] * ear) * env[1]
+                     + (rkn[3] + grn[3] * ear) * env[2];
+            } else {
+                dum1 = grn[0] * ear;
+                dum2 = (grn[1] * env[0] + grn[2] * env[1] + grn[3] * env[2]) * ear;
+            }
+            for (b = 0; b < nbody; ++b) {
+                const int in = (jj >= body_start[b] && jj < body_end[b]);
+                int md;
+                for (md = 0; md < 6; ++md) {
+                    c = 6 * b + md;
+                    acc[c] += (in ? dum1 * env[md] : 0.0) - dum2 * mxpot[(size_t)c * ldm + jj];
+                }
+            }
+            for (k = 0; k < nbeta; ++k) {
+                c = 6 * nbody + k;
+                acc[c] += -dum1 * dinc[(size_t)k * n + jj] - dum2 * mxpot[(size_t)c * ldm + jj];
+            }
+        }
+        {
+            const double sld = on_body(m, x) ? 2.0 * PI : 4.0 * PI;
+            const int special = fabs(v) < (double)1.e-8f || fabs(v + 1.0) < (double)1.e-8f;
+            for (c = 0; c < ncol; ++c) {
+                zdouble r = acc[c] / sld;
+                if (c >= 6 * nbody && isol == 1 && !special)
+                    r += or_vinp(x[0], x[1], x[2], betas[c - 6 * nbody], v, wk, w1, h);
+                pot[(size_t)c * npts + p] = r;
+            }
+        }
+        free(acc);
+    }
+    free(dinc);
+}
+

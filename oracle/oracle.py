@@ -130,6 +130,10 @@ def _configure(L):
         L.or_fingreen_region.restype = ctypes.c_int
         L.or_vinp.argtypes = [ctypes.c_double] * 8
         L.or_vinp.restype = ctypes.c_double * 2
+        L.or_field_potential.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_double, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ip, ip,
+                                         ctypes.c_int, dp, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                         ctypes.c_void_p]
     return L
 
 
@@ -497,6 +501,28 @@ def normal_equations(case: Case, A: np.ndarray, B: np.ndarray):
     L.or_normal_equations(tn, n, Af.ctypes.data, C.ctypes.data)
     L.or_normal_rhs(tn, n, Af.ctypes.data, B.shape[1], Bf.ctypes.data, D.ctypes.data)
     return C, D
+
+
+def field_potential(case: Case, xf: np.ndarray, v, wk, w1, wvn, betas_rad, mxpot: np.ndarray, isol=None):
+    """CalPotential(Multi) (src/PressureElevation.f90:53-250) at field points
+    xf (npts, 3) for every column of mxpot (n x (6 nbody + nbeta)): returns
+    pot (npts, 6 nbody + nbeta)."""
+    L = lib()
+    m, keep = _mesh_struct(case)
+    npts = len(xf)
+    x = np.ascontiguousarray(xf, dtype=np.float64)
+    b = np.ascontiguousarray(betas_rad, dtype=np.float64)
+    phi = np.asfortranarray(mxpot, dtype=np.complex128)
+    ncol = phi.shape[1]
+    out = np.zeros((npts, ncol), dtype=np.complex128, order="F")
+    st = np.ascontiguousarray(case.body_start); en = np.ascontiguousarray(case.body_end)
+    w = np.ascontiguousarray(wvn if wvn is not None else np.zeros(1), dtype=np.float64)
+    L.or_field_potential(ctypes.byref(m), npts, _dp(x), float(v), float(wk), float(w1), _dp(w),
+                         len(w) if wvn is not None else 0, float(case.ctl.h), case.nbody, _ip(st), _ip(en),
+                         len(b), _dp(b), case.ctl.isol if isol is None else isol, phi.ctypes.data, phi.shape[0],
+                         out.ctypes.data)
+    del keep
+    return out
 
 
 def forces(case: Case, mxpot: np.ndarray, v, wk, w1, betas_rad):
