@@ -438,6 +438,70 @@ def three_bodies(args):
     print(json.dumps(line), flush=True)
 
 
+def field_map(args):
+    """A wave-field map of the 6048-panel array (deep water, one frequency,
+    8 headings, 30 modes solved once, untimed): free-surface elevation at a
+    64 x 64 grid of points around the bodies (those inside a body's waterline
+    box left out) for all 38 columns, each step one hg_field_points call from
+    host coordinates to host results.  Beside it the CPU oracle on 256 of the
+    points, and the difference between the two there."""
+    pkg, mesh = _mesh()
+    hg = pkg.hamsgpu
+    prec = hg.HG_PREC_MIXED if args.precision == "mixed" else hg.HG_PREC_FP64
+    betas = BETAS_DEG * math.pi / 180.0
+    w = 0.8
+    v, wk, w1 = _frequency_inputs(pkg, w)
+    s = hg.Solver(precision=prec)
+    s.set_mesh(mesh.nodes, mesh.ncon, mesh.ncn, mesh.xyz_p, mesh.ds, mesh.pnsz, mesh.dxyz_p, mesh.body_ranges)
+    _, _, _, mx = s.solve_frequency(v, wk, w1, -1.0, None, betas)
+    lo, hi = mesh.xyz_p.min(axis=0), mesh.xyz_p.max(axis=0)
+    gx = np.linspace(lo[0] - 40.0, hi[0] + 40.0, 64)
+    gy = np.linspace(lo[1] - 40.0, hi[1] + 40.0, 64)
+    X, Y = np.meshgrid(gx, gy, indexing="ij")
+    pts = np.column_stack([X.ravel(), Y.ravel(), np.zeros(X.size)])
+    inside = np.zeros(len(pts), dtype=bool)
+    for b0, b1 in mesh.body_ranges:
+        q = mesh.xyz_p[b0 - 1:b1]
+        blo, bhi = q.min(axis=0) - 0.5, q.max(axis=0) + 0.5
+        inside |= (pts[:, 0] > blo[0]) & (pts[:, 0] < bhi[0]) & (pts[:, 1] > blo[1]) & (pts[:, 1] < bhi[1])
+    pts = pts[~inside]
+    for _ in range(args.warmup):
+        elv = s.field_points(pts, kind=2)
+    times = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            s.mark(0)
+            elv = s.field_points(pts, kind=2)
+            s.mark(1)
+            times.append(s.elapsed_ms(0, 1))
+    ncol = elv.shape[1]
+    s.close()
+    ms = float(np.mean(times))
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle
+    from helpers import case_from_mesh, max_norm_err
+    case = case_from_mesh(oracle, mesh, h=-1.0, headings_deg=list(BETAS_DEG))
+    sample = pts[:: max(1, len(pts) // 256)][:256]
+    idx = [int(np.flatnonzero((pts == p).all(axis=1))[0]) for p in sample]
+    t0 = time.perf_counter()
+    ref = oracle.field_potential(case, sample, v, wk, w1, None, betas, mx)
+    tcpu = time.perf_counter() - t0
+    ref = 1j * w1 / 9.80665 * ref
+    line = {"metric": "field points/s (free-surface elevation, all 38 columns per point)",
+            "value": len(pts) / (ms / 1e3), "unit": "points/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "complex128", "data": "synthetic",
+            "config": {"workload": "5-body array, 6048 panels, deep water, w 0.8 rad/s, 8 headings, 30 modes; "
+                                   "%d free-surface points" % len(pts), "solve_form": args.precision,
+                       "timing": "host coordinates in, host results out (hg_field_points), CUDA events"},
+            "vs_oracle_max_norm_err": max_norm_err(elv[idx], ref),
+            "cpu_baseline": {"value": len(sample) / tcpu, "unit": "points/s", "cores": os.cpu_count(),
+                             "kind": "port", "sample": "%d of the points, C oracle with OpenMP over points" % len(sample)},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def _launch_count(n, prec, sweeps=1, nd=30, nbeta=8):
     """Kernels the library launches per frequency-solve, from its launch
     sequence (checked against the ncu launch list of one solve)."""
@@ -509,7 +573,7 @@ def main():
                     help="mixed-form refinement: classical iterative refinement or GMRES-IR")
     ap.add_argument("--lu-tensor", type=int, default=3, choices=[0, 1, 3],
                     help="LU trailing updates: 3 split-TF32 tensor cores, 1 TF32, 0 FP32 SIMT")
-    ap.add_argument("--workload", default="array", choices=["array", "batch", "serve", "three"],
+    ap.add_argument("--workload", default="array", choices=["array", "batch", "serve", "three", "field"],
                     help="array: the 6048-panel frequency sweep (headline); batch / serve: the request server")
     ap.add_argument("--requests", type=int, default=None, help="batch / serve: number of requests")
     args = ap.parse_args()
@@ -520,6 +584,9 @@ def main():
         return
     if args.workload == "three":
         three_bodies(args)
+        return
+    if args.workload == "field":
+        field_map(args)
         return
     if args.workload != "array":
         if args.requests is None:

@@ -67,6 +67,7 @@ struct hg_ctx {
   DevBuf<int> ncon, ncn, body_of, body_start, body_end, ipiv, status, info;
   DevBuf<int> bins;                      // finite depth: pairs binned by the cost of their Green function
   DevBuf<float> tab;                     // finite depth, mixed form: tabulated Green function
+  DevBuf<float4> pgauss;                 // mixed form: Gauss points of the panel integrals (relative to ox, oy)
   // frequency
   double v = 0, wk = 0, w1 = 0, h = -1, nm0 = 0;
   int nk = 0;
@@ -84,7 +85,8 @@ struct hg_ctx {
   // field points (hg_field_points): coordinates, on-body flags, DUM2 / DUM1 rows, weights, potentials
   DevBuf<double> fpx;
   DevBuf<int> fonb;
-  DevBuf<double2> fA, fS, fW, fout;
+  DevBuf<double2> fA, fS, fW, fout, fout2;
+  DevBuf<float2> fAf, fSf;
   int inner_its = 0;                     // GMRES iterations of the last solve
   int irsp = 0;
   bool factored = false;
@@ -651,6 +653,9 @@ int hg_set_mesh(hg_ctx* c, int n, int ntnd, const double* nodes, const int* ncon
     c->oy = sy / n;
     c->rmax = std::sqrt((x1 - x0) * (x1 - x0) + (y1 - y0) * (y1 - y0));
   }
+  CK(c->pgauss.ensure((size_t)n * hg::kPanelGauss));
+  CK(hg::launch_panel_gauss(c->st, n, c->rec.p, c->ox, c->oy, c->pgauss.p));
+  CK(cudaStreamSynchronize(c->st));
   c->slots_mesh = false;
   c->mesh_set = true;
   c->factored = false;
@@ -731,7 +736,7 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
       CK(c->tab.ensure(hg::fintab_floats() + (size_t)6 * n));
       hg::FinTab tab;
       CK(hg::fintab_build(c->st, fs, 1.02 * c->rmax + 1.0, c->tab.p, &tab));
-      CK(hg::launch_green_fill_mixed_fin(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, tab, c->ox, c->oy,
+      CK(hg::launch_green_fill_mixed_fin(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, tab, c->ox, c->oy, c->pgauss.p,
                                          c->tab.p + hg::fintab_floats(), c->Af.p, c->Sf.p, tn, c->status.p));
     } else if (!deep) {
       const bool binned = (long long)tn * n < 2147483647LL;
@@ -739,8 +744,8 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
       CK(hg::launch_green_fill_fin_fma(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, c->o.grn_kind, c->Af.p, c->Sf.p, tn,
                                        c->status.p, binned ? c->bins.p : nullptr));
     } else if (!special && c->o.grn_kind == 8)
-      CK(hg::launch_green_fill_mixed(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, c->v, c->ox, c->oy, c->Af.p, c->Sf.p, tn,
-                                     c->status.p));
+      CK(hg::launch_green_fill_mixed(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, c->v, c->ox, c->oy, c->pgauss.p, c->Af.p,
+                                     c->Sf.p, tn, c->status.p));
     else
       CK(hg::launch_green_fill<float2>(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, deep, c->o.grn_kind, c->Af.p,
                                        c->Sf.p, tn, c->status.p));
@@ -872,16 +877,29 @@ int hg_field_points(hg_ctx* c, int npts, const double* xyz, int kind, int isol, 
   cudaSetDevice(c->o.device);
   const int n = c->n, nrad = 6 * c->nbody, nbeta = c->dif_done ? c->nbeta : 0, ncol = nrad + nbeta;
   const bool deep = c->h < 0.0;
+  const bool special = std::fabs(c->v) < (double)1.e-8f || std::fabs(c->v + 1.0) < (double)1.e-8f;
   const FinState fs = fin_state(c);
-  // Field points in chunks of up to 2048 rows: two chunk x n complex128
-  // matrices (DUM2 and DUM1) at a time.
+  // The mixed form in deep water takes its single-precision fill for the
+  // field rows (its 1e-4 contract) and double-float products with the FP64
+  // solution; otherwise the FP64 fill and complex128 products.
+  const bool fast = mixed(c) && deep && !special && c->o.grn_kind == 8;
+  // Field points in chunks of up to 2048 rows: two chunk x n matrices (DUM2
+  // and DUM1) at a time.
   const int chunk = std::min(npts, 2048);
+  const int ldc = (chunk + 1) & ~1;  // even leading dimension: 16-byte aligned columns of complex64
   CK(c->fpx.ensure((size_t)chunk * 3));
   CK(c->fonb.ensure(chunk));
-  CK(c->fA.ensure((size_t)chunk * n));
-  CK(c->fS.ensure((size_t)chunk * n));
   CK(c->fW.ensure((size_t)n * ncol));
   CK(c->fout.ensure((size_t)chunk * ncol));
+  if (fast) {
+    CK(c->fAf.ensure((size_t)ldc * n));
+    CK(c->fSf.ensure((size_t)ldc * n));
+    CK(c->fout2.ensure((size_t)chunk * ncol));
+    CK(c->rws.ensure(hg::resid_work_bytes(ldc, ncol, n)));
+  } else {
+    CK(c->fA.ensure((size_t)chunk * n));
+    CK(c->fS.ensure((size_t)chunk * n));
+  }
   const bool binned = !deep && (long long)chunk * n < 2147483647LL;
   if (binned) CK(c->bins.ensure(hg::fin_bins_ints(n, chunk)));
   // source weights [radiation modes | -grad phi_I . n of the solved headings]
@@ -895,11 +913,21 @@ int hg_field_points(hg_ctx* c, int npts, const double* xyz, int kind, int isol, 
     CK(cudaMemcpyAsync(c->fpx.p, hx.data(), (size_t)m * 3 * sizeof(double), cudaMemcpyHostToDevice, c->st));
     CK(hg::launch_field_on_body(c->st, m, c->fpx.p, m, n, c->ntnd, c->nodes.p, c->ncon.p, c->ncn.p, c->dxyz.p,
                                 c->pnsz.p, c->fonb.p));
-    // rows = field points, no free term: fA = DUM2, fS = DUM1 (FP64 in both forms)
-    CK(hg::launch_green_fill<double2>(c->st, c->rec.p, c->fpx.p, m, n, m, fs, deep, c->o.grn_kind, c->fA.p, c->fS.p, m,
-                                      c->status.p, binned ? c->bins.p : nullptr, 0));
-    CK(hg::gemm<double>(c->st, false, m, ncol, n, one, c->fS.p, m, c->fW.p, n, zero, c->fout.p, m, WS(c)));
-    CK(hg::gemm<double>(c->st, false, m, ncol, n, mone, c->fA.p, m, c->X.p, n, one, c->fout.p, m, WS(c)));
+    // rows = field points, no free term: A rows = DUM2, S rows = DUM1
+    if (fast) {
+      const int ldm = (m + 1) & ~1;
+      CK(hg::launch_green_fill_mixed(c->st, c->rec.p, c->fpx.p, m, n, m, c->v, c->ox, c->oy, c->pgauss.p, c->fAf.p,
+                                     c->fSf.p, ldm, c->status.p, 0));
+      CK(hg::resid_df(c->st, false, m, ncol, n, c->fSf.p, ldm, c->fW.p, n, nullptr, 0, 1.0, c->fout2.p, m, c->rws.p,
+                      c->rws.cap, false));
+      CK(hg::resid_df(c->st, false, m, ncol, n, c->fAf.p, ldm, c->X.p, n, c->fout2.p, m, -1.0, c->fout.p, m, c->rws.p,
+                      c->rws.cap, false));
+    } else {
+      CK(hg::launch_green_fill<double2>(c->st, c->rec.p, c->fpx.p, m, n, m, fs, deep, c->o.grn_kind, c->fA.p, c->fS.p,
+                                        m, c->status.p, binned ? c->bins.p : nullptr, 0));
+      CK(hg::gemm<double>(c->st, false, m, ncol, n, one, c->fS.p, m, c->fW.p, n, zero, c->fout.p, m, WS(c)));
+      CK(hg::gemm<double>(c->st, false, m, ncol, n, mone, c->fA.p, m, c->X.p, n, one, c->fout.p, m, WS(c)));
+    }
     CK(hg::launch_field_finish(c->st, m, ncol, nrad, c->fout.p, m, c->fonb.p, c->fpx.p, m, c->betas.p, c->v, c->wk,
                                c->w1, c->h, c->o.g, c->o.rho, isol, kind));
     CK(cudaMemcpy2DAsync(out + 2 * (size_t)p0, (size_t)ldo * sizeof(double2), c->fout.p, (size_t)m * sizeof(double2),

@@ -179,6 +179,48 @@ static cudaError_t upload_cheb_constants() {
   return e;
 }
 
+// Gauss points of one panel for panel_gauss_f, from its record (double):
+// the flat panel of the closed form, X = PO + ksi ui + eta uj.
+__device__ __forceinline__ void panel_gauss_points(const double* __restrict__ pr, double ox, double oy, float4* q) {
+  const int nv = (int)pr[PR_NCN];
+  double v[4][3];
+  for (int c = 0; c < 4; ++c) {
+    const int k = (c < nv) ? c : nv - 1;
+    const double ks = pr[PR_KSI + k], et = pr[PR_ETA + k];
+    for (int d = 0; d < 3; ++d) v[c][d] = pr[PR_PO + d] + ks * pr[PR_UI + d] + et * pr[PR_UJ + d];
+  }
+  double a2 = 0.0;
+  for (int c = 0; c < nv; ++c) {
+    const int e = (c + 1 == nv) ? 0 : c + 1;
+    a2 += pr[PR_KSI + c] * pr[PR_ETA + e] - pr[PR_KSI + e] * pr[PR_ETA + c];
+  }
+  const double sgn = ((a2 > 0.0) == (nv == 4)) ? 1.0 : -1.0;
+  // 3 x 3 rule (points 0-8), then 2 x 2 (points 9-12)
+  const double gp3[3] = {-0.7745966692414834, 0.0, 0.7745966692414834}, gw3[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
+  const double gp2[2] = {-0.5773502691896258, 0.5773502691896258}, gw2[2] = {1.0, 1.0};
+  for (int t = 0; t < 13; ++t) {
+    const bool r3 = t < 9;
+    const int a = r3 ? t / 3 : (t - 9) / 2, b = r3 ? t % 3 : (t - 9) % 2;
+    const double u = r3 ? gp3[a] : gp2[a], w = r3 ? gp3[b] : gp2[b];
+    const double wt = r3 ? gw3[a] * gw3[b] : gw2[a] * gw2[b];
+    const double N[4] = {0.25 * (1 - u) * (1 - w), 0.25 * (1 + u) * (1 - w), 0.25 * (1 + u) * (1 + w),
+                         0.25 * (1 - u) * (1 + w)};
+    const double Nu[4] = {-0.25 * (1 - w), 0.25 * (1 - w), 0.25 * (1 + w), -0.25 * (1 + w)};
+    const double Nw[4] = {-0.25 * (1 - u), -0.25 * (1 + u), 0.25 * (1 + u), 0.25 * (1 - u)};
+    double X[3] = {0, 0, 0}, Xu[3] = {0, 0, 0}, Xw[3] = {0, 0, 0};
+    for (int c = 0; c < 4; ++c)
+      for (int d = 0; d < 3; ++d) {
+        X[d] += N[c] * v[c][d];
+        Xu[d] += Nu[c] * v[c][d];
+        Xw[d] += Nw[c] * v[c][d];
+      }
+    const double cx = Xu[1] * Xw[2] - Xu[2] * Xw[1], cy = Xu[2] * Xw[0] - Xu[0] * Xw[2],
+                 cz = Xu[0] * Xw[1] - Xu[1] * Xw[0];
+    q[t] = make_float4((float)(X[0] - ox), (float)(X[1] - oy), (float)X[2],
+                       (float)(sgn * wt * sqrt(cx * cx + cy * cy + cz * cz)));
+  }
+}
+
 // Single-precision pair loop of the mixed form.  Per pair only FP32
 // arithmetic, except (a) the self and adjacent pairs, within 2 panel sizes
 // (0.04 of the 50-panel-size FLAG radius), whose Newman integrals stay in
@@ -194,13 +236,14 @@ static cudaError_t upload_cheb_constants() {
 template <bool FIN>
 __global__ void __launch_bounds__(FILL_ROWS)
 k_green_fill_mixed(const double* __restrict__ rec, const double* __restrict__ fx, int ldf, int n, int tn, float vf,
-                   double ox, double oy, FinTab tab, const float* __restrict__ diag, float2* __restrict__ A,
-                   float2* __restrict__ S, long lda, int* status) {
+                   double ox, double oy, const float4* __restrict__ pg, FinTab tab, const float* __restrict__ diag,
+                   float2* __restrict__ A, float2* __restrict__ S, long lda, int* status, int ndiag) {
   __shared__ alignas(128) double tile[FILL_COLS * PR_SIZE];
   __shared__ alignas(8) uint64_t bar;
   __shared__ PanelF pfs[FILL_COLS];
   __shared__ float pds[FILL_COLS][4];  // area, normal
   __shared__ float pxs[FILL_COLS][8];  // xq, yq, zq (relative), FLAG radius squared, Newman origin (relative)
+  __shared__ float4 pgs[FILL_COLS][kPanelGauss];  // Gauss points of the panel integrals beyond 4 panel sizes
   const int col0 = blockIdx.y * FILL_COLS;
   const int ncol = min(FILL_COLS, n - col0);
   if (threadIdx.x == 0) {
@@ -236,6 +279,8 @@ k_green_fill_mixed(const double* __restrict__ rec, const double* __restrict__ fx
     px[6] = (float)pr[PR_PO + 2];
     px[7] = 0.f;
   }
+  for (int t = threadIdx.x; t < ncol * kPanelGauss; t += FILL_ROWS)
+    pgs[t / kPanelGauss][t % kPanelGauss] = pg[(size_t)col0 * kPanelGauss + t];
   __syncthreads();
   const int i = blockIdx.x * FILL_ROWS + threadIdx.x;
   if (i >= tn) return;
@@ -262,8 +307,12 @@ k_green_fill_mixed(const double* __restrict__ rec, const double* __restrict__ fx
         double s64, e0, e1, e2;
         newman_pair(tile + jj * PR_SIZE, xp, yp, zp, s64, e0, e1, e2);
         sij = (float)s64; d0 = (float)e0; d1 = (float)e1; d2 = (float)e2;
-      } else {
+      } else if (d2f <= 0.0064f * fl2) {
         newman_pair_f(pfs[jj], xpf - px[4], ypf - px[5], zpf - px[6], sij, d0, d1, d2);
+      } else if (d2f <= 0.0576f * fl2) {
+        panel_gauss_f<9>(pgs[jj], xpf, ypf, zpf, sij, d0, d1, d2);
+      } else {
+        panel_gauss_f<4>(pgs[jj] + 9, xpf, ypf, zpf, sij, d0, d1, d2);
       }
     }
     float2 g[4];
@@ -311,20 +360,21 @@ k_green_fill_mixed(const double* __restrict__ rec, const double* __restrict__ fx
       ai = (g[1].y * n0 + g[2].y * n1 + g[3].y * n2) * ear;
       sr = g[0].x * ear;
     }
-    if (i == j) ar += 6.28318530717959f;
+    if (i == j && i < ndiag) ar += 6.28318530717959f;
     A[i + (long)j * lda] = make_float2(ar, ai);
     S[i + (long)j * lda] = make_float2(sr, g[0].y * ear);
   }
 }
 
 cudaError_t launch_green_fill_mixed(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
-                                    double v, double ox, double oy, float2* A, float2* S, long lda, int* status) {
+                                    double v, double ox, double oy, const float4* pg, float2* A, float2* S, long lda,
+                                    int* status, int ndiag) {
   cudaError_t e = upload_cheb_constants();
   if (e != cudaSuccess) return e;
   dim3 grid((tn + FILL_ROWS - 1) / FILL_ROWS, (n + FILL_COLS - 1) / FILL_COLS);
   FinTab none = {};
-  k_green_fill_mixed<false><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, (float)v, ox, oy, none, nullptr, A, S,
-                                                         lda, status);
+  k_green_fill_mixed<false><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, (float)v, ox, oy, pg, none, nullptr, A, S,
+                                                         lda, status, ndiag < 0 ? tn : ndiag);
   return cudaGetLastError();
 }
 
@@ -339,12 +389,12 @@ __global__ void k_fin_diag(int n, const double* __restrict__ rec, FinState fs, f
 }
 
 cudaError_t launch_green_fill_mixed_fin(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
-                                        const FinState& fs, const FinTab& tab, double ox, double oy, float* diag,
-                                        float2* A, float2* S, long lda, int* status) {
+                                        const FinState& fs, const FinTab& tab, double ox, double oy,
+                                        const float4* pg, float* diag, float2* A, float2* S, long lda, int* status) {
   k_fin_diag<<<(n + 31) / 32, 32, 0, st>>>(n, rec, fs, diag);
   dim3 grid((tn + FILL_ROWS - 1) / FILL_ROWS, (n + FILL_COLS - 1) / FILL_COLS);
-  k_green_fill_mixed<true><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, (float)fs.v, ox, oy, tab, diag, A, S,
-                                                        lda, status);
+  k_green_fill_mixed<true><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, (float)fs.v, ox, oy, pg, tab, diag, A, S,
+                                                        lda, status, tn);
   return cudaGetLastError();
 }
 template cudaError_t launch_green_fill<double2>(cudaStream_t, const double*, const double*, int, int, int,
@@ -353,6 +403,16 @@ template cudaError_t launch_green_fill<double2>(cudaStream_t, const double*, con
 template cudaError_t launch_green_fill<float2>(cudaStream_t, const double*, const double*, int, int, int,
                                                const FinState&, bool, int, float2*, float2*, long, int*, int*,
                                                int);
+
+__global__ void k_panel_gauss(int n, const double* __restrict__ rec, double ox, double oy, float4* __restrict__ pg) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) panel_gauss_points(rec + (size_t)j * PR_SIZE, ox, oy, pg + (size_t)j * kPanelGauss);
+}
+
+cudaError_t launch_panel_gauss(cudaStream_t st, int n, const double* rec, double ox, double oy, float4* pg) {
+  k_panel_gauss<<<(n + 63) / 64, 64, 0, st>>>(n, rec, ox, oy, pg);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_prep_panels(cudaStream_t st, int n, int ntnd, const double* nodes, const int* ncon, const int* ncn,
                                const double* xyz_p, const double* ds, const double* pnsz, const double* dxyz_p,

@@ -170,4 +170,40 @@ __device__ __forceinline__ void newman_pair_f(const PanelF& pf, float p0, float 
   d2 = sg * (pf.ui[2] * sxt + pf.uj[2] * syt + pf.uk[2] * szt);
 }
 
+// Gauss rules of the panel integrals for field points 4 or more panel sizes
+// away, where the closed form loses accuracy in single precision: its edge
+// terms are each of the panel's size while the integral is of size
+// area / distance, so rounding grows with distance (2e-6 relative at 4 panel
+// sizes, 2.5e-4 at 50), whereas Gauss-Legendre rules on the flat panel
+// (bilinear map; triangles as quads with a collapsed edge) hold 3e-7: the
+// integrand is smooth there and every term has the sign of the sum.  The
+// 3 x 3 rule serves 4 to 12 panel sizes, the 2 x 2 rule (also 3e-7 there)
+// the rest.  The points of both rules (the 9, then the 4), each
+// (x - ox, y - oy, z, signed weight), are prepared once per mesh
+// (launch_panel_gauss); the signed weight is the Gauss weight times |Jacobian|
+// times the sign that reproduces the closed form's convention, which follows
+// the vertex order (quads: the sign of the panel's signed area in its own
+// frame; triangles: the opposite).  Outputs as newman_pair_f: the integral
+// of 1/r and sg times the gradient terms, here d = -sum w (X_q - P)/r^3.
+template <int NQ>
+__device__ __forceinline__ void panel_gauss_f(const float4* __restrict__ q, float xp, float yp, float zp, float& sij,
+                                              float& d0, float& d1, float& d2) {
+  float s = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    const float4 g = q[k];
+    const float dx = g.x - xp, dy = g.y - yp, dz = g.z - zp;
+    const float ir = rsqrtf(dx * dx + dy * dy + dz * dz);
+    const float wi = g.w * ir, wi3 = wi * ir * ir;
+    s += wi;
+    gx = fmaf(dx, wi3, gx);
+    gy = fmaf(dy, wi3, gy);
+    gz = fmaf(dz, wi3, gz);
+  }
+  sij = s;
+  d0 = -gx;
+  d1 = -gy;
+  d2 = -gz;
+}
+
 }  // namespace hg

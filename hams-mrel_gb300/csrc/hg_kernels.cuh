@@ -10,6 +10,11 @@ struct FinState;
 __device__ __forceinline__ void store_c(double2* p, double re, double im) { *p = make_double2(re, im); }
 __device__ __forceinline__ void store_c(float2* p, double re, double im) { *p = make_float2((float)re, (float)im); }
 
+// Gauss points of the single-precision panel integrals (hg_green32.cuh,
+// panel_gauss_f): kPanelGauss float4 per panel, relative to (ox, oy).
+constexpr int kPanelGauss = 13;
+cudaError_t launch_panel_gauss(cudaStream_t st, int n, const double* rec, double ox, double oy, float4* pg);
+
 cudaError_t launch_prep_panels(cudaStream_t st, int n, int ntnd, const double* nodes, const int* ncon, const int* ncn,
                                const double* xyz_p, const double* ds, const double* pnsz, const double* dxyz_p,
                                double* rec, int* status);
@@ -35,15 +40,16 @@ size_t fintab_floats();
 cudaError_t fintab_build(cudaStream_t st, const FinState& fs, double rmax, float* buf, FinTab* out);
 // diag: device scratch of 6 n floats (the coincident pairs' FP64 values).
 cudaError_t launch_green_fill_mixed_fin(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
-                                        const FinState& fs, const FinTab& tab, double ox, double oy, float* diag,
-                                        float2* A, float2* S, long lda, int* status);
+                                        const FinState& fs, const FinTab& tab, double ox, double oy,
+                                        const float4* pg, float* diag, float2* A, float2* S, long lda, int* status);
 // Scratch ints of the cost-binned finite-depth fill: bin cursors + one pair index per pair.
 inline size_t fin_bins_ints(int n, int tn) { return 16 + (size_t)n * tn; }
 cudaError_t launch_green_points_fin(cudaStream_t st, int npts, const double* pts, const int* flags, const FinState& fs,
                                     double* out);
 
 cudaError_t launch_green_fill_mixed(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
-                                    double v, double ox, double oy, float2* A, float2* S, long lda, int* status);
+                                    double v, double ox, double oy, const float4* pg, float2* A, float2* S, long lda,
+                                    int* status, int ndiag = -1);  // ndiag: rows with the 2 pi free term (-1: all)
 
 cudaError_t launch_incident(cudaStream_t st, int n, const double* xyz_p, const double* dxyz_p, int nbeta,
                             const double* betas, double v, double wk, double w1, double h, double2* w);

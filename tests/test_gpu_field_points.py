@@ -4,8 +4,10 @@ PressureElevationMulti.f90:55-360) against the oracle.
 
 The oracle is given the GPU's own solved panel potentials, so the check
 covers the field-point step alone (the solve has its own parity tests).
-Deep water: the field-point Green function and panel sums are FP64 in both
-forms, held to 1e-10 max-normalised.  Finite depth: the Pidcock-region
+Deep water: the plain form's field-point Green function and panel sums are
+FP64, held to 1e-10 max-normalised; the mixed form takes its single-precision
+fill for the field rows and double-float products with the FP64 solution,
+held to 1e-5 (inside the mixed form's 1e-4 contract).  Finite depth: the Pidcock-region
 series noise of the Green function (see test_gpu_parity.py) bounds the
 agreement; the GPU is held to ten times the measured spread between the
 plain and the FMA-compiled oracle, never looser than 1e-10 where that spread
@@ -22,6 +24,7 @@ from helpers import case_from_mesh, gpu_frequency, gpu_solver, max_norm_err
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-10
+MIXED_TOL = 1e-5
 
 
 @pytest.fixture(scope="module")
@@ -64,10 +67,11 @@ def test_field_points_deep_match_oracle(pkg, oracle, cyl_case, precision):
     pts = _points(cyl_case, np.random.default_rng(5))
     got = s.field_points(pts, kind=0, isol=1)
     ref = _oracle_pot(oracle, cyl_case, pts, w, mx)
+    tol = TOL if precision == 0 else MIXED_TOL
     assert got.shape == ref.shape == (len(pts), 6 + 2)
-    assert max_norm_err(got, ref) < TOL
+    assert max_norm_err(got, ref) < tol
     for c in range(got.shape[1]):
-        assert max_norm_err(got[:, c], ref[:, c]) < TOL * 10
+        assert max_norm_err(got[:, c], ref[:, c]) < tol * 10
     # pressure = i w rho pot, elevation = i w / g pot
     v, wk, w1, wvn = pkg.hamsgpu.wave_properties(3, w, -1.0)
     prs = s.field_points(pts, kind=1, isol=1)
@@ -77,7 +81,7 @@ def test_field_points_deep_match_oracle(pkg, oracle, cyl_case, precision):
     # isol = 2 leaves out the incident potential
     g2 = s.field_points(pts, kind=0, isol=2)
     assert np.array_equal(g2[:, :6], got[:, :6])
-    assert max_norm_err(g2, _oracle_pot(oracle, cyl_case, pts, w, mx, isol=2)) < TOL
+    assert max_norm_err(g2, _oracle_pot(oracle, cyl_case, pts, w, mx, isol=2)) < tol
     s.close()
 
 
@@ -90,20 +94,21 @@ def test_centroids_reproduce_solved_potential(pkg, cyl_case):
     s.close()
 
 
-def test_field_points_chunked(pkg, oracle, cyl_case):
-    """More points than one 2048-row chunk."""
-    s = gpu_solver(pkg, cyl_case, 0)
+@pytest.mark.parametrize("precision", [0, 1])
+def test_field_points_chunked(pkg, oracle, cyl_case, precision):
+    """More points than one 2048-row chunk (the second chunk has an odd row count)."""
+    s = gpu_solver(pkg, cyl_case, precision)
     w = 0.6
     amas, bdmp, exfc, mx = gpu_frequency(pkg, s, cyl_case, w)
     g = np.linspace(-60.0, 60.0, 47)
     X, Y = np.meshgrid(g, g, indexing="ij")
     pts = np.column_stack([X.ravel(), Y.ravel() + 0.37, np.zeros(X.size)])
-    pts = pts[np.hypot(pts[:, 0], pts[:, 1]) > 6.0]
-    assert len(pts) > 2048
+    pts = pts[np.hypot(pts[:, 0], pts[:, 1]) > 6.0][:2191]
+    assert len(pts) > 2048 and (len(pts) - 2048) % 2 == 1
     got = s.field_points(pts, kind=2, isol=1)
     ref = _oracle_pot(oracle, cyl_case, pts, w, mx)
     v, wk, w1, wvn = pkg.hamsgpu.wave_properties(3, w, -1.0)
-    assert max_norm_err(got, 1j * w1 / 9.80665 * ref) < TOL
+    assert max_norm_err(got, 1j * w1 / 9.80665 * ref) < (TOL if precision == 0 else MIXED_TOL)
     s.close()
 
 
