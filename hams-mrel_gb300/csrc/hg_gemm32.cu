@@ -9,6 +9,7 @@
 // single stage and the CTA also prefetches its C tile into shared memory
 // together with A and B, so the read of C overlaps the multiply; two CTAs
 // share an SM so that one CTA's stores overlap the other's arithmetic.
+#include <mutex>
 #include "hg_linalg.cuh"
 #include "hg_tma.cuh"
 
@@ -232,7 +233,11 @@ cudaError_t launch_wide(cudaStream_t st, int m, int n, int k, float2 alpha, cons
 // stages double-buffered by cp.async.  Small tiles give enough CTAs to
 // fill the GPU without splitting K.
 // ---------------------------------------------------------------------------
-constexpr int kSRows = 32, kSK = 32, kSThreads = 256, kSMaxCW = 48, kSStages = 2;
+// Four stages in flight (80 KB of dynamic shared memory at 48 columns): the
+// products this kernel serves (a 256-deep block of L or U times the
+// right-hand sides) read their A block once from HBM, so the copies in
+// flight per SM, not the FMAs, set their speed.
+constexpr int kSRows = 32, kSK = 32, kSThreads = 256, kSMaxCW = 48, kSStages = 4;
 
 template <int CPT, bool VEC>
 __device__ __forceinline__ void skinny_stage(float2* As, float2* Bs, const float2* __restrict__ A, long lda,
@@ -272,8 +277,9 @@ __global__ void __launch_bounds__(kSThreads)
 k_cgemm_skinny(int m, int n, int k, float2 alpha, const float2* __restrict__ A, long lda,
                const float2* __restrict__ B, long ldb, float2 beta, float2* __restrict__ C, long ldc) {
   constexpr int CW = 8 * CPT;
-  __shared__ __align__(16) float2 As[kSStages][kSK * kSRows];
-  __shared__ __align__(16) float2 Bs[kSStages][kSK * CW];
+  extern __shared__ __align__(16) float2 s_skinny[];
+  float2* As = s_skinny;                            // [kSStages][kSK * kSRows]
+  float2* Bs = s_skinny + kSStages * kSK * kSRows;  // [kSStages][kSK * CW]
   const int tid = threadIdx.x, tx = tid & 31, cg = tid >> 5;
   const int m0 = blockIdx.x * kSRows;
   float ar[CPT], ai[CPT];
@@ -282,7 +288,8 @@ k_cgemm_skinny(int m, int n, int k, float2 alpha, const float2* __restrict__ A, 
   const int nst = (k + kSK - 1) / kSK;
 #pragma unroll
   for (int s = 0; s < kSStages - 1; ++s) {
-    if (s < nst) skinny_stage<CPT, VEC>(As[s], Bs[s], A, lda, B, ldb, m, n, k, m0, s * kSK, tid);
+    if (s < nst)
+      skinny_stage<CPT, VEC>(As + s * kSK * kSRows, Bs + s * kSK * CW, A, lda, B, ldb, m, n, k, m0, s * kSK, tid);
     cp_async_commit();
   }
   for (int s = 0; s < nst; ++s) {
@@ -290,10 +297,12 @@ k_cgemm_skinny(int m, int n, int k, float2 alpha, const float2* __restrict__ A, 
     cp_async_wait<kSStages - 2>();
     __syncthreads();  // stage s landed; the buffer of stage s - 1 is free again
     const int sn = s + kSStages - 1;
-    if (sn < nst) skinny_stage<CPT, VEC>(As[sn % kSStages], Bs[sn % kSStages], A, lda, B, ldb, m, n, k, m0, sn * kSK, tid);
+    if (sn < nst)
+      skinny_stage<CPT, VEC>(As + (sn % kSStages) * kSK * kSRows, Bs + (sn % kSStages) * kSK * CW, A, lda, B, ldb, m,
+                             n, k, m0, sn * kSK, tid);
     cp_async_commit();
-    const float2* as = As[b];
-    const float2* bs = Bs[b] + cg * CPT;
+    const float2* as = As + b * kSK * kSRows;
+    const float2* bs = Bs + b * kSK * CW + cg * CPT;
 #pragma unroll 4
     for (int l = 0; l < kSK; ++l) {
       const float2 a = as[l * kSRows + tx];
@@ -325,15 +334,33 @@ k_cgemm_skinny(int m, int n, int k, float2 alpha, const float2* __restrict__ A, 
   }
 }
 
+template <int CPT, bool VEC>
+cudaError_t launch_skinny_v(cudaStream_t st, int m, int n, int k, float2 alpha, const float2* A, long lda,
+                            const float2* B, long ldb, float2 beta, float2* C, long ldc) {
+  constexpr size_t smem = (size_t)kSStages * kSK * (kSRows + 8 * CPT) * sizeof(float2);
+  static bool done[64] = {false};
+  static std::mutex mu;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 0 || dev >= 64 || !done[dev]) {
+      e = cudaFuncSetAttribute(k_cgemm_skinny<CPT, VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      if (dev >= 0 && dev < 64) done[dev] = true;
+    }
+  }
+  const dim3 grid((m + kSRows - 1) / kSRows);
+  k_cgemm_skinny<CPT, VEC><<<grid, kSThreads, smem, st>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  return cudaGetLastError();
+}
+
 template <int CPT>
 cudaError_t launch_skinny(cudaStream_t st, bool vec, int m, int n, int k, float2 alpha, const float2* A, long lda,
                           const float2* B, long ldb, float2 beta, float2* C, long ldc) {
-  const dim3 grid((m + kSRows - 1) / kSRows);
-  if (vec)
-    k_cgemm_skinny<CPT, true><<<grid, kSThreads, 0, st>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
-  else
-    k_cgemm_skinny<CPT, false><<<grid, kSThreads, 0, st>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
-  return cudaGetLastError();
+  if (vec) return launch_skinny_v<CPT, true>(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  return launch_skinny_v<CPT, false>(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
 }
 
 }  // namespace

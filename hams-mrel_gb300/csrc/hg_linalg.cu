@@ -299,32 +299,119 @@ __global__ void k_laswp(T* A, long lda, int ncols, const int* ipiv, int r0, int 
   }
 }
 
-// X = L^{-1} X for the unit-lower jb x jb block L (lda) and ncols columns of X (ldx).
+template <typename T> __device__ __forceinline__ T shfl_c(T v, int src) {
+  v.x = __shfl_sync(0xffffffffu, v.x, src);
+  v.y = __shfl_sync(0xffffffffu, v.y, src);
+  return v;
+}
+
+// After the panel at rows/columns [k, k + jb): the row interchanges
+// ipiv[k..k+jb) on the other columns of [c0, c1), and X = L11^-1 X on the
+// columns right of the panel (L11 the panel's unit-lower jb x jb block), in
+// one pass: one warp per column.  The jb interchanges (in LAPACK's order)
+// are first composed into labels: lane r learns which row's value ends up in
+// block row k + r, and up to jb "outside" slots (rows below the block that
+// an interchange touched) learn theirs; every warp composes them for itself
+// (jb shuffle steps).  A column's values are then read once (all reads
+// before any write) and written to their final rows, and lanes r > c
+// subtract L(r, c) x_c for c = 0 .. jb - 2 with x_c shuffled from lane c.
 template <typename T>
-__global__ void k_trsm_lower_unit(const T* L, long lda, int jb, T* X, long ldx, int ncols) {
-  __shared__ T sl[kNB][kNB + 1];
-  for (int e = threadIdx.x; e < jb * jb; e += blockDim.x) {
-    const int r = e % jb, c = e / jb;
-    sl[r][c] = L[r + (long)c * lda];
+__global__ void __launch_bounds__(256)
+k_swap_trsm(T* __restrict__ A, long lda, int c0, int c1, int k, int jb, const int* __restrict__ ipiv) {
+  __shared__ T Ls[kNB][kNB + 1];  // Ls[c][r] = L(r, c)
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (c1 > k + jb) {
+    for (int e = tid; e < jb * jb; e += blockDim.x) {
+      const int r = e % jb, c = e / jb;
+      Ls[c][r] = A[(k + r) + (long)(k + c) * lda];
+    }
   }
+  const int tl = (lane < jb) ? ipiv[k + lane] - 1 - k : lane;  // relative target of interchange `lane`
+  int blab = lane;          // row (relative to k) whose value ends in block row lane
+  int opos = -1, olab = 0;  // outside slot of this lane: its row and the row whose value ends there
+  int nused = 0;
+  for (int r = 0; r < jb; ++r) {
+    const int t = __shfl_sync(0xffffffffu, tl, r);
+    if (t == r) continue;
+    int s;
+    int b;
+    if (t < jb) {
+      s = -1;
+      b = __shfl_sync(0xffffffffu, blab, t);
+    } else {
+      const unsigned m = __ballot_sync(0xffffffffu, opos == t);
+      if (m) {
+        s = __ffs(m) - 1;
+      } else {
+        s = nused++;
+        if (lane == s) { opos = t; olab = t; }
+      }
+      b = __shfl_sync(0xffffffffu, olab, s);
+    }
+    const int a = __shfl_sync(0xffffffffu, blab, r);
+    if (lane == r) blab = b;
+    if (s < 0) {
+      if (lane == t) blab = a;
+    } else if (lane == s) {
+      olab = a;
+    }
+  }
+  __syncthreads();  // Ls
+  const int ncols = c1 - c0 - jb;
+  const int q = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (q >= ncols) return;
+  const int col = (c0 + q < k) ? c0 + q : c0 + q + jb;
+  T* x = A + (long)col * lda + k;
+  T v, ov;
+  v.x = 0; v.y = 0; ov = v;
+  if (lane < jb) v = x[blab];
+  if (lane < nused) ov = x[olab];
+  __syncwarp();
+  if (col > k) {
+    for (int c = 0; c + 1 < jb; ++c) {
+      const T xc = shfl_c(v, c);
+      if (lane > c && lane < jb) v = csub(v, cmul(Ls[c][lane], xc));
+    }
+  }
+  if (lane < jb) x[lane] = v;
+  if (lane < nused) x[opos] = ov;
+}
+
+// The row permutation of a whole factorisation: perm[r] = the original row
+// whose value the pivots (LAPACK order, ipiv 1-based) bring to row r.  One
+// thread follows one original row x: interchange r moves the value at row r
+// to ipiv[r] and the value at ipiv[r] up to r, and a value that has moved up
+// to row r (or sits at r once interchange r is done) never moves again.
+__global__ void k_perm_trace(int n, const int* __restrict__ ipiv, int* __restrict__ perm) {
+  extern __shared__ int s_piv[];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s_piv[i] = ipiv[i] - 1;
   __syncthreads();
-  const int col = blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= ncols) return;
-  T x[kNB];
-  T* xc = X + (long)col * ldx;
-#pragma unroll
-  for (int r = 0; r < kNB; ++r)
-    if (r < jb) x[r] = xc[r];
-#pragma unroll
-  for (int r = 0; r < kNB; ++r) {
-    if (r >= jb) break;
-#pragma unroll
-    for (int c = 0; c < kNB; ++c)
-      if (c < r) x[r] = csub(x[r], cmul(sl[r][c], x[c]));
+  const int x0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x0 >= n) return;
+  int x = x0;
+  for (int r = 0; r <= x; ++r) {
+    const int p = s_piv[r];
+    if (r == x) {
+      x = p;
+    } else if (p == x) {
+      x = r;
+      break;
+    }
   }
-#pragma unroll
-  for (int r = 0; r < kNB; ++r)
-    if (r < jb) xc[r] = x[r];
+  perm[x] = x0;
+}
+
+// dst[r, c] = src[perm[r], c]
+__global__ void k_gather_rows(int n, int nc, const int* __restrict__ perm, const float2* __restrict__ src, long lds,
+                              float2* __restrict__ dst, long ldd) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+  if (r < n && c < nc) dst[r + (long)c * ldd] = src[perm[r] + (long)c * lds];
+}
+
+__global__ void k_copy_cols(int n, int nc, const float2* __restrict__ src, long lds, float2* __restrict__ dst,
+                            long ldd) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+  if (r < n && c < nc) dst[r + (long)c * ldd] = src[r + (long)c * lds];
 }
 
 // X = U^{-1} X for the non-unit upper jb x jb block U.
@@ -372,9 +459,12 @@ constexpr int kTcMinN = 1024;
 //   linv  L_kk^-1 of every 256-wide diagonal block (256 x 256 each, kept for getrs_inv)
 //   uinv  U_kk^-1 of every diagonal block
 //   y     the intermediate solution of getrs_inv (n x kSolveChunk)
+//   perm  the row permutation of the pivots (n ints, for getrs_inv)
 constexpr int kSolveChunk = 64;
+// Largest order whose pivots k_perm_trace composes in shared memory.
+constexpr int kPermMaxN = 48 * 1024;
 struct LuWork {
-  size_t tc, minv, linv, uinv, y, total;
+  size_t tc, minv, linv, uinv, y, perm, total;
   explicit LuWork(int n) {
     const size_t blk = (size_t)kOuterNB * kOuterNB * sizeof(float2);
     const size_t nblk = (size_t)((n + kOuterNB - 1) / kOuterNB);
@@ -384,7 +474,8 @@ struct LuWork {
     linv = minv + blk;
     uinv = linv + nblk * blk;
     y = uinv + nblk * blk;
-    total = y + up((size_t)n * kSolveChunk * sizeof(float2));
+    perm = y + up((size_t)n * kSolveChunk * sizeof(float2));
+    total = perm + up((size_t)n * sizeof(int));
   }
 };
 
@@ -417,12 +508,10 @@ cudaError_t factor_columns(cudaStream_t st, bool use_cluster, int n, typename cx
     const int jb = (c1 - k < kNB) ? c1 - k : kNB;
     cudaError_t e = panel<R>(st, use_cluster, n, A, lda, k, jb, ipiv, info);
     if (e != cudaSuccess) return e;
-    const int w = c1 - c0;
-    k_laswp<T><<<(w + 127) / 128, 128, 0, st>>>(A + (long)c0 * lda, lda, w, ipiv, k, k + jb, k - c0, k - c0 + jb);
+    const int other = c1 - c0 - jb;
+    if (other > 0) k_swap_trsm<T><<<(other + 7) / 8, 256, 0, st>>>(A, lda, c0, c1, k, jb, ipiv);
     const int rest = c1 - k - jb;
     if (rest > 0) {
-      k_trsm_lower_unit<T><<<(rest + 127) / 128, 128, 0, st>>>(A + k + (long)k * lda, lda, jb,
-                                                                 A + k + (long)(k + jb) * lda, lda, rest);
       e = gemm<R>(st, false, n - k - jb, rest, jb, mone, A + (k + jb) + (long)k * lda, lda,
                   A + k + (long)(k + jb) * lda, lda, one, A + (k + jb) + (long)(k + jb) * lda, lda);
       if (e != cudaSuccess) return e;
@@ -537,6 +626,15 @@ cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* i
       if (e != cudaSuccess) return e;
     }
   }
+  // the pivots as one row permutation (getrs_inv gathers the right-hand sides by it)
+  if (n <= kPermMaxN) {
+    const size_t ps = (size_t)n * sizeof(int);
+    if (ps > 48 * 1024) {
+      e = cudaFuncSetAttribute(k_perm_trace, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ps);
+      if (e != cudaSuccess) return e;
+    }
+    k_perm_trace<<<(n + 255) / 256, 256, ps, st>>>(n, ipiv, reinterpret_cast<int*>(wb + lw.perm));
+  }
   // U_kk^-1 of every diagonal block, in one launch
   return trsm_inverse_blocks<float>(st, true, reinterpret_cast<const float2*>(A), lda, n, kOuterNB,
                                     reinterpret_cast<float2*>(wb + lw.uinv), kOuterNB, 0, (n + kOuterNB - 1) / kOuterNB);
@@ -563,10 +661,16 @@ cudaError_t getrs_inv(cudaStream_t st, int n, int nrhs, const float2* LU, long l
   const size_t blk = (size_t)kOuterNB * kOuterNB;
   const float2 mone = make_float2(-1.f, 0.f), one = make_float2(1.f, 0.f);
   const int nblk = (n + kOuterNB - 1) / kOuterNB;
-  k_laswp<float2><<<(nrhs + 127) / 128, 128, 0, st>>>(B, ldb, nrhs, ipiv, 0, n, 0, 0);
+  const int* perm = reinterpret_cast<const int*>(wb + lw.perm);
+  if (n > kPermMaxN) k_laswp<float2><<<(nrhs + 127) / 128, 128, 0, st>>>(B, ldb, nrhs, ipiv, 0, n, 0, 0);
   for (int c0 = 0; c0 < nrhs; c0 += kSolveChunk) {
     const int nc = (nrhs - c0 < kSolveChunk) ? nrhs - c0 : kSolveChunk;
     float2* Bc = B + (long)c0 * ldb;
+    if (n <= kPermMaxN) {  // Bc = P Bc through Y
+      const dim3 g((n + 255) / 256, nc);
+      k_gather_rows<<<g, 256, 0, st>>>(n, nc, perm, Bc, ldb, Y, n);
+      k_copy_cols<<<g, 256, 0, st>>>(n, nc, Y, n, Bc, ldb);
+    }
     for (int b = 0; b < nblk; ++b) {
       const int K = b * kOuterNB, jb = (n - K < kOuterNB) ? n - K : kOuterNB;
       k_apply_inv<<<dim3((jb + 31) / 32, (nc + 7) / 8), 256, 0, st>>>(jb, nc, Linv + b * blk, Bc + K, ldb, Y + K, n);
