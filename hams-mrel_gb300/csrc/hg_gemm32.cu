@@ -238,6 +238,11 @@ cudaError_t launch_wide(cudaStream_t st, int m, int n, int k, float2 alpha, cons
 // right-hand sides) read their A block once from HBM, so the copies in
 // flight per SM, not the FMAs, set their speed.
 constexpr int kSRows = 32, kSK = 32, kSThreads = 256, kSMaxCW = 48, kSStages = 4;
+// Row stride of the B stage in shared memory: CW + 2 complex, so that the
+// 32 consecutive k of one column that a warp copies land on 8 bank pairs
+// (4-way) instead of one (32-way at the bare 48-column stride), and rows
+// stay 16-byte aligned for the paired reads.
+template <int CPT> constexpr int skinny_bstride() { return 8 * CPT + 2; }
 
 template <int CPT, bool VEC>
 __device__ __forceinline__ void skinny_stage(float2* As, float2* Bs, const float2* __restrict__ A, long lda,
@@ -268,7 +273,7 @@ __device__ __forceinline__ void skinny_stage(float2* As, float2* Bs, const float
     const int l = e % kSK, c = e / kSK;
     const int gk = k0 + l;
     const bool ok = c < n && gk < k;
-    cp_async8(Bs + l * CW + c, ok ? B + gk + (long)c * ldb : B, ok);
+    cp_async8(Bs + l * skinny_bstride<CPT>() + c, ok ? B + gk + (long)c * ldb : B, ok);
   }
 }
 
@@ -276,10 +281,10 @@ template <int CPT, bool VEC>
 __global__ void __launch_bounds__(kSThreads)
 k_cgemm_skinny(int m, int n, int k, float2 alpha, const float2* __restrict__ A, long lda,
                const float2* __restrict__ B, long ldb, float2 beta, float2* __restrict__ C, long ldc) {
-  constexpr int CW = 8 * CPT;
+  constexpr int BST = skinny_bstride<CPT>();
   extern __shared__ __align__(16) float2 s_skinny[];
   float2* As = s_skinny;                            // [kSStages][kSK * kSRows]
-  float2* Bs = s_skinny + kSStages * kSK * kSRows;  // [kSStages][kSK * CW]
+  float2* Bs = s_skinny + kSStages * kSK * kSRows;  // [kSStages][kSK * BST]
   const int tid = threadIdx.x, tx = tid & 31, cg = tid >> 5;
   const int m0 = blockIdx.x * kSRows;
   float ar[CPT], ai[CPT];
@@ -289,7 +294,7 @@ k_cgemm_skinny(int m, int n, int k, float2 alpha, const float2* __restrict__ A, 
 #pragma unroll
   for (int s = 0; s < kSStages - 1; ++s) {
     if (s < nst)
-      skinny_stage<CPT, VEC>(As + s * kSK * kSRows, Bs + s * kSK * CW, A, lda, B, ldb, m, n, k, m0, s * kSK, tid);
+      skinny_stage<CPT, VEC>(As + s * kSK * kSRows, Bs + s * kSK * BST, A, lda, B, ldb, m, n, k, m0, s * kSK, tid);
     cp_async_commit();
   }
   for (int s = 0; s < nst; ++s) {
@@ -298,17 +303,17 @@ k_cgemm_skinny(int m, int n, int k, float2 alpha, const float2* __restrict__ A, 
     __syncthreads();  // stage s landed; the buffer of stage s - 1 is free again
     const int sn = s + kSStages - 1;
     if (sn < nst)
-      skinny_stage<CPT, VEC>(As + (sn % kSStages) * kSK * kSRows, Bs + (sn % kSStages) * kSK * CW, A, lda, B, ldb, m,
-                             n, k, m0, sn * kSK, tid);
+      skinny_stage<CPT, VEC>(As + (sn % kSStages) * kSK * kSRows, Bs + (sn % kSStages) * kSK * BST, A, lda, B, ldb,
+                             m, n, k, m0, sn * kSK, tid);
     cp_async_commit();
     const float2* as = As + b * kSK * kSRows;
-    const float2* bs = Bs + b * kSK * CW + cg * CPT;
+    const float2* bs = Bs + b * kSK * BST + cg * CPT;
 #pragma unroll 4
     for (int l = 0; l < kSK; ++l) {
       const float2 a = as[l * kSRows + tx];
 #pragma unroll
       for (int j = 0; j < CPT; j += 2) {
-        const float4 bb = *reinterpret_cast<const float4*>(bs + l * CW + j);
+        const float4 bb = *reinterpret_cast<const float4*>(bs + l * BST + j);
         ar[j] = fmaf(a.x, bb.x, ar[j]);
         ar[j] = fmaf(-a.y, bb.y, ar[j]);
         ai[j] = fmaf(a.x, bb.y, ai[j]);
@@ -337,7 +342,7 @@ k_cgemm_skinny(int m, int n, int k, float2 alpha, const float2* __restrict__ A, 
 template <int CPT, bool VEC>
 cudaError_t launch_skinny_v(cudaStream_t st, int m, int n, int k, float2 alpha, const float2* A, long lda,
                             const float2* B, long ldb, float2 beta, float2* C, long ldc) {
-  constexpr size_t smem = (size_t)kSStages * kSK * (kSRows + 8 * CPT) * sizeof(float2);
+  constexpr size_t smem = (size_t)kSStages * kSK * (kSRows + skinny_bstride<CPT>()) * sizeof(float2);
   static bool done[64] = {false};
   static std::mutex mu;
   int dev = 0;

@@ -315,9 +315,12 @@ template <typename T> __device__ __forceinline__ T shfl_c(T v, int src) {
 // (jb shuffle steps).  A column's values are then read once (all reads
 // before any write) and written to their final rows, and lanes r > c
 // subtract L(r, c) x_c for c = 0 .. jb - 2 with x_c shuffled from lane c.
+// perm (optional): the running row permutation of the factorisation, one
+// more column (of row numbers) that takes the same interchanges.
 template <typename T>
 __global__ void __launch_bounds__(256)
-k_swap_trsm(T* __restrict__ A, long lda, int c0, int c1, int k, int jb, const int* __restrict__ ipiv) {
+k_swap_trsm(T* __restrict__ A, long lda, int c0, int c1, int k, int jb, const int* __restrict__ ipiv,
+            int* __restrict__ perm) {
   __shared__ T Ls[kNB][kNB + 1];  // Ls[c][r] = L(r, c)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (c1 > k + jb) {
@@ -359,6 +362,15 @@ k_swap_trsm(T* __restrict__ A, long lda, int c0, int c1, int k, int jb, const in
   __syncthreads();  // Ls
   const int ncols = c1 - c0 - jb;
   const int q = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (perm && q == ncols) {
+    int* x = perm + k;
+    const int v = (lane < jb) ? x[blab] : 0;
+    const int ov = (lane < nused) ? x[olab] : 0;
+    __syncwarp();
+    if (lane < jb) x[lane] = v;
+    if (lane < nused) x[opos] = ov;
+    return;
+  }
   if (q >= ncols) return;
   const int col = (c0 + q < k) ? c0 + q : c0 + q + jb;
   T* x = A + (long)col * lda + k;
@@ -377,28 +389,9 @@ k_swap_trsm(T* __restrict__ A, long lda, int c0, int c1, int k, int jb, const in
   if (lane < nused) x[opos] = ov;
 }
 
-// The row permutation of a whole factorisation: perm[r] = the original row
-// whose value the pivots (LAPACK order, ipiv 1-based) bring to row r.  One
-// thread follows one original row x: interchange r moves the value at row r
-// to ipiv[r] and the value at ipiv[r] up to r, and a value that has moved up
-// to row r (or sits at r once interchange r is done) never moves again.
-__global__ void k_perm_trace(int n, const int* __restrict__ ipiv, int* __restrict__ perm) {
-  extern __shared__ int s_piv[];
-  for (int i = threadIdx.x; i < n; i += blockDim.x) s_piv[i] = ipiv[i] - 1;
-  __syncthreads();
-  const int x0 = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x0 >= n) return;
-  int x = x0;
-  for (int r = 0; r <= x; ++r) {
-    const int p = s_piv[r];
-    if (r == x) {
-      x = p;
-    } else if (p == x) {
-      x = r;
-      break;
-    }
-  }
-  perm[x] = x0;
+__global__ void k_iota(int n, int* __restrict__ perm) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n) perm[r] = r;
 }
 
 // dst[r, c] = src[perm[r], c]
@@ -459,10 +452,9 @@ constexpr int kTcMinN = 1024;
 //   linv  L_kk^-1 of every 256-wide diagonal block (256 x 256 each, kept for getrs_inv)
 //   uinv  U_kk^-1 of every diagonal block
 //   y     the intermediate solution of getrs_inv (n x kSolveChunk)
-//   perm  the row permutation of the pivots (n ints, for getrs_inv)
+//   perm  the row permutation of the pivots (n ints, for getrs_inv): perm[r]
+//         is the original row that the interchanges bring to row r
 constexpr int kSolveChunk = 64;
-// Largest order whose pivots k_perm_trace composes in shared memory.
-constexpr int kPermMaxN = 48 * 1024;
 struct LuWork {
   size_t tc, minv, linv, uinv, y, perm, total;
   explicit LuWork(int n) {
@@ -500,7 +492,7 @@ cudaError_t panel(cudaStream_t st, bool use_cluster, int n, typename cx<R>::T* A
 // 32-wide panels (pivots applied only inside [c0, c1)).
 template <typename R>
 cudaError_t factor_columns(cudaStream_t st, bool use_cluster, int n, typename cx<R>::T* A, long lda, int c0, int c1,
-                           int* ipiv, int* info) {
+                           int* ipiv, int* info, int* perm = nullptr) {
   typedef typename cx<R>::T T;
   T mone, one;
   mone.x = -1; mone.y = 0; one.x = 1; one.y = 0;
@@ -508,8 +500,8 @@ cudaError_t factor_columns(cudaStream_t st, bool use_cluster, int n, typename cx
     const int jb = (c1 - k < kNB) ? c1 - k : kNB;
     cudaError_t e = panel<R>(st, use_cluster, n, A, lda, k, jb, ipiv, info);
     if (e != cudaSuccess) return e;
-    const int other = c1 - c0 - jb;
-    if (other > 0) k_swap_trsm<T><<<(other + 7) / 8, 256, 0, st>>>(A, lda, c0, c1, k, jb, ipiv);
+    const int other = c1 - c0 - jb + (perm ? 1 : 0);
+    if (other > 0) k_swap_trsm<T><<<(other + 7) / 8, 256, 0, st>>>(A, lda, c0, c1, k, jb, ipiv, perm);
     const int rest = c1 - k - jb;
     if (rest > 0) {
       e = gemm<R>(st, false, n - k - jb, rest, jb, mone, A + (k + jb) + (long)k * lda, lda,
@@ -555,10 +547,13 @@ k_apply_inv(int jb, int nc, const float2* __restrict__ M, const float2* __restri
   for (int j = 0; j < 8; ++j) { ar[j] = 0.f; ai[j] = 0.f; }
   const int p0 = w * 32;
   if (r < jb) {
-#pragma unroll 8
+    float2 mv[32];  // all 32 loads of M in flight at once
+#pragma unroll
+    for (int q = 0; q < 32; ++q) mv[q] = (p0 + q < jb) ? M[r + (long)(p0 + q) * kOuterNB] : make_float2(0.f, 0.f);
+#pragma unroll
     for (int q = 0; q < 32; ++q) {
       const int p = p0 + q;
-      const float2 m = (p < jb) ? M[r + (long)p * kOuterNB] : make_float2(0.f, 0.f);
+      const float2 m = mv[q];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const float2 x = xs[p][j];
@@ -601,10 +596,12 @@ cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* i
   const size_t tcb = lw.minv;
   char* wb = static_cast<char*>(work);
   float2* Minv = reinterpret_cast<float2*>(wb + lw.minv);
+  int* perm = reinterpret_cast<int*>(wb + lw.perm);
+  k_iota<<<(n + 255) / 256, 256, 0, st>>>(n, perm);
   const size_t blk = (size_t)kOuterNB * kOuterNB;
   for (int K = 0; K < n; K += kOuterNB) {
     const int jbo = (n - K < kOuterNB) ? n - K : kOuterNB;
-    e = factor_columns<R>(st, use_cluster, n, A, lda, K, K + jbo, ipiv, info);
+    e = factor_columns<R>(st, use_cluster, n, A, lda, K, K + jbo, ipiv, info, perm);
     if (e != cudaSuccess) return e;
     k_laswp<T><<<(n + 127) / 128, 128, 0, st>>>(A, lda, n, ipiv, K, K + jbo, K, K + jbo);
     // inverse of this diagonal block's unit-lower triangle (for U12 here and
@@ -625,15 +622,6 @@ cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* i
                    A12, lda, reinterpret_cast<float2*>(A + (K + jbo) + (long)(K + jbo) * lda), lda, work, tcb, info);
       if (e != cudaSuccess) return e;
     }
-  }
-  // the pivots as one row permutation (getrs_inv gathers the right-hand sides by it)
-  if (n <= kPermMaxN) {
-    const size_t ps = (size_t)n * sizeof(int);
-    if (ps > 48 * 1024) {
-      e = cudaFuncSetAttribute(k_perm_trace, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ps);
-      if (e != cudaSuccess) return e;
-    }
-    k_perm_trace<<<(n + 255) / 256, 256, ps, st>>>(n, ipiv, reinterpret_cast<int*>(wb + lw.perm));
   }
   // U_kk^-1 of every diagonal block, in one launch
   return trsm_inverse_blocks<float>(st, true, reinterpret_cast<const float2*>(A), lda, n, kOuterNB,
@@ -662,11 +650,10 @@ cudaError_t getrs_inv(cudaStream_t st, int n, int nrhs, const float2* LU, long l
   const float2 mone = make_float2(-1.f, 0.f), one = make_float2(1.f, 0.f);
   const int nblk = (n + kOuterNB - 1) / kOuterNB;
   const int* perm = reinterpret_cast<const int*>(wb + lw.perm);
-  if (n > kPermMaxN) k_laswp<float2><<<(nrhs + 127) / 128, 128, 0, st>>>(B, ldb, nrhs, ipiv, 0, n, 0, 0);
   for (int c0 = 0; c0 < nrhs; c0 += kSolveChunk) {
     const int nc = (nrhs - c0 < kSolveChunk) ? nrhs - c0 : kSolveChunk;
     float2* Bc = B + (long)c0 * ldb;
-    if (n <= kPermMaxN) {  // Bc = P Bc through Y
+    {  // Bc = P Bc through Y
       const dim3 g((n + 255) / 256, nc);
       k_gather_rows<<<g, 256, 0, st>>>(n, nc, perm, Bc, ldb, Y, n);
       k_copy_cols<<<g, 256, 0, st>>>(n, nc, Y, n, Bc, ldb);

@@ -84,9 +84,9 @@ k_getf2_cluster(typename cx<R>::T* __restrict__ P, long lda, int m, int jb, int 
     const int r = e % rl, c = e / rl;
     tile[c * rpc + r] = P[(r0 + r) + (long)c * lda];
   }
-  // row 0 of the panel for column 0's publication
+  __syncthreads();  // the tile is complete before any thread reads another thread's elements
+  // row 0 of the panel for column 0's publication (read remotely after the first cluster barrier)
   if (rank == 0 && tid < jb) pub_jrow[0][tid] = tile[tid * rpc];
-  __syncthreads();
 
   for (int jj = 0; jj < jb; ++jj) {
     const int q = jj & 1;

@@ -26,6 +26,7 @@ EXPORTS = [
     "hg_bench_gemm", "hg_green_points_noalloc", "hg_gesv", "hg_gemm_check",
     "hg_solve_sweep", "hg_gmres_iterations", "hg_solve_footprint", "hg_server_create", "hg_server_submit",
     "hg_server_wait", "hg_server_stats", "hg_server_last_error", "hg_server_destroy", "hg_field_points",
+    "hg_case_read", "hg_case_free", "hg_case_info", "hg_case_arrays", "hg_case_run", "hg_case_write",
 ]
 
 
@@ -120,6 +121,14 @@ def load(build_if_missing: bool = True):
                                      c_void_p]
     L.hg_panel_geometry.argtypes = [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_void_p]
+    L.hg_case_read.argtypes = [ctypes.c_char_p, P(c_void_p), ctypes.c_char_p, c_int]
+    L.hg_case_free.argtypes = [c_void_p]
+    L.hg_case_free.restype = None
+    L.hg_case_info.argtypes = [c_void_p, c_void_p, c_void_p]
+    L.hg_case_arrays.argtypes = [c_void_p] + [c_void_p] * 11
+    L.hg_case_run.argtypes = [c_void_p, ctypes.c_char_p, P(HgOpts), c_int, ctypes.c_char_p, c_int]
+    L.hg_case_write.argtypes = [c_void_p, ctypes.c_char_p, c_void_p, c_void_p, c_void_p, c_double, c_double,
+                                ctypes.c_char_p, c_int]
     _LIB = L
     return L
 
@@ -475,3 +484,67 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+class Case:
+    """A HAMS input deck (ControlFile.in and meshes) read by the library
+    (hg_case_*): inspect what was read, run every frequency on the GPU and
+    write the HAMS- and WAMIT-format result files."""
+
+    def __init__(self, input_dir):
+        self.L = load()
+        self.h = ctypes.c_void_p()
+        err = ctypes.create_string_buffer(512)
+        rc = self.L.hg_case_read(os.fsencode(input_dir), ctypes.byref(self.h), err, len(err))
+        if rc != 0:
+            self.h = None
+            raise HamsGpuError(rc, err.value.decode())
+        info = np.zeros(12, dtype=np.int32)
+        dinfo = np.zeros(2)
+        self.L.hg_case_info(self.h, _ptr(info), _ptr(dinfo))
+        keys = ["n", "nl", "ntnd", "nbody", "nper", "nbeta", "irsp", "isol", "nfp", "sybo", "inft", "ouft"]
+        self.info = {k: int(v) for k, v in zip(keys, info)}
+        self.info["h"], self.info["refl"] = float(dinfo[0]), float(dinfo[1])
+
+    def arrays(self):
+        i = self.info
+        n, nl, nt, nb, npr, nbeta = i["n"], i["nl"], i["ntnd"], i["nbody"], i["nper"], i["nbeta"]
+        out = {"nodes": np.zeros((nt, 3), order="F"), "ncon": np.zeros((n, 4), dtype=np.int32, order="F"),
+               "ncn": np.zeros(n, dtype=np.int32), "xyz_p": np.zeros((n, 3), order="F"), "ds": np.zeros(n),
+               "pnsz": np.zeros(n), "dxyz_p": np.zeros((n, 6), order="F"), "lid_xyz_p": np.zeros((nl, 3), order="F"),
+               "body_ranges": np.zeros((nb, 2), dtype=np.int32), "freq": np.zeros((npr, 6)),
+               "headings": np.zeros(nbeta)}
+        self.L.hg_case_arrays(self.h, *[_ptr(out[k]) for k in ("nodes", "ncon", "ncn", "xyz_p", "ds", "pnsz",
+                                                                "dxyz_p", "lid_xyz_p", "body_ranges", "freq",
+                                                                "headings")])
+        return out
+
+    def run(self, output_dir, precision=HG_PREC_FP64, nslots=2, device=0, **opts_kw):
+        opts = HgOpts()
+        self.L.hg_default_opts(ctypes.byref(opts))
+        opts.device, opts.precision = device, precision
+        for k, v in opts_kw.items():
+            setattr(opts, k, v)
+        err = ctypes.create_string_buffer(512)
+        rc = self.L.hg_case_run(self.h, os.fsencode(output_dir), ctypes.byref(opts), int(nslots), err, len(err))
+        if rc != 0:
+            raise HamsGpuError(rc, err.value.decode())
+
+    def write(self, output_dir, amas, bdmp, exfc, rho=1000.0, g=9.80665):
+        """Result files from amas/bdmp (nper, nd, nd) and exfc (nper, nbeta, nd)."""
+        a = np.ascontiguousarray(np.transpose(np.asarray(amas, dtype=np.float64), (0, 2, 1)))
+        b = np.ascontiguousarray(np.transpose(np.asarray(bdmp, dtype=np.float64), (0, 2, 1)))
+        f = np.ascontiguousarray(np.transpose(np.asarray(exfc, dtype=np.complex128), (0, 2, 1)))
+        err = ctypes.create_string_buffer(512)
+        rc = self.L.hg_case_write(self.h, os.fsencode(output_dir), _ptr(a), _ptr(b), _ptr(f), float(rho), float(g),
+                                  err, len(err))
+        if rc != 0:
+            raise HamsGpuError(rc, err.value.decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.hg_case_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

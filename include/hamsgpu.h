@@ -332,6 +332,40 @@ int hg_gemm_check(hg_ctx *ctx, int variant, int m, int n, int k, const double *a
  * last hg_solve_frequency: [0] fill, [1] LU, [2] solves and refinement, [3] forces. */
 int hg_stage_times(const hg_ctx *ctx, float *ms4);
 
+/*
+ * A whole HAMS run from its input deck (the HAMS_Prog executable's work for
+ * NSYS = 1): ControlFile.in, HullMesh[_b].pnl, WaterPlaneMesh[_b].pnl (IRSP =
+ * 1) and gen_mod_<b>_<dof>.txt in input_dir, read as ReadControlFile
+ * (src/InputFiles.f90:46-224), ReadBodyMesh(Multi) / ReadWTPLMesh(Multi)
+ * (src/ReadPanelMesh.f90, src/ReadPanelMeshMulti.f90) and CalNormals read
+ * them; every frequency of the list solved on the device; results written as
+ * the reference writes them:
+ *   <out>/Hams_format/OAMASS1-6.txt, ODAMPING1-6.txt, OEXFOR1-6.txt
+ *       (RFORCE / EFORCE, src/PotentWavForce.f90:100-218 and the Multi forms)
+ *   <out>/Wamit_format/AmssDamp.1, ExcForce.3 (the same routines, in the
+ *       order they write: per frequency and body pair)
+ *   <out>/Wamit_format/PressureElevation.6p for field points (single body;
+ *       src/PressureElevation.f90:336-470, through hg_field_points)
+ * hg_case_read parses and computes the panel geometry and wave properties
+ * (host only); hg_case_info / hg_case_arrays expose what was read:
+ *   info[12]  = n, nl, ntnd, nbody, nper, nbeta, irsp, isol, nfp, sybo, inft, ouft
+ *   dinfo[2]  = h, refl
+ *   freq[6*nper] = (V, WK, W1, TP, WL, OUFR) per entry
+ * hg_case_run solves and writes (nslots frequencies in flight, as
+ * hg_solve_sweep; one at a time when field points are written).
+ * hg_case_write writes the result files from given A, B, F (per entry
+ * blocks as hg_solve_sweep returns them).  Errors: non-zero return, message
+ * in err[errlen].  Symmetry planes (ISX/ISY) are rejected. */
+typedef struct hg_case hg_case;
+int hg_case_read(const char *input_dir, hg_case **out, char *err, int errlen);
+void hg_case_free(hg_case *c);
+int hg_case_info(const hg_case *c, int *info, double *dinfo);
+int hg_case_arrays(const hg_case *c, double *nodes, int *ncon, int *ncn, double *xyz_p, double *ds, double *pnsz,
+                   double *dxyz_p, double *lid_xyz_p, int *body_ranges, double *freq, double *headings);
+int hg_case_run(hg_case *c, const char *output_dir, const hg_opts *opts, int nslots, char *err, int errlen);
+int hg_case_write(const hg_case *c, const char *output_dir, const double *amas, const double *bdmp,
+                  const double *exfc, double rho, double g, char *err, int errlen);
+
 #ifdef __cplusplus
 }
 #endif

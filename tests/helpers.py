@@ -37,3 +37,85 @@ def gpu_frequency(pkg, solver, case, value, betas_deg=None):
         betas_deg = ctl.headings
     betas = np.array(betas_deg, dtype=np.float64) * np.pi / 180.0
     return solver.solve_frequency(v, wk, w1, ctl.h, wvn, betas, irsp=1 if case.nl > 0 else 0, isol=ctl.isol)
+
+
+def _ulp(tok):
+    """Unit in the last printed place of a Fortran-formatted number."""
+    t = tok.upper()
+    if "E" in t:
+        mant, ex = t.split("E")
+        dec = len(mant.split(".")[1]) if "." in mant else 0
+        return 10.0 ** (int(ex) - dec)
+    if "." in t:
+        return 10.0 ** (-len(t.split(".")[1]))
+    return 0.0
+
+
+def file_values_max(path, first_value, nlines=None):
+    """Largest magnitude among the fields from first_value on."""
+    with open(path) as f:
+        lines = f.read().splitlines()[:nlines]
+    top = 0.0
+    for ln in lines:
+        for t in ln.split()[first_value:]:
+            try:
+                top = max(top, abs(float(t)))
+            except ValueError:
+                pass
+    return top
+
+
+def compare_result_file(got_path, exp_path, nlines=None, floor=1e-6, scale_by="column", first_value=0,
+                        scale_value=None, phase=None, phase_unit=1.0):
+    """Compare two HAMS/WAMIT result files: the same number of lines (or the
+    first nlines), every line of the same length (same edit descriptors), text
+    tokens equal and numbers within one printed unit plus floor x the largest
+    magnitude of their column (scale_by="column") or of all value columns of
+    the file from field first_value on (scale_by="file"), or scale_value
+    for those fields when given.  phase = (magnitude field, phase field):
+    a phase is held to the angle that the floor of its magnitude's column
+    subtends at that magnitude (times phase_unit per radian), since the
+    phase of a near-zero complex number is rounding noise.  Returns (worst
+    excess, lines compared)."""
+    with open(got_path) as f:
+        got = f.read().splitlines()
+    with open(exp_path) as f:
+        exp = f.read().splitlines()
+    if nlines is None:
+        assert len(got) == len(exp), f"{got_path}: {len(got)} lines, expected {len(exp)}"
+        nlines = len(exp)
+    assert len(got) >= nlines and len(exp) >= nlines
+    rows_g = [ln.split() for ln in got[:nlines]]
+    rows_e = [ln.split() for ln in exp[:nlines]]
+    ncol = max(len(r) for r in rows_e)
+    scale = [0.0] * ncol
+    for r in rows_e:
+        for j, t in enumerate(r):
+            try:
+                scale[j] = max(scale[j], abs(float(t)))
+            except ValueError:
+                pass
+    if scale_by == "file":
+        top = max(scale[first_value:]) if ncol > first_value else 0.0
+        if scale_value is not None:
+            top = scale_value
+        scale = [top if j >= first_value else scale[j] for j in range(ncol)]
+    worst = 0.0
+    for i, (lg, le, rg, re_) in enumerate(zip(got, exp, rows_g, rows_e)):
+        assert len(lg) == len(le), f"{got_path}:{i + 1}: line length {len(lg)} != {len(le)}\n{lg}\n{le}"
+        assert len(rg) == len(re_), f"{got_path}:{i + 1}: {len(rg)} fields != {len(re_)}"
+        for j, (a, b) in enumerate(zip(rg, re_)):
+            try:
+                x, y = float(a), float(b)
+            except ValueError:
+                assert a == b, f"{got_path}:{i + 1}: '{a}' != '{b}'"
+                continue
+            if phase is not None and j == phase[1]:
+                mag = max(abs(float(re_[phase[0]])), 1e-300)
+                tol = 1.01 * max(_ulp(a), _ulp(b)) + 2.0 * phase_unit * floor * scale[phase[0]] / mag
+            else:
+                tol = 1.01 * max(_ulp(a), _ulp(b)) + floor * scale[j]
+            excess = abs(x - y) / tol if tol > 0 else (0.0 if x == y else float("inf"))
+            assert excess <= 1.0, f"{got_path}:{i + 1} field {j + 1}: {a} vs {b} (tol {tol:.3g})\n{lg}\n{le}"
+            worst = max(worst, excess)
+    return worst, nlines

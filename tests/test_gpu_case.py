@@ -1,0 +1,137 @@
+"""A whole HAMS run on the GPU from the reference's own input decks
+(hg_case_run): the result files against the files the reference ships
+(pinned frequencies, rules of test_case_io.py) and, for every frequency,
+against the same writer fed the oracle's results (ALL_FREQ_FLOOR of each
+file's largest entry: the finite-depth Green function's extrapolated series
+make both results rounding-dependent, and with irregular-frequency removal
+the normal equations amplify that to 2e-5 at some frequencies of these decks,
+measured between two equally valid FP64 evaluations).  Single-body
+field points: PressureElevation.6p against the oracle's field potential put
+through WamitNondimens (src/PressureElevation.f90:336-385), restated below."""
+import os
+import shutil
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from helpers import compare_result_file
+from test_case_io import FLOOR, NPER_EXPECTED, PINNED, expected_files, scale_rule
+
+pytestmark = pytest.mark.gpu
+
+ALL_FREQ_FLOOR = {"config1": 1e-6, "example5": 1e-4, "example3": 1e-4}
+
+
+@pytest.mark.parametrize("name", ["config1", "example5", "example3"])
+def test_case_run_matches_shipped_and_oracle_files(pkg, oracle, name, tmp_path):
+    d = os.path.join(GOLDEN, name, "input")
+    c = pkg.hamsgpu.Case(d)
+    gpu_dir = os.path.join(tmp_path, "gpu")
+    c.run(gpu_dir, precision=pkg.hamsgpu.HG_PREC_FP64, nslots=2)
+    # shipped files, pinned frequencies
+    nf = PINNED[name]
+    for exp_path, sub, fname in expected_files(name):
+        with open(exp_path) as f:
+            n_exp = len(f.read().splitlines())
+        nl = None if nf == c.info["nper"] == NPER_EXPECTED[name] else n_exp // NPER_EXPECTED[name] * nf
+        compare_result_file(os.path.join(gpu_dir, sub, fname), exp_path, nlines=nl, floor=FLOOR[name],
+                            **scale_rule(os.path.dirname(exp_path), fname, nl))
+    # every frequency against the oracle's results through the same writer
+    case = oracle.load_case(d)
+    freqs = case.ctl.wvnb if name != "example5" else case.ctl.wvnb[:4]
+    res = [oracle.solve_frequency(case, w) for w in freqs]
+    ora_dir = os.path.join(tmp_path, "oracle")
+    amas = np.array([r.amas for r in res])
+    bdmp = np.array([r.bdmp for r in res])
+    exfc = np.array([r.exfc for r in res])
+    pad = c.info["nper"] - len(freqs)
+    if pad:
+        amas = np.concatenate([amas, np.repeat(amas[-1:], pad, axis=0)])
+        bdmp = np.concatenate([bdmp, np.repeat(bdmp[-1:], pad, axis=0)])
+        exfc = np.concatenate([exfc, np.repeat(exfc[-1:], pad, axis=0)])
+    c.write(ora_dir, amas, bdmp, exfc)
+    nper = c.info["nper"]
+    for sub, fname in [("Hams_format", f"{s}{k}.txt") for s in ("OAMASS", "ODAMPING", "OEXFOR") for k in range(1, 7)] + \
+                      [("Wamit_format", "AmssDamp.1"), ("Wamit_format", "ExcForce.3")]:
+        got, ref = os.path.join(gpu_dir, sub, fname), os.path.join(ora_dir, sub, fname)
+        with open(ref) as f:
+            n_ref = len(f.read().splitlines())
+        nl = n_ref // nper * len(freqs)
+        compare_result_file(got, ref, nlines=nl, floor=ALL_FREQ_FLOOR[name],
+                            **scale_rule(os.path.join(ora_dir, sub), fname, nl))
+    c.close()
+
+
+def _nondim(vcp, pressure, diffraction, md, special, w1, refl, rho=1000.0, g=9.80665):
+    """WamitNondimens (src/PressureElevation.f90:336-385), AMP = 1."""
+    nfac = (rho if special else rho * g) if pressure else 1.0
+    if diffraction:
+        r = vcp / nfac
+    else:
+        mexp = 0 if md <= 3 else 1
+        r = vcp / nfac / refl ** (mexp + 1) if special else vcp / nfac * (-1j * w1) / refl ** mexp
+    r = np.where(np.abs(r) < 1e-15, 0.0, r)
+    return (-r.imag - 1j * r.real) if diffraction else (r.real - 1j * r.imag)
+
+
+def test_case_run_field_points_file(pkg, oracle, tmp_path):
+    """example5 with two frequencies and four field points (two below the
+    free surface: pressure; two on it: elevation)."""
+    src = os.path.join(GOLDEN, "example5", "input")
+    d = os.path.join(tmp_path, "deck")
+    shutil.copytree(src, d)
+    pts = np.array([[30.0, 5.0, -4.0], [-12.0, 25.0, -1.5], [40.0, -20.0, 0.0], [0.0, 60.0, 0.0]])
+    with open(os.path.join(d, "ControlFile.in")) as f:
+        lines = f.read().split("\n")
+    out = []
+    for ln in lines:
+        if ln.startswith("    Number_of_frequencies"):
+            ln = ln.replace("-10", " -2")
+        if ln.startswith("    Number_of_headings"):
+            ln = ln.replace("-36", " -3")
+        if ln.startswith("    Number_of_field_points"):
+            out.append(ln[:27] + "%16d" % len(pts))
+            out += ["    %12.4f %12.4f %12.4f    Global_coords_point_%d" % (p[0], p[1], p[2], k + 1)
+                    for k, p in enumerate(pts)]
+            continue
+        out.append(ln)
+    with open(os.path.join(d, "ControlFile.in"), "w") as f:
+        f.write("\n".join(out))
+    c = pkg.hamsgpu.Case(d)
+    assert c.info["nfp"] == 4 and c.info["nper"] == 2 and c.info["nbeta"] == 3
+    c.run(os.path.join(tmp_path, "out"), precision=pkg.hamsgpu.HG_PREC_FP64, nslots=1)
+    with open(os.path.join(tmp_path, "out", "Wamit_format", "PressureElevation.6p")) as f:
+        rows = [ln.split() for ln in f.read().splitlines()]
+    case = oracle.load_case(d)
+    heads = case.ctl.headings
+    betas = np.radians(heads)
+    below = np.abs(pts[:, 2]) > 1e-6
+    nrow = 0
+    for w in case.ctl.wvnb:
+        v, wk, w1, wvn = oracle.wave_properties(case.ctl, w)
+        r = oracle.solve_frequency(case, w)
+        pot = oracle.field_potential(case, pts, v, wk, w1, wvn, betas, r.mxpot, isol=case.ctl.isol)
+        vcp = np.where(below[:, None], 1j * w1 * 1000.0 * pot, 1j * w1 / 9.80665 * pot)
+        scale = np.abs(vcp).max()
+        for p in np.flatnonzero(below):   # radiation lines: points below the free surface only
+            row = rows[nrow]; nrow += 1
+            assert int(row[1]) == p + 1 and abs(float(row[0]) - w1) < 1e-6
+            for md in range(1, 7):
+                z = _nondim(vcp[p, md - 1], True, False, md, False, w1, case.ctl.refl)
+                got = float(row[2 * md]) + 1j * float(row[2 * md + 1])
+                assert abs(got - z) <= 1e-6 * max(abs(z), 1e-12) + 1e-6 * scale * w1 / 9806.65
+        zs = {(p, ib): _nondim(vcp[p, 6 + ib], bool(below[p]), True, 0, False, w1, case.ctl.refl)
+              for ib in range(len(heads)) for p in range(len(pts))}
+        zmax = max(abs(z) for z in zs.values())
+        for ib, b in enumerate(heads):
+            for p in range(len(pts)):
+                row = rows[nrow]; nrow += 1
+                z = zs[(p, ib)]
+                tol = 2e-6 * abs(z) + 1e-6 * zmax
+                assert int(row[2]) == p + 1 and abs(float(row[1]) - b) < 1e-9
+                got = float(row[5]) + 1j * float(row[6])
+                assert abs(got - z) <= tol, (p, b, got, z)
+                assert abs(float(row[3]) - abs(z)) <= tol
+    assert nrow == len(rows)
+    c.close()

@@ -66,6 +66,44 @@ def test_gesv_fp64_matches_lapack(solver, n, nrhs):
     assert _rel(x, x_ref) < 1e-12
 
 
+PIVOT_SHAPES = [(40, 3), (300, 5), (702, 48), (1030, 38)]
+
+
+@pytest.mark.parametrize("n,nrhs", PIVOT_SHAPES)
+def test_gesv_fp64_with_row_interchanges(solver, n, nrhs):
+    """Plain Gaussian matrices: partial pivoting interchanges rows at almost
+    every step (the diagonally weighted systems above need none), across
+    panel and cluster-CTA boundaries; run three times (a race would show as
+    run-to-run differences)."""
+    rng = np.random.default_rng(1000 + n)
+    a = np.asfortranarray(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    b = np.asfortranarray(rng.standard_normal((n, nrhs)) + 1j * rng.standard_normal((n, nrhs)))
+    lu_ref, piv_ref, info_ref = sla.lapack.zgetrf(a)
+    x_ref, _ = sla.lapack.zgetrs(lu_ref, piv_ref, b)
+    for _ in range(3):
+        lu, ipiv, x, it, info = solver.gesv(a, b, precision=0)
+        assert info == 0
+        np.testing.assert_array_equal(ipiv, piv_ref + 1)
+        assert _rel(lu, lu_ref) < 1e-12
+        assert _rel(x, x_ref) < 1e-10
+
+
+@pytest.mark.parametrize("n,nrhs", PIVOT_SHAPES + [(2100, 8)])
+def test_gesv_mixed_with_row_interchanges(solver, n, nrhs):
+    """The complex64 LU (cluster panels, fused interchanges, tensor-core
+    updates from order 1024) on Gaussian matrices: LAPACK's pivot sequence
+    where single precision does not tie-break differently, and refinement to
+    the FP64 solution."""
+    rng = np.random.default_rng(2000 + n)
+    a = np.asfortranarray(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    b = np.asfortranarray(rng.standard_normal((n, nrhs)) + 1j * rng.standard_normal((n, nrhs)))
+    x_ref = np.linalg.solve(a, b)
+    for _ in range(2):
+        lu, ipiv, x, it, info = solver.gesv(a, b, precision=1)
+        assert info == 0 and it > 0
+        assert _rel(x, x_ref) < 1e-9
+
+
 @pytest.mark.parametrize("n,nrhs", SHAPES)
 def test_gesv_mixed_refines_to_tolerance(solver, n, nrhs):
     a, b = _system(n, nrhs, seed=n + 1)
