@@ -506,18 +506,22 @@ def _launch_count(n, prec, sweeps=1, nd=30, nbeta=8):
     """Kernels the library launches per frequency-solve, from its launch
     sequence (checked against the ncu launch list of one solve)."""
     nb, nbo = 32, 256
-    def inner(jb):  # 32-wide panels of one outer panel: panel + laswp, then trsm + update while columns remain
+    def inner(jb):  # 32-wide panels: panel + fused interchanges / L11 solve, then the update while columns remain
         p = (jb + nb - 1) // nb
-        return 2 * p + 2 * (p - 1)
-    if prec == 1 and n >= 1024:
+        return 2 * p + (p - 1)
+    tc = prec == 1 and n >= 1024
+    if tc:
         outer = (n + nbo - 1) // nbo
-        # per outer panel: pivots to the other columns, L_kk^-1; where columns remain: I - L_kk^-1 and two
-        # tensor-core GEMMs (U12, trailing update) with their operand packing; then one batched U_kk^-1
-        lu = sum(inner(min(nbo, n - k)) for k in range(0, n, nbo)) + 2 * outer + 7 * (outer - 1) + 1
+        # the permutation's start (1); per outer panel: pivots to the other columns, L_kk^-1; where columns
+        # remain: I - L_kk^-1 and two tensor-core GEMMs (U12, trailing update) with their operand packing;
+        # then one batched U_kk^-1
+        lu = 1 + sum(inner(min(nbo, n - k)) for k in range(0, n, nbo)) + 2 * outer + 7 * (outer - 1) + 1
     else:
         lu = inner(n)
     blocks = (n + nbo - 1) // nbo
-    getrs = 1 + 2 * (2 * blocks - 1)                # laswp + (trsm or block-inverse product, gemm) down and up
+    # right-hand sides permuted (gather + copy with the block inverses, else one interchange kernel), then
+    # (block-inverse product or trsm, gemm) down and up
+    getrs = (2 if tc else 1) + 2 * (2 * blocks - 1)
     fill = 1
     forces = 1
     if prec == 0:
