@@ -8,8 +8,12 @@
 // HAMS-format and WAMIT-format result files (RFORCE / EFORCE,
 // src/PotentWavForce.f90:100-218, src/PotentWavForceMulti.f90:100-223; the pressure and
 // elevation file of OutputPressureElevation_Radiation / _Diffraction,
-// src/PressureElevation.f90:336-470, single body).  Host code: parsing,
-// orchestration and formatting; every solve runs on the GPU.
+// src/PressureElevation.f90:336-470, single body), and the motion equations
+// of SolveMotion / SolveMotionMulti (src/SolveMotion.f90, src/SolveMotionMulti.f90)
+// with the hydrostatic decks of ReadHydroStatic(Multi) (src/HydroStatic.f90,
+// src/HydroStaticMulti.f90): Motion.4 and Hydrostat.hst.  Host code: parsing,
+// orchestration, the 6 NBODY x 6 NBODY motion solves per frequency and
+// heading, and formatting; every boundary-integral solve runs on the GPU.
 //
 // The writers reproduce the reference's Fortran edit descriptors (Fw.d,
 // Ew.d, ESw.d, Iw) character for character, including its choices that a
@@ -177,6 +181,10 @@ struct hg_case {
   std::vector<int> ncon, ncn, ranges;                     // n x 4 column-major (1-based), n, 2 x nbody (1-based)
   // per frequency (CalWaveProperts)
   std::vector<double> v, wk, w1, tp, wl, oufr, wvn;       // wvn: nper x kNk (finite depth)
+  // hydrostatic decks (per body, 6 x 6 row-major each): mass, external linear and
+  // quadratic damping, hydrostatic and external restoring
+  bool hydro = false;
+  std::vector<double> matx, blnr, bqdr, crs, kstf;
   std::string err;
 };
 
@@ -415,6 +423,31 @@ void read_meshes(hg_case* c) {
   }
 }
 
+// ReadHydroStatic(Multi) (src/HydroStatic.f90:41-82): Hydrostatic.in or
+// Hydrostatic_<b>.in per body, five 6 x 6 matrices in FORMAT(6(2x,E12.5))
+// after a title line each; the centre of gravity is read past.  Decks without
+// them run without motions.
+void read_hydrostatics(hg_case* c) {
+  const int nb = c->nbody;
+  std::vector<double>* mats[5] = {&c->matx, &c->blnr, &c->bqdr, &c->crs, &c->kstf};
+  for (auto* m : mats) m->assign((size_t)36 * nb, 0.0);
+  for (int b = 0; b < nb; ++b) {
+    const std::string path = c->dir + "/Hydrostatic" + (nb > 1 ? "_" + std::to_string(b + 1) : std::string()) + ".in";
+    if (!file_exists(path)) return;
+    const auto lines = read_lines(path);
+    size_t i = 3;  // title, centre of gravity, title
+    for (auto* m : mats) {
+      for (int r = 0; r < 6; ++r) {
+        if (i >= lines.size()) raise(-7, "%s ends early", path.c_str());
+        const std::string& ln = lines[i++];
+        for (int q = 0; q < 6; ++q) (*m)[(size_t)36 * b + 6 * r + q] = f_real(field(ln, 2 + 14 * q, 12), 5);
+      }
+      ++i;  // the next title
+    }
+  }
+  c->hydro = true;
+}
+
 // CalWaveProperts (src/ImplementSubs.f90:40-151) for every entry; TP keeps
 // its previous value where the input type does not set it (type 5), as there.
 void wave_properties(hg_case* c) {
@@ -531,6 +564,9 @@ struct Out {
   void line(const std::string& s) { std::fprintf(f, "%s\n", s.c_str()); }
 };
 
+void write_motions(const hg_case* c, const std::string& wd, const double* amas, const double* bdmp,
+                   const double* exfc, double rho, double g);
+
 // amas/bdmp: nper blocks of nd x nd column-major (row = force DOF, column =
 // mode); exfc: nper blocks of (nbeta x nd) COMPLEX*16 column-major.
 void write_results(const hg_case* c, const std::string& out, const double* amas, const double* bdmp,
@@ -611,6 +647,113 @@ void write_results(const hg_case* c, const std::string& out, const double* amas,
             f3.line(fES(14, 6, c->oufr[k]) + fES(14, 6, beta * 180.0 / kPi) + fI(6, 6 * m + md + 1) +
                     fES(14, 6, mod) + fES(14, 6, phs) + fES(14, 6, nrel) + fES(14, 6, nimg));
           }
+      }
+    }
+  }
+  if (c->hydro) write_motions(c, wd, amas, bdmp, exfc, rho, g);
+}
+
+// ZGESV of the motion equations (6 NBODY unknowns): LU with partial
+// pivoting on |re| + |im| (IZAMAX), one right-hand side.
+bool zgesv_small(int n, std::vector<std::complex<double>>& a, std::vector<std::complex<double>>& b) {
+  auto at = [&](int i, int j) -> std::complex<double>& { return a[(size_t)i + (size_t)j * n]; };
+  auto cabs1 = [](std::complex<double> z) { return std::fabs(z.real()) + std::fabs(z.imag()); };
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    for (int i = k + 1; i < n; ++i)
+      if (cabs1(at(i, k)) > cabs1(at(p, k))) p = i;
+    if (cabs1(at(p, k)) == 0.0) return false;
+    if (p != k) {
+      for (int j = 0; j < n; ++j) std::swap(at(k, j), at(p, j));
+      std::swap(b[k], b[p]);
+    }
+    const std::complex<double> r = 1.0 / at(k, k);
+    for (int i = k + 1; i < n; ++i) {
+      const std::complex<double> l = at(i, k) * r;
+      at(i, k) = l;
+      for (int j = k + 1; j < n; ++j) at(i, j) -= l * at(k, j);
+      b[i] -= l * b[k];
+    }
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    std::complex<double> t = b[k];
+    for (int j = k + 1; j < n; ++j) t -= at(k, j) * b[j];
+    b[k] = t / at(k, k);
+  }
+  return true;
+}
+
+// SolveMotion / SolveMotionMulti: motions DSPL from
+//   [-w^2 (M + A) + i w (B + B_lin [+ B_quad w |DSPL|]) + C + K] DSPL = -Im F - i Re F,
+// the quadratic damping by fixed-point iteration until sum |dDSPL|/|DSPL| <= 1e-6
+// (single body: every component in the sum, as there; several bodies: zero
+// components left out, as there); Motion.4 lines for regular frequencies.
+void write_motions(const hg_case* c, const std::string& wd, const double* amas, const double* bdmp,
+                   const double* exfc, double rho, double g) {
+  const int nb = c->nbody, nd = 6 * nb, nbeta = (int)c->headings.size(), np = c->nper;
+  auto blk = [&](const std::vector<double>& m, int i, int j) {
+    const int bi = i / 6, bj = j / 6;
+    return bi == bj ? m[(size_t)36 * bi + 6 * (i % 6) + (j % 6)] : 0.0;
+  };
+  {
+    Out fh(wd + "/Hydrostat.hst");  // FORMAT(2I6,2X,ES14.6)
+    for (int i = 0; i < nd; ++i)
+      for (int j = 0; j < nd; ++j) fh.line(fI(6, i + 1) + fI(6, j + 1) + "  " + fES(14, 6, blk(c->crs, i, j) / (rho * g)));
+  }
+  double qnorm = 0.0;
+  for (double x : c->bqdr) qnorm = std::max(qnorm, std::fabs(x));
+  Out f4(wd + "/Motion.4");
+  std::vector<std::complex<double>> left((size_t)nd * nd), rhs(nd), dspl(nd), dspl1(nd);
+  for (int k = 0; k < np; ++k) {
+    const double w1 = c->w1[k];
+    const double* A = amas + (size_t)k * nd * nd;
+    const double* B = bdmp + (size_t)k * nd * nd;
+    for (int ib = 0; ib < nbeta; ++ib) {
+      const double* F = exfc + 2 * ((size_t)k * nbeta * nd);
+      auto build = [&](bool quad) {
+        for (int j = 0; j < nd; ++j)
+          for (int i = 0; i < nd; ++i) {
+            double damp = B[i + (size_t)j * nd] + blk(c->blnr, i, j);
+            if (quad) damp += blk(c->bqdr, i, j) * w1 * std::abs(dspl[j]);
+            left[(size_t)i + (size_t)j * nd] =
+                std::complex<double>(-w1 * w1 * (blk(c->matx, i, j) + A[i + (size_t)j * nd]) + blk(c->crs, i, j) +
+                                         blk(c->kstf, i, j),
+                                     w1 * damp);
+          }
+        for (int i = 0; i < nd; ++i) {
+          const double* f = F + 2 * (ib + (size_t)i * nbeta);
+          rhs[i] = std::complex<double>(-f[1], -f[0]);
+        }
+      };
+      build(false);
+      if (!zgesv_small(nd, left, rhs)) raise(-8, "motion equations singular (entry %d, heading %d)", k + 1, ib + 1);
+      dspl = rhs;
+      if (qnorm >= 1.e-6) {
+        double rerr = 100.0;
+        int guard = 0;
+        while (rerr > 1.e-6) {
+          if (++guard > 10000) raise(-8, "quadratic-damping iteration did not settle (entry %d, heading %d)", k + 1, ib + 1);
+          build(true);
+          if (!zgesv_small(nd, left, rhs)) raise(-8, "motion equations singular (entry %d, heading %d)", k + 1, ib + 1);
+          dspl1 = rhs;
+          rerr = 0.0;
+          for (int j = 0; j < nd; ++j) {
+            const double dj = std::abs(dspl1[j] - dspl[j]), aj = std::abs(dspl1[j]);
+            if (nb == 1 || aj > 0.0) rerr += dj / aj;
+          }
+          dspl = dspl1;
+        }
+      }
+      if (special(c->tp[k])) continue;
+      const double beta = c->headings[ib] * kPi / 180.0;
+      for (int md = 0; md < nd; ++md) {
+        const int mexp = (md % 6 < 3) ? 2 : 3;
+        const double nfac = 1.0 / std::pow(c->refl, mexp);
+        const double nrel = dspl[md].real() / nfac, nimg = dspl[md].imag() / nfac;
+        const double magn = std::sqrt(nrel * nrel + nimg * nimg);
+        const double phs = std::atan2(nimg, nrel) * (180.0 / kPi);
+        f4.line(fES(14, 6, c->oufr[k]) + fES(14, 6, beta * 180.0 / kPi) + fI(6, md + 1) + fES(14, 6, magn) +
+                fES(14, 6, phs) + fES(14, 6, nrel) + fES(14, 6, nimg));
       }
     }
   }
@@ -743,6 +886,7 @@ int hg_case_read(const char* input_dir, hg_case** out, char* err, int errlen) {
   try {
     read_control(c);
     read_meshes(c);
+    read_hydrostatics(c);
     wave_properties(c);
   } catch (const CaseError& e) {
     set_err(err, errlen, e.msg);

@@ -346,6 +346,9 @@ int hg_stage_times(const hg_ctx *ctx, float *ms4);
  *       order they write: per frequency and body pair)
  *   <out>/Wamit_format/PressureElevation.6p for field points (single body;
  *       src/PressureElevation.f90:336-470, through hg_field_points)
+ *   <out>/Wamit_format/Motion.4, Hydrostat.hst when Hydrostatic[_b].in are
+ *       present (SolveMotion / SolveMotionMulti, src/SolveMotion*.f90;
+ *       ReadHydroStatic, src/HydroStatic*.f90)
  * hg_case_read parses and computes the panel geometry and wave properties
  * (host only); hg_case_info / hg_case_arrays expose what was read:
  *   info[12]  = n, nl, ntnd, nbody, nper, nbeta, irsp, isol, nfp, sybo, inft, ouft

@@ -5,7 +5,8 @@ Run once in a checkout that has the HAMS-MREL reference next to it:
     python tests/golden/make_golden.py /path/to/HAMS-MREL
 
 It copies, unchanged, the input decks and the expected HAMS/WAMIT-format
-outputs of three reference cases into tests/golden/<case>/:
+outputs (added mass and damping, excitation, and for the two examples the
+motions and hydrostatics) of three reference cases into tests/golden/<case>/:
 
   config1   test/data/config1            3 bodies x 234 panels, h = 70 m,
                                          3 frequencies x 3 headings, IRSP = 0
@@ -28,11 +29,13 @@ CASES = {
                 ["OAMASS%d.txt", "ODAMPING%d.txt", "OEXFOR%d.txt"]),
     "example5": ("examples/example5_single_body/Input", "examples/example5_single_body/Output",
                  ["Hams_format/OAMASS%d.txt", "Hams_format/ODAMPING%d.txt", "Hams_format/OEXFOR%d.txt",
-                  "Wamit_format/AmssDamp.1", "Wamit_format/ExcForce.3"]),
+                  "Wamit_format/AmssDamp.1", "Wamit_format/ExcForce.3", "Wamit_format/Motion.4",
+                  "Wamit_format/Hydrostat.hst"]),
     "example3": ("examples/example3_multi_bodies_gen_mod/Input",
                  "examples/example3_multi_bodies_gen_mod/Output",
                  ["Hams_format/OAMASS%d.txt", "Hams_format/ODAMPING%d.txt", "Hams_format/OEXFOR%d.txt",
-                  "Wamit_format/AmssDamp.1", "Wamit_format/ExcForce.3"]),
+                  "Wamit_format/AmssDamp.1", "Wamit_format/ExcForce.3", "Wamit_format/Motion.4",
+                  "Wamit_format/Hydrostat.hst"]),
 }
 
 
