@@ -572,7 +572,8 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--slots", type=int, default=4, help="frequency-solves in flight (hg_solve_sweep slots)")
+    ap.add_argument("--slots", type=int, default=0,
+                    help="frequency-solves in flight (hg_solve_sweep slots); 0: at most 8, balanced over the steps")
     ap.add_argument("--refine", default="classical", choices=["classical", "gmres"],
                     help="mixed-form refinement: classical iterative refinement or GMRES-IR")
     ap.add_argument("--lu-tensor", type=int, default=3, choices=[0, 1, 3],
@@ -586,6 +587,14 @@ def main():
         world = int(os.environ.get("WORLD_SIZE", "1"))
         cpu_reference(args.steps, args.warmup, rank, world)
         return
+    auto_slots = args.slots <= 0
+    if auto_slots:
+        # at most 8 in flight (measured at 6048 panels: 4 -> 67.7, 6 -> 68.3, 8 -> 72.4 freq-solves/s),
+        # spread evenly over the rounds the timed frequencies make
+        rounds = -(-args.steps // 8)
+        args.slots = max(1, -(-args.steps // rounds))
+        if args.workload == "three":
+            args.slots = min(args.slots, 4)
     if args.workload == "three":
         three_bodies(args)
         return
@@ -595,7 +604,7 @@ def main():
     if args.workload != "array":
         if args.requests is None:
             args.requests = 512 if args.workload == "batch" else 24
-        if args.slots == 4:
+        if auto_slots:
             args.slots = 8
         served(args)
         return
