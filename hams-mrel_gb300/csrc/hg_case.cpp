@@ -493,7 +493,15 @@ std::string fit(std::string s, int w) {
   return std::string(w - s.size(), ' ') + s;
 }
 
+// Non-finite values as gfortran writes them.
+std::string nonfinite(int w, double x) {
+  if (std::isnan(x)) return fit("NaN", w);
+  const std::string s = (x < 0 ? "-" : "") + std::string(w >= 9 ? "Infinity" : "Inf");
+  return fit(s, w);
+}
+
 std::string fF(int w, int d, double x) {  // Fw.d
+  if (!std::isfinite(x)) return nonfinite(w, x);
   char b[64];
   snprintf(b, sizeof(b), "%.*f", d, x);
   return fit(b, w);
@@ -529,6 +537,7 @@ std::string exponent(int e, bool with_letter) {
 }
 
 std::string fE(int w, int d, double x) {  // Ew.d: 0.ddddddE+XX
+  if (!std::isfinite(x)) return nonfinite(w, x);
   std::string dg;
   int e;
   sig_digits(x, d, dg, e);
@@ -538,6 +547,7 @@ std::string fE(int w, int d, double x) {  // Ew.d: 0.ddddddE+XX
 }
 
 std::string fES(int w, int d, double x) {  // ESw.d: d.ddddddE+XX
+  if (!std::isfinite(x)) return nonfinite(w, x);
   std::string dg;
   int e;
   sig_digits(x, d + 1, dg, e);
@@ -705,6 +715,7 @@ void write_motions(const hg_case* c, const std::string& wd, const double* amas, 
   Out f4(wd + "/Motion.4");
   std::vector<std::complex<double>> left((size_t)nd * nd), rhs(nd), dspl(nd), dspl1(nd);
   for (int k = 0; k < np; ++k) {
+    if (special(c->tp[k])) continue;  // no motions are written for the zero- and infinite-frequency limits
     const double w1 = c->w1[k];
     const double* A = amas + (size_t)k * nd * nd;
     const double* B = bdmp + (size_t)k * nd * nd;
@@ -726,15 +737,21 @@ void write_motions(const hg_case* c, const std::string& wd, const double* amas, 
         }
       };
       build(false);
-      if (!zgesv_small(nd, left, rhs)) raise(-8, "motion equations singular (entry %d, heading %d)", k + 1, ib + 1);
+      // a singular system leaves NaN motions in the file (the reference's ZGESV result is not checked either)
+      const std::complex<double> nan(std::nan(""), std::nan(""));
+      bool ok = zgesv_small(nd, left, rhs);
       dspl = rhs;
-      if (qnorm >= 1.e-6) {
+      if (!ok) std::fill(dspl.begin(), dspl.end(), nan);
+      if (ok && qnorm >= 1.e-6) {
         double rerr = 100.0;
         int guard = 0;
         while (rerr > 1.e-6) {
           if (++guard > 10000) raise(-8, "quadratic-damping iteration did not settle (entry %d, heading %d)", k + 1, ib + 1);
           build(true);
-          if (!zgesv_small(nd, left, rhs)) raise(-8, "motion equations singular (entry %d, heading %d)", k + 1, ib + 1);
+          if (!zgesv_small(nd, left, rhs)) {
+            std::fill(dspl.begin(), dspl.end(), nan);
+            break;
+          }
           dspl1 = rhs;
           rerr = 0.0;
           for (int j = 0; j < nd; ++j) {
@@ -744,7 +761,6 @@ void write_motions(const hg_case* c, const std::string& wd, const double* amas, 
           dspl = dspl1;
         }
       }
-      if (special(c->tp[k])) continue;
       const double beta = c->headings[ib] * kPi / 180.0;
       for (int md = 0; md < nd; ++md) {
         const int mexp = (md % 6 < 3) ? 2 : 3;

@@ -143,3 +143,46 @@ def test_case_run_field_points_file(pkg, oracle, tmp_path):
                 assert abs(float(row[3]) - abs(z)) <= tol
     assert nrow == len(rows)
     c.close()
+
+
+def test_case_run_zero_and_infinite_frequency_entries(pkg, tmp_path):
+    """0_inf_frequency_limits = 1 adds the zero- and infinite-frequency limits
+    as the first two entries (CalWaveProperts, src/ImplementSubs.f90:45-70):
+    they write added mass only in AmssDamp.1 and no ExcForce.3 lines, and the
+    regular entries are those of the same deck without them."""
+    src = os.path.join(GOLDEN, "config1", "input")
+    d = os.path.join(tmp_path, "deck")
+    shutil.copytree(src, d)
+    with open(os.path.join(d, "ControlFile.in")) as f:
+        lines = f.read().split("\n")
+    for i, ln in enumerate(lines):
+        if "0_inf_frequency_limits" in ln:
+            lines[i] = ln[:27] + "%16d" % 1
+    with open(os.path.join(d, "ControlFile.in"), "w") as f:
+        f.write("\n".join(lines))
+    c = pkg.hamsgpu.Case(d)
+    assert c.info["sybo"] == 1 and c.info["nper"] == 5
+    freq = c.arrays()["freq"]
+    assert list(freq[0, :4]) == [0.0, 0.0, 0.0, -1.0] and list(freq[1, :4]) == [-1.0, -1.0, -1.0, 0.0]
+    c.run(os.path.join(tmp_path, "with"), precision=pkg.hamsgpu.HG_PREC_FP64, nslots=2)
+    ref = pkg.hamsgpu.Case(src)
+    ref.run(os.path.join(tmp_path, "without"), precision=pkg.hamsgpu.HG_PREC_FP64, nslots=2)
+    nd = 18
+    with open(os.path.join(tmp_path, "with", "Wamit_format", "AmssDamp.1")) as f:
+        am = f.read().splitlines()
+    with open(os.path.join(tmp_path, "without", "Wamit_format", "AmssDamp.1")) as f:
+        am0 = f.read().splitlines()
+    assert len(am) == 5 * nd * nd and len(am0) == 3 * nd * nd
+    assert all(len(ln.split()) == 4 for ln in am[:2 * nd * nd])
+    assert am[2 * nd * nd:] == am0
+    with open(os.path.join(tmp_path, "with", "Wamit_format", "ExcForce.3")) as f:
+        ex = f.read()
+    with open(os.path.join(tmp_path, "without", "Wamit_format", "ExcForce.3")) as f:
+        assert ex == f.read()
+    with open(os.path.join(tmp_path, "with", "Hams_format", "OAMASS3.txt")) as f:
+        oa = f.read().splitlines()
+    assert len(oa) == 5 * 9 and oa[0].startswith("  0.000   0.000") and oa[9].startswith(" -1.000  -1.000")
+    a = np.array([[float(t) for t in ln.split()] for ln in oa])
+    assert np.all(np.isfinite(a))
+    c.close()
+    ref.close()
