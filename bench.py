@@ -110,14 +110,19 @@ class ClockSampler:
 
 
 def _dist():
+    """One process per GPU under torchrun (NCCL; gloo where no GPU is visible,
+    as in the CPU tests of this host logic)."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws > 1:
         import torch
         import torch.distributed as dist
         rank = int(os.environ["RANK"])
         local = int(os.environ.get("LOCAL_RANK", rank))
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:
+            dist.init_process_group("gloo")
         return dist, rank, ws, local
     return None, 0, 1, 0
 
@@ -131,9 +136,16 @@ def _max_over_ranks(dist, x, local):
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}")
+    dev = f"cuda:{local}" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def shard_frequencies(rank, world, n):
+    """Frequencies are independent: rank r takes entries r, r + world, ...
+    (no data exchange; the ranks meet only at the timing barrier)."""
+    return list(range(rank, n, world))
 
 
 def _mesh():
@@ -209,7 +221,7 @@ def ours(args, dist, rank, world, local):
     pkg, mesh = _mesh()
     hg = pkg.hamsgpu
     prec = hg.HG_PREC_MIXED if args.precision == "mixed" else hg.HG_PREC_FP64
-    my_freqs = [FREQS[k] for k in range(rank, N_FREQ, world)]
+    my_freqs = [FREQS[k] for k in shard_frequencies(rank, world, N_FREQ)]
     betas = BETAS_DEG * math.pi / 180.0
     nd = 30
     nslots = args.slots
