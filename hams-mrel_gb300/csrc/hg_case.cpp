@@ -11,7 +11,8 @@
 // src/PressureElevation.f90:336-470, single body), and the motion equations
 // of SolveMotion / SolveMotionMulti (src/SolveMotion.f90, src/SolveMotionMulti.f90)
 // with the hydrostatic decks of ReadHydroStatic(Multi) (src/HydroStatic.f90,
-// src/HydroStaticMulti.f90): Motion.4 and Hydrostat.hst.  Host code: parsing,
+// src/HydroStaticMulti.f90): Motion.4 and Hydrostat.hst; and the single-body
+// Hydrostar-format files (src/PrintOutput.f90).  Host code: parsing,
 // orchestration, the 6 NBODY x 6 NBODY motion solves per frequency and
 // heading, and formatting; every boundary-integral solve runs on the GPU.
 //
@@ -575,7 +576,9 @@ struct Out {
 };
 
 void write_motions(const hg_case* c, const std::string& wd, const double* amas, const double* bdmp,
-                   const double* exfc, double rho, double g);
+                   const double* exfc, double rho, double g, std::vector<std::complex<double>>* dspl_all);
+void write_hydrostar(const hg_case* c, const std::string& out, const double* amas, const double* bdmp,
+                     const double* exfc, const std::vector<std::complex<double>>* dspl_all);
 
 // amas/bdmp: nper blocks of nd x nd column-major (row = force DOF, column =
 // mode); exfc: nper blocks of (nbeta x nd) COMPLEX*16 column-major.
@@ -660,7 +663,9 @@ void write_results(const hg_case* c, const std::string& out, const double* amas,
       }
     }
   }
-  if (c->hydro) write_motions(c, wd, amas, bdmp, exfc, rho, g);
+  std::vector<std::complex<double>> dspl;
+  if (c->hydro) write_motions(c, wd, amas, bdmp, exfc, rho, g, &dspl);
+  if (nb == 1) write_hydrostar(c, out, amas, bdmp, exfc, c->hydro ? &dspl : nullptr);
 }
 
 // ZGESV of the motion equations (6 NBODY unknowns): LU with partial
@@ -699,7 +704,7 @@ bool zgesv_small(int n, std::vector<std::complex<double>>& a, std::vector<std::c
 // (single body: every component in the sum, as there; several bodies: zero
 // components left out, as there); Motion.4 lines for regular frequencies.
 void write_motions(const hg_case* c, const std::string& wd, const double* amas, const double* bdmp,
-                   const double* exfc, double rho, double g) {
+                   const double* exfc, double rho, double g, std::vector<std::complex<double>>* dspl_all) {
   const int nb = c->nbody, nd = 6 * nb, nbeta = (int)c->headings.size(), np = c->nper;
   auto blk = [&](const std::vector<double>& m, int i, int j) {
     const int bi = i / 6, bj = j / 6;
@@ -714,8 +719,8 @@ void write_motions(const hg_case* c, const std::string& wd, const double* amas, 
   for (double x : c->bqdr) qnorm = std::max(qnorm, std::fabs(x));
   Out f4(wd + "/Motion.4");
   std::vector<std::complex<double>> left((size_t)nd * nd), rhs(nd), dspl(nd), dspl1(nd);
+  dspl_all->assign((size_t)np * std::max(nbeta, 1) * nd, std::complex<double>(0.0, 0.0));
   for (int k = 0; k < np; ++k) {
-    if (special(c->tp[k])) continue;  // no motions are written for the zero- and infinite-frequency limits
     const double w1 = c->w1[k];
     const double* A = amas + (size_t)k * nd * nd;
     const double* B = bdmp + (size_t)k * nd * nd;
@@ -746,7 +751,7 @@ void write_motions(const hg_case* c, const std::string& wd, const double* amas, 
         double rerr = 100.0;
         int guard = 0;
         while (rerr > 1.e-6) {
-          if (++guard > 10000) raise(-8, "quadratic-damping iteration did not settle (entry %d, heading %d)", k + 1, ib + 1);
+          if (++guard > 10000) break;  // keeps the last iterate (the reference loops until it settles)
           build(true);
           if (!zgesv_small(nd, left, rhs)) {
             std::fill(dspl.begin(), dspl.end(), nan);
@@ -761,6 +766,8 @@ void write_motions(const hg_case* c, const std::string& wd, const double* amas, 
           dspl = dspl1;
         }
       }
+      std::copy(dspl.begin(), dspl.end(), dspl_all->begin() + ((size_t)k * nbeta + ib) * nd);
+      if (special(c->tp[k])) continue;  // Motion.4 holds the regular frequencies only
       const double beta = c->headings[ib] * kPi / 180.0;
       for (int md = 0; md < nd; ++md) {
         const int mexp = (md % 6 < 3) ? 2 : 3;
@@ -772,6 +779,66 @@ void write_motions(const hg_case* c, const std::string& wd, const double* amas, 
                 fES(14, 6, phs) + fES(14, 6, nrel) + fES(14, 6, nimg));
       }
     }
+  }
+}
+
+// Hydrostar-format files of a single body (PrintBody_RealVal / PrintBody_CmplxVal
+// / PrintEnd, src/PrintOutput.f90; opened by CreateHydrostarFiles,
+// src/InputFiles.f90:339-357; written from src/HAMS_Prog.f90:306-331): per
+// entry one line FORMAT(F8.4, NBETA ES14.6, NBETA F12.4) of w and, per
+// heading, the real value and 0 (AddedMass_ij, WaveDamping_ij) or the
+// modulus and the phase ATAN2D(-Re, -Im) in [0, 360) (Excitation_k,
+// Motion_k), then two closing lines.
+void write_hydrostar(const hg_case* c, const std::string& out, const double* amas, const double* bdmp,
+                     const double* exfc, const std::vector<std::complex<double>>* dspl_all) {
+  const int nbeta = (int)c->headings.size(), np = c->nper, nd = 6;
+  const std::string hd = out + "/Hydrostar_format";
+  make_dir(hd);
+  const std::string end1 = "#" + std::string(60, '-'), end2 = "#ENDFILE";
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j)
+      for (int which = 0; which < 2; ++which) {
+        const double* m = which == 0 ? amas : bdmp;
+        Out f(hd + "/" + (which == 0 ? "AddedMass_" : "WaveDamping_") + std::to_string(i + 1) + std::to_string(j + 1) +
+              ".rao");
+        for (int k = 0; k < np; ++k) {
+          const double v = m[(size_t)k * nd * nd + i + (size_t)j * nd];
+          std::string s = fF(8, 4, c->w1[k]);
+          for (int b = 0; b < nbeta; ++b) s += fES(14, 6, v);
+          for (int b = 0; b < nbeta; ++b) s += fF(12, 4, 0.0);
+          f.line(s);
+        }
+        f.line(end1);
+        f.line(end2);
+      }
+  auto cmplx_line = [&](int k, const std::complex<double>* vals, size_t stride) {
+    std::string s = fF(8, 4, c->w1[k]);
+    for (int b = 0; b < nbeta; ++b) s += fES(14, 6, std::abs(vals[b * stride]));
+    for (int b = 0; b < nbeta; ++b) {
+      const std::complex<double> z = vals[b * stride];
+      double phs = std::atan2(-z.real(), -z.imag()) * (180.0 / kPi);
+      if (phs < 0.0) phs += 360.0;
+      s += fF(12, 4, phs);
+    }
+    return s;
+  };
+  std::vector<std::complex<double>> tmp(nbeta);
+  for (int md = 0; md < 6; ++md) {
+    Out fx(hd + "/Excitation_" + std::to_string(md + 1) + ".rao");
+    for (int k = 0; k < np; ++k) {
+      for (int b = 0; b < nbeta; ++b) {
+        const double* p = exfc + 2 * ((size_t)k * nbeta * nd + b + (size_t)md * nbeta);
+        tmp[b] = std::complex<double>(p[0], p[1]);
+      }
+      fx.line(cmplx_line(k, tmp.data(), 1));
+    }
+    fx.line(end1);
+    fx.line(end2);
+    if (!dspl_all) continue;
+    Out fm(hd + "/Motion_" + std::to_string(md + 1) + ".rao");
+    for (int k = 0; k < np; ++k) fm.line(cmplx_line(k, dspl_all->data() + (size_t)k * nbeta * nd + md, nd));
+    fm.line(end1);
+    fm.line(end2);
   }
 }
 

@@ -349,6 +349,8 @@ int hg_stage_times(const hg_ctx *ctx, float *ms4);
  *   <out>/Wamit_format/Motion.4, Hydrostat.hst when Hydrostatic[_b].in are
  *       present (SolveMotion / SolveMotionMulti, src/SolveMotion*.f90;
  *       ReadHydroStatic, src/HydroStatic*.f90)
+ *   <out>/Hydrostar_format/AddedMass_ij.rao, WaveDamping_ij.rao,
+ *       Excitation_k.rao, Motion_k.rao for a single body (src/PrintOutput.f90)
  * hg_case_read parses and computes the panel geometry and wave properties
  * (host only); hg_case_info / hg_case_arrays expose what was read:
  *   info[12]  = n, nl, ntnd, nbody, nper, nbeta, irsp, isol, nfp, sybo, inft, ouft

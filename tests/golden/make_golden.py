@@ -6,7 +6,8 @@ Run once in a checkout that has the HAMS-MREL reference next to it:
 
 It copies, unchanged, the input decks and the expected HAMS/WAMIT-format
 outputs (added mass and damping, excitation, and for the two examples the
-motions and hydrostatics) of three reference cases into tests/golden/<case>/:
+motions and hydrostatics; for example5 a sample of the Hydrostar-format
+files) of three reference cases into tests/golden/<case>/:
 
   config1   test/data/config1            3 bodies x 234 panels, h = 70 m,
                                          3 frequencies x 3 headings, IRSP = 0
@@ -30,7 +31,11 @@ CASES = {
     "example5": ("examples/example5_single_body/Input", "examples/example5_single_body/Output",
                  ["Hams_format/OAMASS%d.txt", "Hams_format/ODAMPING%d.txt", "Hams_format/OEXFOR%d.txt",
                   "Wamit_format/AmssDamp.1", "Wamit_format/ExcForce.3", "Wamit_format/Motion.4",
-                  "Wamit_format/Hydrostat.hst"]),
+                  "Wamit_format/Hydrostat.hst"] +
+                 ["Hydrostar_format/%s.rao" % f for f in (
+                     "AddedMass_11", "AddedMass_15", "AddedMass_33", "WaveDamping_11", "WaveDamping_13",
+                     "WaveDamping_33", "Excitation_1", "Excitation_3", "Excitation_5", "Motion_1", "Motion_3",
+                     "Motion_5")]),
     "example3": ("examples/example3_multi_bodies_gen_mod/Input",
                  "examples/example3_multi_bodies_gen_mod/Output",
                  ["Hams_format/OAMASS%d.txt", "Hams_format/ODAMPING%d.txt", "Hams_format/OEXFOR%d.txt",

@@ -66,7 +66,8 @@ def file_values_max(path, first_value, nlines=None):
 
 
 def compare_result_file(got_path, exp_path, nlines=None, floor=1e-6, scale_by="column", first_value=0,
-                        scale_value=None, phase=None, phase_unit=1.0):
+                        scale_value=None, phase=None, phase_unit=1.0, phase_pairs=None, phase_period=None,
+                        skip_fields=()):
     """Compare two HAMS/WAMIT result files: the same number of lines (or the
     first nlines), every line of the same length (same edit descriptors), text
     tokens equal and numbers within one printed unit plus floor x the largest
@@ -75,8 +76,11 @@ def compare_result_file(got_path, exp_path, nlines=None, floor=1e-6, scale_by="c
     for those fields when given.  phase = (magnitude field, phase field):
     a phase is held to the angle that the floor of its magnitude's column
     subtends at that magnitude (times phase_unit per radian), since the
-    phase of a near-zero complex number is rounding noise.  Returns (worst
-    excess, lines compared)."""
+    phase of a near-zero complex number is rounding noise; phase_pairs does
+    the same for several (magnitude, phase) field pairs, phase_period wraps
+    phase differences (360 for [0, 360)); skip_fields are not compared
+    (their width still is, through the line length).  Returns (worst excess,
+    lines compared)."""
     with open(got_path) as f:
         got = f.read().splitlines()
     with open(exp_path) as f:
@@ -105,17 +109,24 @@ def compare_result_file(got_path, exp_path, nlines=None, floor=1e-6, scale_by="c
         assert len(lg) == len(le), f"{got_path}:{i + 1}: line length {len(lg)} != {len(le)}\n{lg}\n{le}"
         assert len(rg) == len(re_), f"{got_path}:{i + 1}: {len(rg)} fields != {len(re_)}"
         for j, (a, b) in enumerate(zip(rg, re_)):
+            if j in skip_fields:
+                continue
             try:
                 x, y = float(a), float(b)
             except ValueError:
                 assert a == b, f"{got_path}:{i + 1}: '{a}' != '{b}'"
                 continue
-            if phase is not None and j == phase[1]:
-                mag = max(abs(float(re_[phase[0]])), 1e-300)
-                tol = 1.01 * max(_ulp(a), _ulp(b)) + 2.0 * phase_unit * floor * scale[phase[0]] / mag
+            pairs = list(phase_pairs or []) + ([tuple(phase)] if phase is not None else [])
+            magf = next((pm for pm, pp in pairs if pp == j), None)
+            diff = abs(x - y)
+            if magf is not None:
+                mag = max(abs(float(re_[magf])), 1e-300)
+                tol = 1.01 * max(_ulp(a), _ulp(b)) + 2.0 * phase_unit * floor * scale[magf] / mag
+                if phase_period:
+                    diff = min(diff, phase_period - diff)
             else:
                 tol = 1.01 * max(_ulp(a), _ulp(b)) + floor * scale[j]
-            excess = abs(x - y) / tol if tol > 0 else (0.0 if x == y else float("inf"))
+            excess = diff / tol if tol > 0 else (0.0 if x == y else float("inf"))
             assert excess <= 1.0, f"{got_path}:{i + 1} field {j + 1}: {a} vs {b} (tol {tol:.3g})\n{lg}\n{le}"
             worst = max(worst, excess)
     return worst, nlines

@@ -50,7 +50,12 @@ def expected_files(name):
     exp = os.path.join(GOLDEN, name, "expected")
     out = []
     for f in sorted(os.listdir(exp)):
-        sub = "Wamit_format" if f in ("AmssDamp.1", "ExcForce.3", "Motion.4", "Hydrostat.hst") else "Hams_format"
+        if f.endswith(".rao"):
+            sub = "Hydrostar_format"
+        elif f in ("AmssDamp.1", "ExcForce.3", "Motion.4", "Hydrostat.hst"):
+            sub = "Wamit_format"
+        else:
+            sub = "Hams_format"
         out.append((os.path.join(exp, f), sub, f))
     return out
 
@@ -82,6 +87,27 @@ def scale_rule(exp_dir, fname, nlines):
     and ExcForce.3 (magnitudes, phases, parts) column by column."""
     if fname == "ExcForce.3":  # the phase column is ATAN2D(...) * 180 / PI: degrees * 180/pi per radian
         return {"scale_by": "column", "phase": (3, 4), "phase_unit": (180.0 / np.pi) ** 2}
+    if fname.endswith(".rao"):
+        # one line per entry: w, NBETA values, NBETA zeros or phases in [0, 360)
+        if fname.startswith(("AddedMass", "WaveDamping")):
+            # one matrix entry per file: the floor scales with the largest entry among the shipped files
+            # of the kind (the noise of the reference's Green values follows the whole matrix)
+            stem = fname.split("_")[0]
+            top = max(file_values_max(os.path.join(exp_dir, f), 1, nlines) for f in os.listdir(exp_dir)
+                      if f.startswith(stem + "_"))
+            return {"scale_by": "file", "first_value": 1, "scale_value": top}
+        nbeta = 36
+        rule = {"scale_by": "file", "first_value": 1, "phase_pairs": [(1 + b, 1 + nbeta + b) for b in range(nbeta)],
+                "phase_unit": 180.0 / np.pi, "phase_period": 360.0}
+        if fname.startswith("Motion"):
+            # placeholder hydrostatics, as for Motion.4; and the phases of the shipped files are arg(DSPL),
+            # while PrintBody_CmplxVal (src/PrintOutput.f90), which the reference calls for the motions as
+            # for the excitation (src/HAMS_Prog.f90:313-314), writes ATAN2D(-Re, -Im) = 270 deg - arg(DSPL):
+            # the shipped motion files come from another version of the program (its Motion.4 too), so
+            # only the moduli are compared and the phases follow the source
+            rule["floor"] = 1e-3
+            rule["skip_fields"] = set(range(1 + nbeta, 1 + 2 * nbeta))
+        return rule
     if fname == "Motion.4":
         # motions of a system whose mass, restoring and damping decks are
         # placeholders (rows 1..6): weakly restrained DOFs amplify the solver's
@@ -116,6 +142,8 @@ def test_writer_reproduces_golden_files(pkg, oracle, name, tmp_path):
             n_exp = len(f.read().splitlines())
         if fname == "Hydrostat.hst":  # written once, not per frequency
             nl = None
+        elif fname.endswith(".rao"):  # a line per entry, then two closing lines
+            nl = None if nf == nper_exp else nf
         else:
             assert n_exp % nper_exp == 0
             nl = None if nf == len(case.ctl.wvnb) == nper_exp else n_exp // nper_exp * nf
