@@ -223,6 +223,19 @@ __device__ __forceinline__ bool better(float v, int i, float bv, int bi) {
   return v > bv || (v == bv && i < bi);
 }
 
+// The warp's best candidate under `better` (largest value, smallest row on
+// ties; values < 0 or NaN mean no candidate) in two redux instructions
+// instead of ten dependent shuffles: non-negative floats order as their bit
+// patterns, so the largest value is the largest key bits + 1 (0 = none), and
+// the row is the smallest among the lanes holding that key.
+__device__ __forceinline__ void warp_best(float& v, int& idx) {
+  const unsigned key = (v >= 0.f) ? __float_as_uint(v) + 1u : 0u;
+  const unsigned km = __reduce_max_sync(0xffffffffu, key);
+  const unsigned im = __reduce_min_sync(0xffffffffu, key == km ? (unsigned)idx : 0xffffffffu);
+  idx = (km == 0u) ? INT_MAX : (int)im;
+  v = (km == 0u) ? -1.f : __uint_as_float(km - 1u);
+}
+
 __global__ void __launch_bounds__(kClusterThreads, 1)
 k_getf2_cluster_push(float2* __restrict__ P, long lda, int m, int jb, int rpc, int* __restrict__ ipiv, int k0,
                      int* __restrict__ info) {
@@ -269,25 +282,13 @@ k_getf2_cluster_push(float2* __restrict__ P, long lda, int m, int jb, int rpc, i
         if (better(av, r0 + r, v, idx)) { v = av; idx = r0 + r; }
       }
     }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      const float ov = __shfl_down_sync(0xffffffffu, v, off);
-      const int oi = __shfl_down_sync(0xffffffffu, idx, off);
-      if (better(ov, oi, v, idx)) { v = ov; idx = oi; }
-    }
+    warp_best(v, idx);
     if (lane == 0) { red_v[warp] = v; red_i[warp] = idx; }
     __syncthreads();  // also orders every thread's column jj - 1 updates before the copies below
     if (warp == 0) {
       v = (lane < kWarps) ? red_v[lane] : -1.f;
       idx = (lane < kWarps) ? red_i[lane] : INT_MAX;
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const float ov = __shfl_down_sync(0xffffffffu, v, off);
-        const int oi = __shfl_down_sync(0xffffffffu, idx, off);
-        if (better(ov, oi, v, idx)) { v = ov; idx = oi; }
-      }
-      v = __shfl_sync(0xffffffffu, v, 0);
-      idx = __shfl_sync(0xffffffffu, idx, 0);
+      warp_best(v, idx);
       // (b) pack and push the message
       PanelMsg& msg = sendbuf[q];
       if (lane == 0) { msg.val = v; msg.idx = idx; }
@@ -313,14 +314,7 @@ k_getf2_cluster_push(float2* __restrict__ P, long lda, int m, int jb, int rpc, i
     // (d) the pivot: every warp reduces the 16 local messages
     float pmax = (lane < kClusterCTAs) ? recv[q][lane].val : -1.f;
     int p = (lane < kClusterCTAs) ? recv[q][lane].idx : INT_MAX;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      const float ov = __shfl_down_sync(0xffffffffu, pmax, off);
-      const int oi = __shfl_down_sync(0xffffffffu, p, off);
-      if (better(ov, oi, pmax, p)) { pmax = ov; p = oi; }
-    }
-    pmax = __shfl_sync(0xffffffffu, pmax, 0);
-    p = __shfl_sync(0xffffffffu, p, 0);
+    warp_best(pmax, p);
     if (p == INT_MAX) p = jj;
     const int op = p / rpc;
     const float2* prow = recv[q][op].cand;
@@ -342,12 +336,31 @@ k_getf2_cluster_push(float2* __restrict__ P, long lda, int m, int jb, int rpc, i
         }
         const float2 l = c_mul(tile[jj * rpc + r], rp);
         tile[jj * rpc + r] = l;
-        for (int c = jj + 1; c < jb; ++c) {
-          const float2 u = prow[c];
-          float2 a = tile[c * rpc + r];
-          a.x = fmaf(-l.x, u.x, fmaf(l.y, u.y, a.x));
-          a.y = fmaf(-l.x, u.y, fmaf(-l.y, u.x, a.y));
-          tile[c * rpc + r] = a;
+        // the rank-1 update in chunks of 8 columns with compile-time indices:
+        // the chunk's 8 pivot-row and 8 own-row loads issue back to back (a
+        // column-by-column loop waits on each load, the stores in between
+        // keeping the compiler from hoisting the next loads)
+#pragma unroll
+        for (int c0 = 0; c0 < kClusterNB; c0 += 8) {
+          if (c0 + 8 <= jj + 1 || c0 >= jb) continue;
+          float2 u[8], a[8];
+#pragma unroll
+          for (int t = 0; t < 8; ++t) {
+            const int c = c0 + t;
+            if (c > jj && c < jb) {
+              u[t] = prow[c];
+              a[t] = tile[c * rpc + r];
+            }
+          }
+#pragma unroll
+          for (int t = 0; t < 8; ++t) {
+            const int c = c0 + t;
+            if (c > jj && c < jb) {
+              a[t].x = fmaf(-l.x, u[t].x, fmaf(l.y, u[t].y, a[t].x));
+              a[t].y = fmaf(-l.x, u[t].y, fmaf(-l.y, u[t].x, a[t].y));
+              tile[c * rpc + r] = a[t];
+            }
+          }
         }
       }
     }
