@@ -377,6 +377,173 @@ k_getf2_cluster_push(float2* __restrict__ P, long lda, int m, int jb, int rpc, i
   cluster.sync();  // no CTA leaves while a copy into its shared memory could be pending
 }
 
+// Register-resident form of the pushed-candidate panel, for panels of at
+// most 512 rows per CTA: each thread keeps its one row of the panel (32
+// complex values) in registers for all 32 column steps.  The shared-memory
+// form loads and stores every element of the trailing panel through shared
+// memory at every column (about 60 shared-memory wavefronts per column per
+// SM, the bound of its update); here the update is register FMAs with the
+// pivot row read as broadcast 16-byte loads, and the owners of the candidate
+// row and of row jj write their rows into the message themselves.  The
+// candidate's owner also sends the reciprocal of its pivot value, so the
+// other threads do no division.  Same pivot rule, message protocol and
+// bounded waits as k_getf2_cluster_push.
+struct __align__(16) PanelMsgR {
+  float val;
+  int idx;
+  float2 rcp;               // 1 / candidate[jj] (from the candidate's owner)
+  float2 cand[kClusterNB];  // the candidate row
+  float2 jrow[kClusterNB];  // row jj, from its owner only
+};
+static_assert(sizeof(PanelMsgR) % 16 == 0, "bulk copies move multiples of 16 bytes");
+
+__device__ __forceinline__ float2 pick32(const float2 (&a)[kClusterNB], int j) {
+  float2 x = a[0];
+#pragma unroll
+  for (int c = 1; c < kClusterNB; ++c)
+    if (c == j) x = a[c];
+  return x;
+}
+
+__global__ void __launch_bounds__(kClusterThreads, 1)
+k_getf2_cluster_reg(float2* __restrict__ P, long lda, int m, int jb, int rpc, int* __restrict__ ipiv, int k0,
+                    int* __restrict__ info) {
+  constexpr int kWarps = kClusterThreads / 32;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  __shared__ PanelMsgR sendbuf[2];
+  __shared__ PanelMsgR recv[2][kClusterCTAs];
+  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ float red_v[kWarps];
+  __shared__ int red_i[kWarps];
+  __shared__ int s_bad;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int r0 = rank * rpc;
+  const int rl = max(0, min(rpc, m - r0));
+  const bool own = tid < rl;
+  const int gr = r0 + tid;
+  constexpr uint32_t kMsgBytes = sizeof(PanelMsgR);
+  float2 a[kClusterNB];
+  {
+    const float2* q = P + gr;  // a running pointer: no column address stays live through the steps
+#pragma unroll
+    for (int c = 0; c < kClusterNB; ++c, q += lda) a[c] = (own && c < jb) ? *q : make_float2(0.f, 0.f);
+  }
+  if (tid == 0) {
+    s_bad = 0;
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    mbar_expect_tx(&mbar[0], kClusterCTAs * kMsgBytes);
+    if (jb > 1) mbar_expect_tx(&mbar[1], kClusterCTAs * kMsgBytes);
+  }
+  cluster.sync();  // barriers initialised and armed everywhere before any copy
+
+  bool bad = false;
+  // Fully unrolled: every column index below is a compile-time constant, so
+  // the row stays in registers without selects and the update touches only
+  // the columns right of jj.
+#pragma unroll
+  for (int jj = 0; jj < kClusterNB; ++jj) {
+    if (jj >= jb) break;
+    const int q = jj & 1;
+    const int oj = jj / rpc;
+    // (a) this CTA's candidate for column jj (rows >= jj), reduced by every warp
+    const float2 x = pick32(a, jj);
+    float v = (own && gr >= jj) ? fabsf(x.x) + fabsf(x.y) : -1.f;
+    int idx = (own && gr >= jj) ? gr : INT_MAX;
+    warp_best(v, idx);
+    if (lane == 0) { red_v[warp] = v; red_i[warp] = idx; }
+    __syncthreads();  // (the previous column's message slots were read before this barrier too)
+    v = (lane < kWarps) ? red_v[lane] : -1.f;
+    idx = (lane < kWarps) ? red_i[lane] : INT_MAX;
+    warp_best(v, idx);
+    // (b) the owners write the message: header and candidate row, row jj
+    PanelMsgR& msg = sendbuf[q];
+    if (idx == INT_MAX) {
+      if (tid == 0) { msg.val = -1.f; msg.idx = INT_MAX; }
+    } else if (own && gr == idx) {
+      msg.val = v;
+      msg.idx = idx;
+      msg.rcp = (x.x != 0.f || x.y != 0.f) ? c_recip(x) : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int c = 0; c < kClusterNB; ++c) msg.cand[c] = a[c];
+    }
+    if (own && gr == jj) {
+#pragma unroll
+      for (int c = 0; c < kClusterNB; ++c) msg.jrow[c] = a[c];
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (warp == 0 && lane < kClusterCTAs) {
+      const uint32_t dst = mapa_shared(smem_addr(&recv[q][rank]), lane);
+      const uint32_t bar = mapa_shared(smem_addr(&mbar[q]), lane);
+      bulk_s2s_cluster(dst, smem_addr(&msg), kMsgBytes, bar);
+    }
+    // (c) wait for the 16 messages of this column
+    if (!mbar_wait_timed(&mbar[q], (jj >> 1) & 1, kPanelWaitNs)) bad = true;
+    if (__syncthreads_or(bad)) {
+      if (tid == 0) s_bad = 1;
+      break;
+    }
+    if (tid == 0 && jj + 2 < jb) mbar_expect_tx(&mbar[q], kClusterCTAs * kMsgBytes);
+    // (d) the pivot: every warp reduces the 16 local messages
+    float pmax = (lane < kClusterCTAs) ? recv[q][lane].val : -1.f;
+    int p = (lane < kClusterCTAs) ? recv[q][lane].idx : INT_MAX;
+    warp_best(pmax, p);
+    if (p == INT_MAX) p = jj;
+    const int op = p / rpc;
+    const PanelMsgR& pm = recv[q][op];
+    const bool swap = pmax > 0.f && p != jj;
+    if (rank == 0 && tid == 0) {
+      ipiv[k0 + jj] = k0 + p + 1;
+      if (!(pmax > 0.f) && *info == 0) *info = k0 + jj + 1;
+    }
+    // (e) row jj becomes the pivot row; the owner of row p takes old row jj; update below jj
+    if (own && swap && gr == jj) {
+#pragma unroll
+      for (int c = 0; c < kClusterNB; ++c) a[c] = pm.cand[c];
+    } else if (own && swap && gr == p) {
+      const float2* jrow = recv[q][oj].jrow;
+#pragma unroll
+      for (int c = 0; c < kClusterNB; ++c) a[c] = jrow[c];
+    }
+    if (pmax > 0.f && own && gr > jj) {
+      const float2 rp = pm.rcp;
+      const float2 l = c_mul(pick32(a, jj), rp);
+#pragma unroll
+      for (int c = 0; c < kClusterNB; ++c)
+        if (c == jj) a[c] = l;
+      // columns >= jb hold zeros in every row and in the pivot row and are never stored
+      const float4* u4 = reinterpret_cast<const float4*>(pm.cand);
+#pragma unroll
+      for (int c2 = 0; c2 < kClusterNB / 2; ++c2) {
+        if (2 * c2 + 1 > jj) {
+          const float4 uu = u4[c2];
+          if (2 * c2 > jj) {
+            a[2 * c2].x = fmaf(-l.x, uu.x, fmaf(l.y, uu.y, a[2 * c2].x));
+            a[2 * c2].y = fmaf(-l.x, uu.y, fmaf(-l.y, uu.x, a[2 * c2].y));
+          }
+          a[2 * c2 + 1].x = fmaf(-l.x, uu.z, fmaf(l.y, uu.w, a[2 * c2 + 1].x));
+          a[2 * c2 + 1].y = fmaf(-l.x, uu.w, fmaf(-l.y, uu.z, a[2 * c2 + 1].y));
+        }
+        if ((c2 & 3) == 3) asm volatile("" ::: "memory");  // keep at most 8 columns of loads in flight
+      }
+    }
+  }
+  __syncthreads();
+  if (s_bad) {
+    if (rank == 0 && tid == 0) *info = kPanelTimeout;
+  } else if (own) {
+    float2* q = P + gr;
+#pragma unroll
+    for (int c = 0; c < kClusterNB; ++c, q += lda) {
+      asm volatile("" : "+l"(q));  // computed here, not kept from the loads
+      if (c < jb) *q = a[c];
+    }
+  }
+  cluster.sync();  // no CTA leaves while a copy into its shared memory could be pending
+}
+
 template <typename R>
 cudaError_t panel_cluster_smem(cudaStream_t st, typename cx<R>::T* P, long lda, int m, int jb, int* ipiv, int k0,
                                int* info) {
@@ -419,6 +586,23 @@ template <>
 cudaError_t panel_cluster<float>(cudaStream_t st, float2* P, long lda, int m, int jb, int* ipiv, int k0, int* info) {
   if (jb > kClusterNB) return cudaErrorNotSupported;
   const int rpc = (m + kClusterCTAs - 1) / kClusterCTAs;
+  if (rpc <= kClusterThreads) {  // one row per thread: the register-resident panel
+    cudaError_t e = cudaFuncSetAttribute(k_getf2_cluster_reg, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kClusterCTAs, 1, 1);
+    cfg.blockDim = dim3(kClusterThreads, 1, 1);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kClusterCTAs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_getf2_cluster_reg, P, lda, m, jb, rpc, ipiv, k0, info);
+  }
   const size_t smem = (size_t)rpc * jb * sizeof(float2);
   if (smem > (size_t)(kPanelSmemMax - kPushStaticSmem)) return panel_cluster_smem<float>(st, P, lda, m, jb, ipiv, k0, info);
   cudaError_t e = cudaFuncSetAttribute(k_getf2_cluster_push, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);

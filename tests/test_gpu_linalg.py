@@ -88,12 +88,13 @@ def test_gesv_fp64_with_row_interchanges(solver, n, nrhs):
         assert _rel(x, x_ref) < 1e-10
 
 
-@pytest.mark.parametrize("n,nrhs", PIVOT_SHAPES + [(2100, 8)])
+@pytest.mark.parametrize("n,nrhs", PIVOT_SHAPES + [(2100, 8), (8400, 4)])
 def test_gesv_mixed_with_row_interchanges(solver, n, nrhs):
     """The complex64 LU (cluster panels, fused interchanges, tensor-core
-    updates from order 1024) on Gaussian matrices: LAPACK's pivot sequence
-    where single precision does not tie-break differently, and refinement to
-    the FP64 solution."""
+    updates from order 1024) on Gaussian matrices, refined to the FP64
+    solution.  Order 8400 takes both panel forms: the shared-memory panel
+    while a panel has more than 16 x 512 rows, the register-resident one
+    after."""
     rng = np.random.default_rng(2000 + n)
     a = np.asfortranarray(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
     b = np.asfortranarray(rng.standard_normal((n, nrhs)) + 1j * rng.standard_normal((n, nrhs)))
