@@ -228,16 +228,19 @@ cudaError_t launch_wide(cudaStream_t st, int m, int n, int k, float2 alpha, cons
 // ---------------------------------------------------------------------------
 // Skinny products, N <= 48 (the blocked triangular solves' updates
 // B2 -= L21 X1 with all right-hand sides at once): 32 rows x CW = 8*CPT
-// columns per CTA, 256 threads (one row x CPT columns each; eight warps so
-// that an SM holding one or two CTAs still has enough warps to issue), 32-deep
-// stages double-buffered by cp.async.  Small tiles give enough CTAs to
-// fill the GPU without splitting K.
+// columns per CTA, 512 threads: one row x CPT columns each, the two halves
+// of the CTA taking the two halves of every 32-deep stage and adding their
+// sums in shared memory at the end.  The triangular solves' updates give
+// at most ~190 such tiles, so an SM holds one CTA and its time is the
+// solve's latency: sixteen warps instead of eight halve the instructions
+// each warp issues.  Small tiles give enough CTAs to fill the GPU without
+// splitting K across CTAs.
 // ---------------------------------------------------------------------------
 // Four stages in flight (80 KB of dynamic shared memory at 48 columns): the
 // products this kernel serves (a 256-deep block of L or U times the
 // right-hand sides) read their A block once from HBM, so the copies in
 // flight per SM, not the FMAs, set their speed.
-constexpr int kSRows = 32, kSK = 32, kSThreads = 256, kSMaxCW = 48, kSStages = 4;
+constexpr int kSRows = 32, kSK = 32, kSThreads = 512, kSMaxCW = 48, kSStages = 4;
 // Row stride of the B stage in shared memory: CW + 2 complex, so that the
 // 32 consecutive k of one column that a warp copies land on 8 bank pairs
 // (4-way) instead of one (32-way at the bare 48-column stride), and rows
@@ -285,7 +288,7 @@ k_cgemm_skinny(int m, int n, int k, float2 alpha, const float2* __restrict__ A, 
   extern __shared__ __align__(16) float2 s_skinny[];
   float2* As = s_skinny;                            // [kSStages][kSK * kSRows]
   float2* Bs = s_skinny + kSStages * kSK * kSRows;  // [kSStages][kSK * BST]
-  const int tid = threadIdx.x, tx = tid & 31, cg = tid >> 5;
+  const int tid = threadIdx.x, tx = tid & 31, cg = (tid >> 5) & 7, kh = tid >> 8;
   const int m0 = blockIdx.x * kSRows;
   float ar[CPT], ai[CPT];
 #pragma unroll
@@ -309,7 +312,7 @@ k_cgemm_skinny(int m, int n, int k, float2 alpha, const float2* __restrict__ A, 
     const float2* as = As + b * kSK * kSRows;
     const float2* bs = Bs + b * kSK * BST + cg * CPT;
 #pragma unroll 4
-    for (int l = 0; l < kSK; ++l) {
+    for (int l = kh * (kSK / 2); l < (kh + 1) * (kSK / 2); ++l) {
       const float2 a = as[l * kSRows + tx];
 #pragma unroll
       for (int j = 0; j < CPT; j += 2) {
@@ -324,6 +327,23 @@ k_cgemm_skinny(int m, int n, int k, float2 alpha, const float2* __restrict__ A, 
         ai[j + 1] = fmaf(a.y, bb.z, ai[j + 1]);
       }
     }
+  }
+  // the upper half's sums join the lower half's (the stage buffers are free
+  // once every copy has landed and every thread has left the loop)
+  cp_async_wait<0>();
+  __syncthreads();
+  float2* red = s_skinny;  // [CPT][8 column groups][32 rows]
+  if (kh == 1) {
+#pragma unroll
+    for (int j = 0; j < CPT; ++j) red[(j * 8 + cg) * 32 + tx] = make_float2(ar[j], ai[j]);
+  }
+  __syncthreads();
+  if (kh == 1) return;
+#pragma unroll
+  for (int j = 0; j < CPT; ++j) {
+    const float2 o = red[(j * 8 + cg) * 32 + tx];
+    ar[j] += o.x;
+    ai[j] += o.y;
   }
   const int row = m0 + tx;
   if (row >= m) return;

@@ -405,6 +405,23 @@ __device__ __forceinline__ float2 pick32(const float2 (&a)[kClusterNB], int j) {
   return x;
 }
 
+// A panel row between registers and a 16-byte aligned message row, two
+// complex values per 16-byte access.
+__device__ __forceinline__ void store_row(float2* dst, const float2 (&a)[kClusterNB]) {
+  float4* d4 = reinterpret_cast<float4*>(dst);
+#pragma unroll
+  for (int c = 0; c < kClusterNB / 2; ++c) d4[c] = make_float4(a[2 * c].x, a[2 * c].y, a[2 * c + 1].x, a[2 * c + 1].y);
+}
+__device__ __forceinline__ void load_row(float2 (&a)[kClusterNB], const float2* src) {
+  const float4* s4 = reinterpret_cast<const float4*>(src);
+#pragma unroll
+  for (int c = 0; c < kClusterNB / 2; ++c) {
+    const float4 v = s4[c];
+    a[2 * c] = make_float2(v.x, v.y);
+    a[2 * c + 1] = make_float2(v.z, v.w);
+  }
+}
+
 __global__ void __launch_bounds__(kClusterThreads, 1)
 k_getf2_cluster_reg(float2* __restrict__ P, long lda, int m, int jb, int rpc, int* __restrict__ ipiv, int k0,
                     int* __restrict__ info) {
@@ -465,12 +482,10 @@ k_getf2_cluster_reg(float2* __restrict__ P, long lda, int m, int jb, int rpc, in
       msg.val = v;
       msg.idx = idx;
       msg.rcp = (x.x != 0.f || x.y != 0.f) ? c_recip(x) : make_float2(0.f, 0.f);
-#pragma unroll
-      for (int c = 0; c < kClusterNB; ++c) msg.cand[c] = a[c];
+      store_row(msg.cand, a);
     }
     if (own && gr == jj) {
-#pragma unroll
-      for (int c = 0; c < kClusterNB; ++c) msg.jrow[c] = a[c];
+      store_row(msg.jrow, a);
     }
     fence_proxy_async_smem();
     __syncthreads();
@@ -500,12 +515,9 @@ k_getf2_cluster_reg(float2* __restrict__ P, long lda, int m, int jb, int rpc, in
     }
     // (e) row jj becomes the pivot row; the owner of row p takes old row jj; update below jj
     if (own && swap && gr == jj) {
-#pragma unroll
-      for (int c = 0; c < kClusterNB; ++c) a[c] = pm.cand[c];
+      load_row(a, pm.cand);
     } else if (own && swap && gr == p) {
-      const float2* jrow = recv[q][oj].jrow;
-#pragma unroll
-      for (int c = 0; c < kClusterNB; ++c) a[c] = jrow[c];
+      load_row(a, recv[q][oj].jrow);
     }
     if (pmax > 0.f && own && gr > jj) {
       const float2 rp = pm.rcp;

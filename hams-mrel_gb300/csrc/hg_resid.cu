@@ -239,8 +239,19 @@ cudaError_t launch_resid(cudaStream_t st, int m, int nc, int k, const float2* A,
   const int ncb = (nc + CW - 1) / CW;
   const int gx = (m + kRRows - 1) / kRRows;
   const size_t ys_bytes = align256((size_t)ncb * k * CW * sizeof(float4));
-  int slices = (2 * 152 + gx * ncb - 1) / (gx * ncb);
-  slices = max(1, min(slices, min(kRMaxSlices, (k + kRK - 1) / kRK)));
+  // Slices of the inner dimension: at least enough CTAs for two per SM, then
+  // the count (up to 16) whose CTAs fill their last wave best (95 row blocks
+  // x 4 slices would run 1.25 waves of 304 CTAs; x 16 slices, 5 full ones).
+  const int kmax = min(kRMaxSlices, (k + kRK - 1) / kRK);
+  int slices = max(1, min((2 * 152 + gx * ncb - 1) / (gx * ncb), kmax));
+  {
+    double best = 0.0;
+    for (int s = slices; s <= kmax; ++s) {
+      const long ctas = (long)gx * ncb * s;
+      const double fill = (double)ctas / (double)(((ctas + 303) / 304) * 304);
+      if (fill > best + 1e-9) { best = fill; slices = s; }
+    }
+  }
   while (slices > 1 && ys_bytes + (size_t)slices * m * nc * sizeof(double2) > ws_bytes) --slices;
   if (ys_bytes + (size_t)slices * m * nc * sizeof(double2) > ws_bytes) return cudaErrorInvalidValue;
   int kchunk = ((k + slices - 1) / slices + kRK - 1) / kRK * kRK;
