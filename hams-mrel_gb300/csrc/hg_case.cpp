@@ -863,6 +863,7 @@ void run(hg_case* c, const char* output_dir, const hg_opts* opts, int nslots) {
   hg_opts o;
   if (opts) o = *opts;
   else hg_default_opts(&o);
+  o.solver = c->isolv;  // the deck's Solver_type (ISOLV) picks the linear solver
   hg_ctx* ctx = nullptr;
   int rc = hg_create(&ctx, &o);
   if (rc) raise(rc, "hg_create failed (%d): no usable CUDA device?", rc);

@@ -97,7 +97,50 @@ __global__ void k_c2z_cols(int rows, const float2* __restrict__ s, long lds, dou
   }
 }
 
+// d[i] = M[i, i] widened to complex128, with 1 where |M[i, i]| < 1e-30:
+// the Jacobi preconditioner of the iterative solver (SETUP_PRECONDITIONER,
+// IterativeSolvers.f90:156-174).
+template <typename T>
+__global__ void k_diag(int n, const T* __restrict__ M, long ldm, double2* __restrict__ d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const T v = M[i + (long)i * ldm];
+  double2 r = make_double2((double)v.x, (double)v.y);
+  if (sqrt(r.x * r.x + r.y * r.y) < 1.0e-30) r = make_double2(1.0, 0.0);
+  d[i] = r;
+}
+
+// Z[:, c] = V[:, c] / d, element by element (the Jacobi branch of
+// APPLY_PRECONDITIONER, IterativeSolvers.f90:296-304).
+__global__ void k_jacobi(int n, const double2* __restrict__ V, long ldv, const double2* __restrict__ d,
+                         double2* __restrict__ Z, long ldz) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+  if (r >= n) return;
+  const double2 v = V[r + (long)c * ldv], q = d[r];
+  const double den = q.x * q.x + q.y * q.y;
+  Z[r + (long)c * ldz] = make_double2((v.x * q.x + v.y * q.y) / den, (v.y * q.x - v.x * q.y) / den);
+}
+
 }  // namespace
+
+cudaError_t diag_extract(cudaStream_t st, int n, const double2* M, long ldm, double2* d) {
+  if (n <= 0) return cudaSuccess;
+  k_diag<double2><<<(n + 255) / 256, 256, 0, st>>>(n, M, ldm, d);
+  return cudaGetLastError();
+}
+
+cudaError_t diag_extract(cudaStream_t st, int n, const float2* M, long ldm, double2* d) {
+  if (n <= 0) return cudaSuccess;
+  k_diag<float2><<<(n + 255) / 256, 256, 0, st>>>(n, M, ldm, d);
+  return cudaGetLastError();
+}
+
+cudaError_t jacobi_apply(cudaStream_t st, int n, int nc, const double2* V, long ldv, const double2* d, double2* Z,
+                         long ldz) {
+  if (n <= 0 || nc <= 0) return cudaSuccess;
+  k_jacobi<<<dim3((n + 255) / 256, nc), 256, 0, st>>>(n, V, ldv, d, Z, ldz);
+  return cudaGetLastError();
+}
 
 cudaError_t col_dots(cudaStream_t st, int n, int nc, int nv, const double2* V, long ldv, long vstride, const double2* W,
                      long ldw, double2* H, int ldh) {

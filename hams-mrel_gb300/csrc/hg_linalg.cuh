@@ -110,6 +110,12 @@ cudaError_t col_dots(cudaStream_t st, int n, int nc, int nv, const double2* V, l
 cudaError_t col_axpy(cudaStream_t st, int n, int nc, int nv, const double2* V, long ldv, long vstride,
                      const double2* H, int ldh, double2* W, long ldw, double sign);
 cudaError_t col_norm2(cudaStream_t st, int n, int nc, const double2* W, long ldw, double* out);
+// Jacobi preconditioner of the iterative solver: d = diag(M) (1 where
+// |M_ii| < 1e-30), Z = V ./ d column by column.
+cudaError_t diag_extract(cudaStream_t st, int n, const double2* M, long ldm, double2* d);
+cudaError_t diag_extract(cudaStream_t st, int n, const float2* M, long ldm, double2* d);
+cudaError_t jacobi_apply(cudaStream_t st, int n, int nc, const double2* V, long ldv, const double2* d, double2* Z,
+                         long ldz);
 cudaError_t col_scale(cudaStream_t st, int n, int nc, const double2* W, long ldw, const double* s, double2* out,
                       long ldo);
 cudaError_t convert_c2z_2d(cudaStream_t st, int rows, int cols, const float2* src, long lds, double2* dst, long ldd);

@@ -27,6 +27,7 @@ EXPORTS = [
     "hg_solve_sweep", "hg_gmres_iterations", "hg_solve_footprint", "hg_server_create", "hg_server_submit",
     "hg_server_wait", "hg_server_stats", "hg_server_last_error", "hg_server_destroy", "hg_field_points",
     "hg_case_read", "hg_case_free", "hg_case_info", "hg_case_arrays", "hg_case_run", "hg_case_write",
+    "hg_iter_info",
 ]
 
 
@@ -34,7 +35,7 @@ class HgOpts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("precision", ctypes.c_int), ("grn_kind", ctypes.c_int),
                 ("max_refine", ctypes.c_int), ("refine_tol", ctypes.c_double), ("rho", ctypes.c_double),
                 ("g", ctypes.c_double), ("lu_tensor", ctypes.c_int), ("refine_method", ctypes.c_int),
-                ("fin_table", ctypes.c_int)]
+                ("fin_table", ctypes.c_int), ("solver", ctypes.c_int)]
 
 
 class HgRequest(ctypes.Structure):
@@ -94,6 +95,7 @@ def load(build_if_missing: bool = True):
     L.hg_green_points.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p]
     L.hg_refine_info.argtypes = [c_void_p, P(c_int), P(c_double)]
     L.hg_gmres_iterations.argtypes = [c_void_p, P(c_int)]
+    L.hg_iter_info.argtypes = [c_void_p, P(c_int), P(c_int), P(c_int), P(c_double)]
     L.hg_stage_times.argtypes = [c_void_p, P(ctypes.c_float)]
     L.hg_green_points_noalloc.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p]
     L.hg_gesv.argtypes = [c_void_p, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_void_p, c_int, P(c_int),
@@ -179,7 +181,7 @@ class Solver:
 
     def __init__(self, precision: int = HG_PREC_FP64, device: int = 0, grn_kind: int = 8,
                  max_refine: int = 10, refine_tol: float = 1e-10, rho: float = 1000.0, g: float = 9.80665,
-                 lu_tensor: int = 3, refine_method: int = 0, fin_table: int = -1):
+                 lu_tensor: int = 3, refine_method: int = 0, fin_table: int = -1, solver: int = 1):
         self.L = load()
         opts = HgOpts()
         self.L.hg_default_opts(ctypes.byref(opts))
@@ -188,6 +190,7 @@ class Solver:
         opts.lu_tensor = lu_tensor
         opts.refine_method = refine_method
         opts.fin_table = fin_table
+        opts.solver = solver
         h = ctypes.c_void_p()
         rc = self.L.hg_create(ctypes.byref(h), ctypes.byref(opts))
         if rc != 0:
@@ -381,6 +384,14 @@ class Solver:
         it = ctypes.c_int()
         self.L.hg_gmres_iterations(self.h, ctypes.byref(it))
         return it.value
+
+    def iter_info(self):
+        """(iterations, restarts, unconverged columns, worst ||r||/||b||) of the last
+        solve with solver = 2."""
+        it, rs, un = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        r = ctypes.c_double()
+        self._check(self.L.hg_iter_info(self.h, ctypes.byref(it), ctypes.byref(rs), ctypes.byref(un), ctypes.byref(r)))
+        return it.value, rs.value, un.value, r.value
 
     def refine_info(self):
         s = ctypes.c_int(); r = ctypes.c_double()

@@ -61,9 +61,17 @@ typedef struct {
                             per pair from a few thousand panels; A, B, F within 1e-5..6e-4 of the
                             FP64 form, the worst where PIDCOCK's near-surface values are noisy):
                             1 on, 0 off (FP64 per pair), -1 automatic (on from 1e6 pairs; default) */
+    int solver;          /* linear solver, the ControlFile's Solver_type (ISOLV, src/HAMS_Prog.f90:161):
+                            1 = LU and triangular solves (default); 2 = restarted GMRES(25) of
+                            src/IterativeSolvers.f90:324-488 on the dense matrix in device memory,
+                            stopping at ||r||_2 < 1e-4 ||b||_2 per right-hand side or after 100
+                            iterations, right-preconditioned by Jacobi (one body) or by the LU of
+                            each body's diagonal block (several bodies), as the reference's
+                            ZBLOCK_GMRES_SOLVE; hg_fill_factor then factors only those blocks */
 } hg_opts;
 
-/* Fill opts with the defaults above (device 0, FP64, GRN_KIND 8, rho 1000, g 9.80665, lu_tensor 3). */
+/* Fill opts with the defaults above (device 0, FP64, GRN_KIND 8, rho 1000, g 9.80665, lu_tensor 3,
+ * solver 1). */
 void hg_default_opts(hg_opts *opts);
 
 /* Create / destroy a context.  opts may be NULL for the defaults. */
@@ -306,6 +314,12 @@ int hg_refine_info(const hg_ctx *ctx, int *sweeps, double *residual);
 /* GMRES iterations (preconditioned operator applications) of the last mixed-form solve
  * with refine_method = 1 (0 otherwise). */
 int hg_gmres_iterations(const hg_ctx *ctx, int *iterations);
+/* Outcome of the last solve with opts.solver = 2: Arnoldi steps taken (the largest over the
+ * right-hand sides, <= 100), restart cycles, right-hand sides left above the tolerance after
+ * 100 steps (the reference prints "GMRES did not converge" for each; their solution is the
+ * last iterate), and the largest final ||r||_2 / ||b||_2 estimate.  HG_ERR_STATE when
+ * opts.solver is not 2. */
+int hg_iter_info(const hg_ctx *ctx, int *iterations, int *restarts, int *unconverged, double *residual);
 
 /* CUDA events on the context's stream, for callers that time a sequence of
  * calls on the device: hg_mark records event slot (0..15); hg_elapsed waits

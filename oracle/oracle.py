@@ -492,6 +492,117 @@ def lu_solve(M: np.ndarray, B: np.ndarray) -> np.ndarray:
     return x
 
 
+def gmres_precond(M: np.ndarray, blocks=None):
+    """The right preconditioner of the reference's GMRES, as a function
+    r -> z.  blocks None: Jacobi, z = r / diag(M) with 1 where |M_ii| < 1e-30
+    (SETUP_PRECONDITIONER, src/IterativeSolvers.f90:156-174, and
+    APPLY_PRECONDITIONER :296-304).  blocks [(start, size), ...]: LU factors
+    of each diagonal block (SETUP_BLOCK_PRECONDITIONER :190-262; APPLY
+    :276-293)."""
+    from scipy.linalg import lapack
+    if blocks is None:
+        d = np.diag(M).astype(np.complex128).copy()
+        d[np.abs(d) < 1e-30] = 1.0
+        return lambda r: r / d
+    facs = []
+    for s0, sz in blocks:
+        lu, piv, _ = lapack.zgetrf(np.asfortranarray(M[s0:s0 + sz, s0:s0 + sz]))
+        facs.append((s0, sz, lu, piv))
+
+    def apply(r):
+        z = np.array(r, dtype=np.complex128)
+        for s0, sz, lu, piv in facs:
+            z[s0:s0 + sz], _ = lapack.zgetrs(lu, piv, z[s0:s0 + sz])
+        return z
+    return apply
+
+
+def _givens(a, b):
+    """ZGIVENS_ROTATION (src/IterativeSolvers.f90:490-530)."""
+    if abs(b) < 1e-300:
+        return 1.0 + 0j, 0j
+    if abs(a) < 1e-300:
+        return 0j, 1.0 + 0j
+    den = math.sqrt(abs(a) ** 2 + abs(b) ** 2)
+    return abs(a) / den + 0j, (a / abs(a)) * np.conj(b) / den
+
+
+def gmres_solve(M: np.ndarray, b: np.ndarray, precond, tol=1e-4, maxit=100, restart=25):
+    """ZGMRES_SOLVE (src/IterativeSolvers.f90:324-488): restarted GMRES(m)
+    with right preconditioning, modified Gram-Schmidt and Givens rotations,
+    x0 = 0, stop when ||r||_2 / ||b||_2 < tol or after maxit Arnoldi steps.
+    Returns (x, iterations, info) with info 0 converged, 1 not."""
+    n = M.shape[0]
+    x = np.zeros(n, dtype=np.complex128)
+    bnorm = np.linalg.norm(b)
+    if bnorm < 1e-30:
+        return x, 0, 0
+    it, info = 0, 1
+    while it < maxit:
+        r = b.copy() if it == 0 else b - M @ x
+        beta = np.linalg.norm(r)
+        if beta / bnorm < tol:
+            info = 0
+            break
+        V = np.zeros((n, restart + 1), dtype=np.complex128)
+        H = np.zeros((restart + 1, restart), dtype=np.complex128)
+        cs = np.zeros(restart, dtype=np.complex128)
+        sn = np.zeros(restart, dtype=np.complex128)
+        g = np.zeros(restart + 1, dtype=np.complex128)
+        V[:, 0] = r / beta
+        g[0] = beta
+        mact = 0
+        for j in range(restart):
+            it += 1
+            if it > maxit:
+                break
+            w = M @ precond(V[:, j])
+            for i in range(j + 1):
+                H[i, j] = np.vdot(V[:, i], w)
+                w = w - H[i, j] * V[:, i]
+            H[j + 1, j] = np.linalg.norm(w)
+            if abs(H[j + 1, j]) > 1e-30:
+                V[:, j + 1] = w / H[j + 1, j]
+            for i in range(j):
+                t = cs[i] * H[i, j] + sn[i] * H[i + 1, j]
+                H[i + 1, j] = -np.conj(sn[i]) * H[i, j] + np.conj(cs[i]) * H[i + 1, j]
+                H[i, j] = t
+            cs[j], sn[j] = _givens(H[j, j], H[j + 1, j])
+            H[j, j] = cs[j] * H[j, j] + sn[j] * H[j + 1, j]
+            H[j + 1, j] = 0
+            t = cs[j] * g[j] + sn[j] * g[j + 1]
+            g[j + 1] = -np.conj(sn[j]) * g[j] + np.conj(cs[j]) * g[j + 1]
+            g[j] = t
+            mact = j + 1
+            if abs(g[j + 1]) / bnorm < tol:
+                info = 0
+                break
+        if mact > 0:
+            y = g[:mact].copy()
+            for i in range(mact - 1, -1, -1):
+                y[i] = 0 if abs(H[i, i]) < 1e-30 else y[i] / H[i, i]
+                y[:i] -= H[:i, i] * y[i]
+            for j in range(mact):
+                x += y[j] * precond(V[:, j])
+        if info == 0:
+            break
+    return x, min(it, maxit), info
+
+
+def gmres_columns(M: np.ndarray, B: np.ndarray, blocks=None, **kw):
+    """ZBLOCK_GMRES_SOLVE (src/IterativeSolvers.f90:535-562): every column
+    separately with the same preconditioner.  Returns (X, iterations per
+    column, info per column)."""
+    P = gmres_precond(M, blocks)
+    X = np.zeros(B.shape, dtype=np.complex128)
+    its, infos = [], []
+    for k in range(B.shape[1]):
+        X[:, k], it, info = gmres_solve(M, B[:, k], P, **kw)
+        its.append(it)
+        infos.append(info)
+    return X, its, infos
+
+
 def normal_equations(case: Case, A: np.ndarray, B: np.ndarray):
     L = lib()
     tn, n = A.shape
@@ -551,8 +662,17 @@ def forces(case: Case, mxpot: np.ndarray, v, wk, w1, betas_rad):
     return amas, bdmp, exfc
 
 
+def body_blocks(case: Case):
+    """Diagonal blocks of the block preconditioner: one per body's hull
+    panels (NELEM_MULTI), none for a single body (Jacobi)."""
+    if case.nbody == 1:
+        return None
+    return [(int(case.body_start[b]), int(case.body_end[b] - case.body_start[b])) for b in range(case.nbody)]
+
+
 def solve_frequency(case: Case, value: float, grn_kind: int = 8, nthreads: int = 0,
-                    betas_deg=None) -> FreqResult:
+                    betas_deg=None, solver: int = 1) -> FreqResult:
+    """One frequency; solver 1 = ZGETRF/ZGETRS, 2 = the GMRES of ISOLV = 2."""
     v, wk, w1, wvn = wave_properties(case.ctl, value)
     if betas_deg is None:
         betas_deg = case.ctl.headings
@@ -560,10 +680,13 @@ def solve_frequency(case: Case, value: float, grn_kind: int = 8, nthreads: int =
     A, S = assemble(case, v, wvn, grn_kind, nthreads)
     B = rhs(case, S, v, wk, w1, betas)
     if case.nl > 0:
-        C, D = normal_equations(case, A, B)
-        X = lu_solve(C, D)
+        M, R = normal_equations(case, A, B)
     else:
-        X = lu_solve(np.asfortranarray(A), np.asfortranarray(B))
+        M, R = np.asfortranarray(A), np.asfortranarray(B)
+    if solver == 2:
+        X = gmres_columns(M, R, body_blocks(case))[0]
+    else:
+        X = lu_solve(M, R)
     amas, bdmp, exfc = forces(case, X, v, wk, w1, betas)
     return FreqResult(w1, wk, amas, bdmp, exfc, X)
 

@@ -18,6 +18,10 @@ files) of three reference cases into tests/golden/<case>/:
                                          2 bodies with lids and generalized
                                          modes, IRSP = 1
 
+and the control file of the reference's GMRES integration test
+(test/data/config1_gmres: config1's deck with Solver_type 2; its meshes are
+config1's) into tests/golden/config1_gmres/.
+
 The GPU machine has no copy of the reference, so the tests read only these
 committed files.
 """
@@ -59,6 +63,10 @@ def main(ref_root: str) -> None:
                 src = os.path.join(ref_root, out, name)
                 if os.path.exists(src):
                     shutil.copy(src, os.path.join(dst_out, os.path.basename(name)))
+    dst = os.path.join(here, "config1_gmres")
+    os.makedirs(dst, exist_ok=True)
+    shutil.copy(os.path.join(ref_root, "test/data/config1_gmres/input/ControlFile.in"),
+                os.path.join(dst, "ControlFile.in"))
 
 
 if __name__ == "__main__":
