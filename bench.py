@@ -231,7 +231,8 @@ def ours(args, dist, rank, world, local):
         vals = [_frequency_inputs(pkg, w) for w in ws]
         return (np.array([x[0] for x in vals]), np.array([x[1] for x in vals]), np.array([x[2] for x in vals]))
 
-    sopts = dict(lu_tensor=args.lu_tensor, refine_method=1 if args.refine == "gmres" else 0)
+    sopts = dict(lu_tensor=args.lu_tensor, refine_method=1 if args.refine == "gmres" else 0,
+                 solver=2 if args.solver == "gmres" else 1)
     s = hg.Solver(precision=prec, device=local, **sopts)
     s.set_mesh(mesh.nodes, mesh.ncon, mesh.ncn, mesh.xyz_p, mesh.ds, mesh.pnsz, mesh.dxyz_p, mesh.body_ranges)
     # warm-up: at least one frequency per slot, so that every slot has its buffers
@@ -254,6 +255,7 @@ def ours(args, dist, rank, world, local):
     # stage breakdown of one frequency-solve running alone (outside the timed region)
     s.solve_frequency(v[0], wk[0], w1[0], -1.0, None, betas, want_potentials=False)
     stages = s.stage_times()
+    iters = s.iter_info() if args.solver == "gmres" else None
 
     # ---- end to end through the C ABI with host buffers: new context, mesh upload,
     #      the sweep, forces and all potentials read back to host memory ----
@@ -295,7 +297,7 @@ def ours(args, dist, rank, world, local):
 
     # ---- roofline of the dominant kernel (the LU trailing-update GEMM) ----
     roof = None
-    if rank == 0:
+    if rank == 0 and args.solver == "lu":
         roof = _roofline(s, mesh.n, prec, hg)
     s.close()
     if rank != 0:
@@ -307,7 +309,7 @@ def ours(args, dist, rank, world, local):
             "dtype": "complex64+fp64-refine" if prec == hg.HG_PREC_MIXED else "complex128",
             "data": "synthetic",
             "config": dict(CONFIG, precision=args.precision, parallelism=f"replicas{world}", slots=nslots,
-                           refine=args.refine, lu_tensor=args.lu_tensor),
+                           refine=args.refine, lu_tensor=args.lu_tensor, solver=args.solver),
             "latency_ms": {"p50": lat_sorted[len(lat) // 2], "p99": lat_sorted[min(len(lat) - 1,
                                                                                   int(0.99 * len(lat)))],
                            "what": f"host wall time per frequency-solve with {nslots} solves in flight"},
@@ -316,8 +318,13 @@ def ours(args, dist, rank, world, local):
             "refine": {"sweeps": sweeps, "residual": resid},
             "e2e": {"value": world * args.steps / t_e2e, "unit": "freq-solves/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
-            "gpu_launches": _launch_count(mesh.n, prec, sweeps) * args.steps,
+            "gpu_launches": _launch_count(mesh.n, prec, sweeps) * args.steps if iters is None else None,
             "clocks": clocks, "roofline": roof, "fp64_form": fp64}
+    if iters is not None:
+        line["iterative"] = {"what": "solver 2 (restarted GMRES(25), tolerance 1e-4), one frequency alone",
+                             "iterations": iters[0], "restarts": iters[1], "unconverged": iters[2],
+                             "residual": iters[3]}
+        del line["refine"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = _cpu_baseline_sample()
     print(json.dumps(line), flush=True)
@@ -590,6 +597,8 @@ def main():
                     help="mixed-form refinement: classical iterative refinement or GMRES-IR")
     ap.add_argument("--lu-tensor", type=int, default=3, choices=[0, 1, 3],
                     help="LU trailing updates: 3 split-TF32 tensor cores, 1 TF32, 0 FP32 SIMT")
+    ap.add_argument("--solver", default="lu", choices=["lu", "gmres"],
+                    help="array workload: linear solver (gmres = the reference's Solver_type 2)")
     ap.add_argument("--workload", default="array", choices=["array", "batch", "serve", "three", "field"],
                     help="array: the 6048-panel frequency sweep (headline); batch / serve: the request server")
     ap.add_argument("--requests", type=int, default=None, help="batch / serve: number of requests")
