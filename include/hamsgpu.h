@@ -371,7 +371,8 @@ int hg_stage_times(const hg_ctx *ctx, float *ms4);
  *   dinfo[2]  = h, refl
  *   freq[6*nper] = (V, WK, W1, TP, WL, OUFR) per entry
  * hg_case_run solves and writes (nslots frequencies in flight, as
- * hg_solve_sweep; one at a time when field points are written).
+ * hg_solve_sweep; one at a time when field points are written); the deck's
+ * Solver_type (src/InputFiles.f90:177-191) sets opts->solver.
  * hg_case_write writes the result files from given A, B, F (per entry
  * blocks as hg_solve_sweep returns them).  Errors: non-zero return, message
  * in err[errlen].  Symmetry planes (ISX/ISY) are rejected. */
