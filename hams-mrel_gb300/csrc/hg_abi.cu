@@ -87,6 +87,9 @@ struct hg_ctx {
   DevBuf<float2> pbf;
   DevBuf<int> pp, pinfo;
   std::vector<size_t> poff;
+  std::vector<cudaStream_t> pst;         // side streams for the per-body blocks
+  std::vector<cudaEvent_t> pev;
+  cudaEvent_t pfork = nullptr;
   int iter_unconv = 0;                   // columns the iterative solver left above its tolerance
   // field points (hg_field_points): coordinates, on-body flags, DUM2 / DUM1 rows, weights, potentials
   DevBuf<double> fpx;
@@ -410,6 +413,36 @@ IterMat iter_mat(const hg_ctx* c) {
   return r;
 }
 
+// The per-body blocks of the preconditioner are independent, and each
+// block's LU and triangular solves are latency-bound chains (cluster panels
+// on 16 SMs), so the blocks run side by side on up to 8 side streams forked
+// from and joined back to the context's stream.
+constexpr int kBlockStreams = 8;
+int fork_blocks(hg_ctx* c) {
+  const int ns = std::min(c->nbody, kBlockStreams);
+  while ((int)c->pst.size() < ns) {
+    cudaStream_t s = nullptr;
+    cudaEvent_t e = nullptr;
+    CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    c->pst.push_back(s);
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    c->pev.push_back(e);
+  }
+  if (!c->pfork) CK(cudaEventCreateWithFlags(&c->pfork, cudaEventDisableTiming));
+  CK(cudaEventRecord(c->pfork, c->st));
+  for (int k = 0; k < ns; ++k) CK(cudaStreamWaitEvent(c->pst[k], c->pfork, 0));
+  return 0;
+}
+int join_blocks(hg_ctx* c) {
+  const int ns = std::min(c->nbody, kBlockStreams);
+  for (int k = 0; k < ns; ++k) {
+    CK(cudaEventRecord(c->pev[k], c->pst[k]));
+    CK(cudaStreamWaitEvent(c->st, c->pev[k], 0));
+  }
+  return 0;
+}
+cudaStream_t block_stream(const hg_ctx* c, int b) { return c->pst[b % kBlockStreams]; }
+
 int setup_iter_precond(hg_ctx* c) {
   const int n = c->n;
   const IterMat im = iter_mat(c);
@@ -428,24 +461,27 @@ int setup_iter_precond(hg_ctx* c) {
   }
   CK(c->pp.ensure(n));
   CK(c->pinfo.ensure(c->nbody));
+  if (im.Mf) CK(c->pbf.ensure(tot));
+  else CK(c->pb.ensure(tot));
+  int r = fork_blocks(c);
+  if (r) return r;
   for (int b = 0; b < c->nbody; ++b) {
     const int s0 = c->bstart[b], sz = c->bend[b] - c->bstart[b];
+    cudaStream_t bs = block_stream(c, b);
     if (im.Mf) {
-      CK(c->pbf.ensure(tot));
       float2* blk = c->pbf.p + c->poff[b];
       CK(cudaMemcpy2DAsync(blk, (size_t)sz * sizeof(float2), im.Mf + s0 + (size_t)s0 * im.ld, (size_t)im.ld * sizeof(float2),
-                           (size_t)sz * sizeof(float2), sz, cudaMemcpyDeviceToDevice, c->st));
-      CK(hg::getrf<float>(c->st, sz, blk, sz, c->pp.p + s0, c->pinfo.p + b, nullptr));
+                           (size_t)sz * sizeof(float2), sz, cudaMemcpyDeviceToDevice, bs));
+      CK(hg::getrf<float>(bs, sz, blk, sz, c->pp.p + s0, c->pinfo.p + b, nullptr));
     } else {
-      CK(c->pb.ensure(tot));
       double2* blk = c->pb.p + c->poff[b];
       CK(cudaMemcpy2DAsync(blk, (size_t)sz * sizeof(double2), im.M + s0 + (size_t)s0 * im.ld,
                            (size_t)im.ld * sizeof(double2), (size_t)sz * sizeof(double2), sz, cudaMemcpyDeviceToDevice,
-                           c->st));
-      CK(hg::getrf<double>(c->st, sz, blk, sz, c->pp.p + s0, c->pinfo.p + b, nullptr));
+                           bs));
+      CK(hg::getrf<double>(bs, sz, blk, sz, c->pp.p + s0, c->pinfo.p + b, nullptr));
     }
   }
-  return 0;
+  return join_blocks(c);
 }
 
 // Z = P^-1 V (n x nc blocks, leading dimension n): APPLY_PRECONDITIONER
@@ -456,21 +492,19 @@ int iter_precond(hg_ctx* c, int nc, const double2* V, double2* Z) {
     CK(hg::jacobi_apply(c->st, n, nc, V, n, c->pd.p, Z, n));
     return 0;
   }
-  if (mixed(c)) {
-    float2* Bf = c->Bf.p;
-    CK(hg::convert_z2c_2d(c->st, n, nc, V, n, Bf, n));
-    for (int b = 0; b < c->nbody; ++b) {
-      const int s0 = c->bstart[b], sz = c->bend[b] - c->bstart[b];
-      CK(hg::getrs<float>(c->st, sz, nc, c->pbf.p + c->poff[b], sz, c->pp.p + s0, Bf + s0, n));
-    }
-    CK(hg::convert_c2z_2d(c->st, n, nc, Bf, n, Z, n));
-  } else {
-    CK(cudaMemcpyAsync(Z, V, (size_t)n * nc * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
-    for (int b = 0; b < c->nbody; ++b) {
-      const int s0 = c->bstart[b], sz = c->bend[b] - c->bstart[b];
-      CK(hg::getrs<double>(c->st, sz, nc, c->pb.p + c->poff[b], sz, c->pp.p + s0, Z + s0, n));
-    }
+  float2* Bf = c->Bf.p;
+  if (mixed(c)) CK(hg::convert_z2c_2d(c->st, n, nc, V, n, Bf, n));
+  else CK(cudaMemcpyAsync(Z, V, (size_t)n * nc * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
+  int r = fork_blocks(c);
+  if (r) return r;
+  for (int b = 0; b < c->nbody; ++b) {  // each block solves its own rows
+    const int s0 = c->bstart[b], sz = c->bend[b] - c->bstart[b];
+    if (mixed(c)) CK(hg::getrs<float>(block_stream(c, b), sz, nc, c->pbf.p + c->poff[b], sz, c->pp.p + s0, Bf + s0, n));
+    else CK(hg::getrs<double>(block_stream(c, b), sz, nc, c->pb.p + c->poff[b], sz, c->pp.p + s0, Z + s0, n));
   }
+  r = join_blocks(c);
+  if (r) return r;
+  if (mixed(c)) CK(hg::convert_c2z_2d(c->st, n, nc, Bf, n, Z, n));
   return 0;
 }
 
@@ -821,6 +855,12 @@ void hg_destroy(hg_ctx* c) {
     if (c->user_ev[k]) cudaEventDestroy(c->user_ev[k]);
   if (c->fork_ev) cudaEventDestroy(c->fork_ev);
   if (c->join_ev) cudaEventDestroy(c->join_ev);
+  for (cudaStream_t s : c->pst) {
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+  }
+  for (cudaEvent_t e : c->pev) cudaEventDestroy(e);
+  if (c->pfork) cudaEventDestroy(c->pfork);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
