@@ -6,7 +6,8 @@ src/IterativeSolvers.f90:156-562).
 1. On the GPU's own FP64 matrices the device GMRES takes the oracle's
    iteration count (restated ZGMRES_SOLVE with modified Gram-Schmidt; the
    device runs classical Gram-Schmidt twice) and reaches its iterate to
-   1e-8: Jacobi for one body, per-body LU blocks for three.
+   1e-8: Jacobi for one body (also on the normal equations of
+   irregular-frequency removal), per-body LU blocks for three.
 2. The reference's own GMRES integration test
    (test/test_integration_gmres.f90:50-101): config1's deck with
    Solver_type 2 against the direct solve's expected outputs, relative
@@ -44,13 +45,16 @@ def _device_and_oracle(pkg, oracle, case, value):
     s = gpu_solver(pkg, case, 0, solver=2)
     s.keep_matrices(True)
     a, b, f, x = gpu_frequency(pkg, s, case, value)
-    A = s.get_matrix(0, case.n)
-    S = s.get_matrix(1, case.n)
+    rows = case.n + case.nl
+    A = s.get_matrix(0, rows)
+    S = s.get_matrix(1, rows)
     its, restarts, unconv, resid = s.iter_info()
     s.close()
     v, wk, w1, wvn = oracle.wave_properties(case.ctl, value)
     betas = [h * np.pi / 180.0 for h in case.ctl.headings]
     B = oracle.rhs(case, S, v, wk, w1, betas)
+    if case.nl > 0:  # GMRES on the normal equations C = A^T A, D = A^T B
+        A, B = oracle.normal_equations(case, A, B)
     xo, its_o, infos = oracle.gmres_columns(A, B, oracle.body_blocks(case))
     return x.copy(), xo, (its, restarts, unconv, resid), its_o, infos
 
@@ -66,6 +70,16 @@ def test_gmres_jacobi_matches_oracle(pkg, oracle, cyl_case, w):
 def test_gmres_block_lu_matches_oracle(pkg, oracle, config1):
     x, xo, (its, restarts, unconv, resid), its_o, infos = _device_and_oracle(pkg, oracle, config1,
                                                                               config1.ctl.wvnb[1])
+    assert unconv == 0 and all(i == 0 for i in infos)
+    assert its == max(its_o)
+    assert max_norm_err(x, xo) < ITER_TOL
+
+
+def test_gmres_jacobi_normal_equations_matches_oracle(pkg, oracle):
+    """example5: one body with lids, irregular-frequency removal (IRSP = 1):
+    Jacobi on C = A^T A (AssbMatx_irr.f90:494-498), finite depth."""
+    case = oracle.load_case(os.path.join(GOLDEN, "example5", "input"))
+    x, xo, (its, restarts, unconv, resid), its_o, infos = _device_and_oracle(pkg, oracle, case, case.ctl.wvnb[2])
     assert unconv == 0 and all(i == 0 for i in infos)
     assert its == max(its_o)
     assert max_norm_err(x, xo) < ITER_TOL
