@@ -9,6 +9,15 @@
 // its row, one cluster barrier, every CTA reads the 16 candidates and rows
 // out of the other CTAs' shared memory, takes the same pivot, and scales and
 // rank-1 updates its own rows.
+//
+// Complex64 panels of up to 16 x 512 rows take a register-resident form
+// (k_getf2_cluster_reg): one panel row per thread for all 32 column steps,
+// the steps unrolled so that every register index is a compile-time
+// constant, and per column one 528-byte message (candidate row, row jj,
+// the candidate's reciprocal) pushed to every CTA by bulk copy.  Taller
+// complex64 panels keep the rows in shared memory (k_getf2_cluster_push),
+// FP64 panels use the loading form (k_getf2_cluster).  All three choose the
+// same pivots and give the same factors.
 #include <mutex>
 #include <climits>
 #include <cooperative_groups.h>

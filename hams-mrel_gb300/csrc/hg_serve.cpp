@@ -210,6 +210,31 @@ void copy_in(std::vector<T>& dst, const T* src, size_t count) {
 
 }  // namespace
 
+// Device memory of the GMRES paths beyond hg_solve_footprint: the Krylov
+// and preconditioned bases (restart 8 for the refinement, 25 for solver 2),
+// and for solver 2 the preconditioner (the diagonal, or the per-body
+// diagonal blocks and their pivots).
+static size_t iter_bytes(const hg_opts& o, const hg_request& q) {
+  const size_t n = (size_t)q.n, nc = (size_t)6 * q.nbody + (size_t)(q.nbeta > 0 ? q.nbeta : 0);
+  size_t b = 0;
+  if (o.solver == 2) {
+    b += (size_t)(2 * 25 + 2) * n * nc * 16;
+    if (q.nbody <= 1) {
+      b += n * 16;
+    } else {
+      size_t blocks = 0;
+      for (int k = 0; k < q.nbody; ++k) {
+        const size_t sz = (size_t)(q.body_ranges[2 * k + 1] - q.body_ranges[2 * k] + 1);
+        blocks += sz * sz;
+      }
+      b += blocks * (o.precision == HG_PREC_MIXED ? 8 : 16) + n * sizeof(int);
+    }
+  } else if (o.refine_method == 1 && o.precision == HG_PREC_MIXED) {
+    b += (size_t)(2 * 8 + 2) * n * nc * 16;
+  }
+  return b;
+}
+
 extern "C" {
 
 int hg_server_create(hg_server** out, const hg_opts* opts, int nslots, double budget_bytes) {
@@ -280,7 +305,8 @@ int hg_server_submit(hg_server* s, const hg_request* q, long long* ticket) {
   r->amas.assign((size_t)q->nfreq * nd * nd, 0.0);
   r->bdmp.assign((size_t)q->nfreq * nd * nd, 0.0);
   r->exfc.assign((size_t)q->nfreq * (q->nbeta > 0 ? q->nbeta : 0) * nd * 2, 0.0);
-  r->slot_bytes = hg_solve_footprint(s->opts.precision, q->n, q->nl, q->nbody, q->nbeta, q->irsp, s->opts.lu_tensor);
+  r->slot_bytes = hg_solve_footprint(s->opts.precision, q->n, q->nl, q->nbody, q->nbeta, q->irsp, s->opts.lu_tensor) +
+                  iter_bytes(s->opts, *q);
   r->reserve = (size_t)std::min(s->nslots, q->nfreq) * r->slot_bytes + mesh_bytes(*r);
   if (r->reserve > s->budget) {
     s->err = "request needs " + std::to_string(r->reserve) + " bytes of device memory, above the budget of " +

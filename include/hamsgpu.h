@@ -197,8 +197,11 @@ int hg_solve_sweep(hg_ctx *ctx, int nfreq, const double *v, const double *wk, co
 
 /*
  * Device bytes one frequency-solve of this size holds in a context (matrices,
- * factor workspace, right-hand sides, refinement buffers, mesh): what the
- * serving loop below reserves per solve in flight.  0 for invalid sizes.
+ * factor workspace, right-hand sides, refinement buffers, mesh) with the
+ * default solver and classical refinement: what the serving loop below
+ * reserves per solve in flight, plus, under opts.solver = 2 or
+ * refine_method = 1, the GMRES bases (and solver 2's preconditioner blocks).
+ * 0 for invalid sizes.
  */
 size_t hg_solve_footprint(int precision, int n, int nl, int nbody, int nbeta, int irsp, int lu_tensor);
 
