@@ -16,8 +16,8 @@
 // constant, and per column one 528-byte message (candidate row, row jj,
 // the candidate's reciprocal) pushed to every CTA by bulk copy.  Taller
 // complex64 panels keep the rows in shared memory (k_getf2_cluster_push),
-// FP64 panels use the loading form (k_getf2_cluster).  All three choose the
-// same pivots and give the same factors.
+// FP64 panels use the loading form (k_getf2_cluster).  The two complex64
+// forms give bitwise-equal factors and pivots.
 #include <mutex>
 #include <climits>
 #include <cooperative_groups.h>
