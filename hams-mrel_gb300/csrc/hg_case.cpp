@@ -35,6 +35,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <memory>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -176,6 +177,7 @@ struct hg_case {
   std::vector<double> headings;              // degrees
   std::vector<std::array<double, 3>> xr;     // rotation centres
   std::vector<double> xfp;                   // field points, 3 per point
+  bool sep = false;                          // separate_wamit_diffraction_radiation_files (several bodies)
   // combined mesh (BuildCombinedArrays order: body after body)
   int n = 0, nl = 0, ntnd = 0;
   std::vector<double> nodes, xyz_p, ds, pnsz, dxyz, lid;  // column-major (ntnd x 3, n x 3, n, n, n x 6, nl x 3)
@@ -274,7 +276,23 @@ void read_control(hg_case* c) {
       const auto v = in.list(3);
       c->xfp.insert(c->xfp.end(), v.begin(), v.end());
     }
+    // WAMIT output layout (InputFiles.f90:204-220): two lines on, an optional
+    // "separate..." line with the flag at column 51 (read with an I edit
+    // descriptor into a LOGICAL: odd is true); one body never separates
+    if (in.i + 3 <= lines.size()) {
+      in.next();
+      in.next();
+      const std::string& ln = in.next();
+      if (ln.find("separate") != std::string::npos || ln.find("Separate") != std::string::npos) {
+        try {
+          c->sep = (f_int(field(ln, 50, 16)) & 1) != 0;
+        } catch (const CaseError&) {
+          c->sep = false;
+        }
+      }
+    }
   }
+  if (c->nbody == 1) c->sep = false;
 }
 
 struct Pnl {
@@ -859,6 +877,83 @@ std::complex<double> wamit_nondim(std::complex<double> vcp, bool pressure, bool 
   return diffraction ? std::complex<double>(-r.imag(), -r.real()) : std::complex<double>(r.real(), -r.imag());
 }
 
+// Incident-wave potential VINP (PatclVelct.f90:42-76) as CalPotentialIncMulti
+// uses it (PressureElevationMulti.f90:277-300): zero unless ISOL = 1, and zero
+// at the zero- and infinite-frequency entries; deep water if H < 0 or H > 500.
+std::complex<double> incident_potential(const hg_case* c, int k, double x, double y, double z, double beta, double g) {
+  if (c->isol != 1 || special(c->tp[k])) return 0.0;
+  const double wk = c->wk[k], w1 = c->w1[k], h = c->h;
+  const double wkx = wk * (x * std::cos(beta) + y * std::sin(beta));
+  const std::complex<double> e(std::cos(wkx), std::sin(wkx));
+  if (h < 0.0 || h > 500.0) return -g / w1 * std::exp(wk * z) * e;
+  return (-w1 / (wk * std::sinh(wk * h))) * std::cosh(wk * (z + h)) * e;
+}
+
+// Several bodies: OutputPressureElevation_RadiationMulti / _DiffractionMulti /
+// _IncidenceMulti (PressureElevationMulti.f90:407-587) into the files that
+// CreateWamitFiles opens (InputFiles.f90:318-338).  Radiation, per point: all
+// six modes of every body; one record per body (the first after the
+// frequency and point number, the others indented 24 columns), or, with
+// separate files, one PressureElevationRadiation_<body>.6p per body.
+// Diffraction, per heading and point: the non-dimensional value (2 reals).
+// Incidence (PressureElevationIncidence.6p): modulus, phase in degrees, real
+// and imaginary parts of the incident wave's value alone.
+void write_pe_multi(const hg_case* c, const char* output_dir, const std::vector<double>& pe, double rho, double g) {
+  const int np = c->nper, nb = c->nbody, nd = 6 * nb, nbeta = (int)c->headings.size(), nc = nd + nbeta;
+  const int nfp = (int)(c->xfp.size() / 3);
+  const std::string wd = std::string(output_dir) + "/Wamit_format";
+  std::unique_ptr<Out> fcomb, fdif;
+  std::vector<std::unique_ptr<Out>> frad;
+  if (c->sep) {
+    fdif.reset(new Out(wd + "/PressureElevationDiffraction.6p"));
+    for (int b = 0; b < nb; ++b) frad.emplace_back(new Out(wd + "/PressureElevationRadiation_" + std::to_string(b + 1) + ".6p"));
+  } else {
+    fcomb.reset(new Out(wd + "/PressureElevation.6p"));
+  }
+  Out finc(wd + "/PressureElevationIncidence.6p");
+  Out& dif = c->sep ? *fdif : *fcomb;
+  for (int k = 0; k < np; ++k) {
+    auto val = [&](int p, int q) {
+      const double* v = pe.data() + (((size_t)k * nfp + p) * nc + q) * 2;
+      return std::complex<double>(v[0], v[1]);
+    };
+    for (int p = 0; p < nfp; ++p) {
+      const bool below = std::fabs(c->xfp[3 * (size_t)p + 2]) > 1.e-6;
+      const std::string head = fES(14, 6, c->oufr[k]) + fI(10, p + 1);
+      for (int b = 0; b < nb; ++b) {
+        std::string s;
+        for (int md = 1; md <= 6; ++md) {
+          const auto z = wamit_nondim(val(p, 6 * b + md - 1), below, false, md, c->tp[k], c->w1[k], c->refl, rho, g);
+          s += fES(14, 6, z.real()) + fES(14, 6, z.imag());
+        }
+        if (c->sep) frad[b]->line(head + s);
+        else fcomb->line((b == 0 ? head : std::string(24, ' ')) + s);
+      }
+    }
+    for (int ib = 0; ib < nbeta; ++ib) {
+      const double beta = c->headings[ib] * kPi / 180.0;
+      const std::string hb = fES(14, 6, c->oufr[k]) + fES(14, 6, beta * 180.0 / kPi);
+      for (int p = 0; p < nfp; ++p) {
+        const bool below = std::fabs(c->xfp[3 * (size_t)p + 2]) > 1.e-6;
+        const auto z = wamit_nondim(val(p, nd + ib), below, true, 0, c->tp[k], c->w1[k], c->refl, rho, g);
+        dif.line(hb + fI(10, p + 1) + fES(14, 6, z.real()) + fES(14, 6, z.imag()));
+      }
+      for (int p = 0; p < nfp; ++p) {
+        const double* xp = c->xfp.data() + 3 * (size_t)p;
+        const bool below = std::fabs(xp[2]) > 1.e-6;
+        const std::complex<double> pot = incident_potential(c, k, xp[0], xp[1], xp[2], beta, g);
+        const bool sp = special(c->tp[k]);
+        const std::complex<double> iw(0.0, c->w1[k]);
+        const std::complex<double> vcp = below ? (sp ? rho * pot : iw * rho * pot) : (sp ? pot : iw / g * pot);
+        const auto z = wamit_nondim(vcp, below, true, 0, c->tp[k], c->w1[k], c->refl, rho, g);
+        const double rel = z.real(), img = z.imag();
+        finc.line(hb + fI(10, p + 1) + fES(14, 6, std::abs(z)) + fES(14, 6, std::atan2(img, rel) * (180.0 / kPi)) +
+                  fES(14, 6, rel) + fES(14, 6, img));
+      }
+    }
+  }
+}
+
 void run(hg_case* c, const char* output_dir, const hg_opts* opts, int nslots) {
   hg_opts o;
   if (opts) o = *opts;
@@ -885,15 +980,15 @@ void run(hg_case* c, const char* output_dir, const hg_opts* opts, int nslots) {
   for (int i = 0; i < nbeta; ++i) betas[i] = c->headings[i] * kPi / 180.0;
   std::vector<double> amas((size_t)np * nd * nd), bdmp((size_t)np * nd * nd), exfc((size_t)np * 2 * std::max(nbeta, 1) * nd);
   const int nfp = (int)(c->xfp.size() / 3);
-  const bool field = nfp > 0 && c->nbody == 1;
-  std::vector<double> pe;  // per frequency: nfp x (6 + nbeta) COMPLEX*16 (pressure below the surface, elevation on it)
+  const bool field = nfp > 0;
+  std::vector<double> pe;  // per frequency: nfp x (6 nbody + nbeta) COMPLEX*16 (pressure below the surface, elevation on it)
   if (!field) {
     check(hg_solve_sweep(ctx, np, c->v.data(), c->wk.data(), c->w1.data(), h, fin ? c->wvn.data() : nullptr,
                          fin ? kNk : 0, c->irsp, betas.data(), nbeta, c->isol, nslots, amas.data(), bdmp.data(),
                          exfc.data(), nullptr, 0, nullptr),
           "hg_solve_sweep");
   } else {
-    const int nc = 6 + nbeta;
+    const int nc = nd + nbeta;
     pe.assign((size_t)np * nfp * nc * 2, 0.0);
     std::vector<double> prs((size_t)nfp * nc * 2), elv((size_t)nfp * nc * 2);
     for (int k = 0; k < np; ++k) {
@@ -913,7 +1008,8 @@ void run(hg_case* c, const char* output_dir, const hg_opts* opts, int nslots) {
     }
   }
   write_results(c, output_dir, amas.data(), bdmp.data(), exfc.data(), o.rho, o.g);
-  if (field) {
+  if (field && c->nbody > 1) write_pe_multi(c, output_dir, pe, o.rho, o.g);
+  if (field && c->nbody == 1) {
     // PressureElevation.6p (formats 1000: ES14.6,I10,12ES14.6 and 1020: 2ES14.6,I10,4ES14.6)
     Out f6(std::string(output_dir) + "/Wamit_format/PressureElevation.6p");
     const int nc = 6 + nbeta;

@@ -361,8 +361,12 @@ int hg_stage_times(const hg_ctx *ctx, float *ms4);
  *       (RFORCE / EFORCE, src/PotentWavForce.f90:100-218 and the Multi forms)
  *   <out>/Wamit_format/AmssDamp.1, ExcForce.3 (the same routines, in the
  *       order they write: per frequency and body pair)
- *   <out>/Wamit_format/PressureElevation.6p for field points (single body;
- *       src/PressureElevation.f90:336-470, through hg_field_points)
+ *   <out>/Wamit_format/PressureElevation.6p for field points
+ *       (src/PressureElevation.f90:336-470, through hg_field_points); with
+ *       several bodies also PressureElevationIncidence.6p, and with the
+ *       control file's separate-files flag PressureElevationRadiation_<b>.6p
+ *       per body plus PressureElevationDiffraction.6p instead
+ *       (src/PressureElevationMulti.f90:407-587, src/InputFiles.f90:318-338)
  *   <out>/Wamit_format/Motion.4, Hydrostat.hst when Hydrostatic[_b].in are
  *       present (SolveMotion / SolveMotionMulti, src/SolveMotion*.f90;
  *       ReadHydroStatic, src/HydroStatic*.f90)

@@ -188,3 +188,117 @@ def test_case_run_zero_and_infinite_frequency_entries(pkg, tmp_path):
     assert np.all(np.isfinite(a))
     c.close()
     ref.close()
+
+
+def _vinp(x, y, z, beta, wk, w1, h, g=9.80665):
+    """VINP (src/PatclVelct.f90:42-76), AMP = 1, wave origin at 0."""
+    e = np.exp(1j * wk * (x * np.cos(beta) + y * np.sin(beta)))
+    if h < 0 or h > 500:
+        return -g / w1 * np.exp(wk * z) * e
+    return -w1 / (wk * np.sinh(wk * h)) * np.cosh(wk * (z + h)) * e
+
+
+@pytest.mark.parametrize("separate", [False, True])
+def test_case_run_field_points_multibody(pkg, oracle, tmp_path, separate):
+    """config1 (three bodies, h = 70 m) with four field points: the WAMIT files
+    of OutputPressureElevation_RadiationMulti / _DiffractionMulti /
+    _IncidenceMulti (src/PressureElevationMulti.f90:407-587), combined or, with
+    the control file's separate-files flag (src/InputFiles.f90:204-220), one
+    radiation file per body and one diffraction file."""
+    src = os.path.join(GOLDEN, "config1", "input")
+    d = os.path.join(tmp_path, "deck")
+    shutil.copytree(src, d)
+    pts = np.array([[20.0, 30.0, -5.0], [-25.0, 60.0, -2.0], [15.0, -30.0, 0.0], [-40.0, 120.0, 0.0]])
+    with open(os.path.join(d, "ControlFile.in")) as f:
+        lines = f.read().split("\n")
+    out, skip = [], False
+    for ln in lines:
+        if ln.startswith("    Number_of_field_points"):
+            out.append(ln[:27] + "%16d" % len(pts))
+            out += ["    %12.4f %12.4f %12.4f" % tuple(p) for p in pts]
+            out.append("   #End Definition of Pressure and/or Elevation")
+            out.append("   #Start Definition of WAMIT output")
+            flag = "    Separate_wamit_diffraction_radiation_files"
+            out.append(flag + " " * (50 - len(flag)) + "%16d" % (1 if separate else 0))
+            skip = True
+            continue
+        if skip and ln.strip().startswith("#End Definition of Pressure"):
+            skip = False
+            continue
+        out.append(ln)
+    with open(os.path.join(d, "ControlFile.in"), "w") as f:
+        f.write("\n".join(out))
+    c = pkg.hamsgpu.Case(d)
+    assert c.info["nfp"] == 4 and c.info["nbody"] == 3
+    c.run(os.path.join(tmp_path, "out"), precision=pkg.hamsgpu.HG_PREC_FP64, nslots=1)
+    wd = os.path.join(tmp_path, "out", "Wamit_format")
+
+    def rows(name):
+        with open(os.path.join(wd, name)) as f:
+            return f.read().splitlines()
+
+    comb = None if separate else rows("PressureElevation.6p")
+    rad = [rows("PressureElevationRadiation_%d.6p" % (b + 1)) for b in range(3)] if separate else None
+    dif = rows("PressureElevationDiffraction.6p") if separate else None
+    inc = rows("PressureElevationIncidence.6p")
+    assert os.path.exists(os.path.join(wd, "PressureElevation.6p")) == (not separate)
+    case = oracle.load_case(d)
+    heads = case.ctl.headings
+    betas = np.radians(heads)
+    below = np.abs(pts[:, 2]) > 1e-6
+    ic = ir = idf = 0
+    irb = [0, 0, 0]
+    for w in case.ctl.wvnb:
+        v, wk, w1, wvn = oracle.wave_properties(case.ctl, w)
+        r = oracle.solve_frequency(case, w)
+        pot = oracle.field_potential(case, pts, v, wk, w1, wvn, betas, r.mxpot, isol=case.ctl.isol)
+        vcp = np.where(below[:, None], 1j * w1 * 1000.0 * pot, 1j * w1 / 9.80665 * pot)
+        zr = np.array([[_nondim(vcp[p, q], bool(below[p]), False, q % 6 + 1, False, w1, case.ctl.refl)
+                        for q in range(18)] for p in range(len(pts))])
+        zmax = np.abs(zr).max()
+        for p in range(len(pts)):
+            for b in range(3):
+                if separate:
+                    t = rad[b][irb[b]].split(); irb[b] += 1
+                    assert int(t[1]) == p + 1 and abs(float(t[0]) - w1) < 1e-6
+                    vals = t[2:]
+                else:
+                    ln = comb[ic]; ic += 1
+                    if b == 0:
+                        t = ln.split()
+                        assert int(t[1]) == p + 1 and abs(float(t[0]) - w1) < 1e-6
+                        vals = t[2:]
+                    else:
+                        assert ln[:24] == " " * 24
+                        vals = ln.split()
+                assert len(vals) == 12
+                for md in range(6):
+                    z = zr[p, 6 * b + md]
+                    got = float(vals[2 * md]) + 1j * float(vals[2 * md + 1])
+                    assert abs(got - z) <= 1e-6 * abs(z) + 1e-6 * zmax, (p, b, md, got, z)
+        zd = np.array([[_nondim(vcp[p, 18 + ib], bool(below[p]), True, 0, False, w1, case.ctl.refl)
+                        for ib in range(len(heads))] for p in range(len(pts))])
+        zdmax = np.abs(zd).max()
+        for ib, b in enumerate(heads):
+            for p in range(len(pts)):
+                if separate:
+                    t = dif[idf].split(); idf += 1
+                else:
+                    t = comb[ic].split(); ic += 1
+                assert len(t) == 5 and int(t[2]) == p + 1 and abs(float(t[1]) - b) < 1e-9
+                got = float(t[3]) + 1j * float(t[4])
+                assert abs(got - zd[p, ib]) <= 2e-6 * abs(zd[p, ib]) + 1e-6 * zdmax
+            for p in range(len(pts)):
+                t = inc[ir].split(); ir += 1
+                pi = _vinp(pts[p, 0], pts[p, 1], pts[p, 2], np.radians(b), wk, w1, case.ctl.h)
+                vi = 1j * w1 * 1000.0 * pi if below[p] else 1j * w1 / 9.80665 * pi
+                z = _nondim(vi, bool(below[p]), True, 0, False, w1, case.ctl.refl)
+                assert len(t) == 7 and int(t[2]) == p + 1
+                assert abs(float(t[5]) + 1j * float(t[6]) - z) <= 2e-6 * abs(z) + 1e-12
+                assert abs(float(t[3]) - abs(z)) <= 2e-6 * abs(z) + 1e-12
+    assert ir == len(inc)
+    if separate:
+        assert idf == len(dif) and all(irb[b] == len(rad[b]) for b in range(3))
+    else:
+        assert ic == len(comb)
+    c.close()
