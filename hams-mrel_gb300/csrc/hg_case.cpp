@@ -7,8 +7,9 @@
 // device through hg_solve_sweep / hg_solve_frequency, and the writers of the
 // HAMS-format and WAMIT-format result files (RFORCE / EFORCE,
 // src/PotentWavForce.f90:100-218, src/PotentWavForceMulti.f90:100-223; the pressure and
-// elevation file of OutputPressureElevation_Radiation / _Diffraction,
-// src/PressureElevation.f90:336-470, single body), and the motion equations
+// elevation files of OutputPressureElevation_Radiation / _Diffraction,
+// src/PressureElevation.f90:336-470, and of their multi-body forms with the
+// incident-wave file, src/PressureElevationMulti.f90:407-587), and the motion equations
 // of SolveMotion / SolveMotionMulti (src/SolveMotion.f90, src/SolveMotionMulti.f90)
 // with the hydrostatic decks of ReadHydroStatic(Multi) (src/HydroStatic.f90,
 // src/HydroStaticMulti.f90): Motion.4 and Hydrostat.hst; and the single-body
@@ -20,8 +21,9 @@
 // Ew.d, ESw.d, Iw) character for character, including its choices that a
 // reader might not expect: the WAMIT phase column of ExcForce.3 is
 // ATAN2D(...) * 180 / PI (degrees converted once more), zero- and infinite-
-// frequency entries write added mass only, and radiation pressure lines are
-// written only for field points below the free surface.
+// frequency entries write added mass only, and single-body radiation pressure
+// lines are written only for field points below the free surface (the
+// multi-body radiation records hold elevations for points on it).
 #include <sys/stat.h>
 #include <sys/types.h>
 
