@@ -55,3 +55,22 @@ def test_gmres_zero_rhs_and_cap(oracle):
     hard = q @ np.diag(np.exp(2j * np.pi * np.arange(40) / 40)) @ q.T
     x, its, infos = oracle.gmres_columns(hard, b[:40], restart=2, maxit=10)
     assert its == [10] and infos == [1]
+
+
+def test_oracle_gmres_on_config1_against_lu(oracle):
+    """The restated ISOLV = 2 path on the reference's own GMRES test deck
+    (test/data/config1_gmres = config1 with Solver_type 2): three bodies, so
+    the block-diagonal LU preconditioner; added mass and damping against the
+    direct solve within the reference's test tolerances
+    (test/test_integration_gmres.f90:50-101: relative Frobenius norm 1e-3 and
+    5e-2)."""
+    import os
+    from conftest import GOLDEN
+    case = oracle.load_case(os.path.join(GOLDEN, "config1", "input"))
+    assert oracle.body_blocks(case) == [(0, 234), (234, 234), (468, 234)]
+    w = case.ctl.wvnb[1]
+    lu = oracle.solve_frequency(case, w, solver=1)
+    it = oracle.solve_frequency(case, w, solver=2)
+    for got, exp, tol in ((it.amas, lu.amas, 1e-3), (it.bdmp, lu.bdmp, 5e-2)):
+        assert np.linalg.norm(got - exp) / np.linalg.norm(exp) < tol
+    assert np.abs(it.exfc - lu.exfc).max() < 1e-3 * np.abs(lu.exfc).max()
