@@ -1102,6 +1102,13 @@ int hg_case_info(const hg_case* c, int* info, double* dinfo) {
   return 0;
 }
 
+int hg_case_options(const hg_case* c, int* isolv, int* separate) {
+  if (!c) return -1;
+  if (isolv) *isolv = c->isolv;
+  if (separate) *separate = c->sep ? 1 : 0;
+  return 0;
+}
+
 int hg_case_arrays(const hg_case* c, double* nodes, int* ncon, int* ncn, double* xyz_p, double* ds, double* pnsz,
                    double* dxyz_p, double* lid_xyz_p, int* body_ranges, double* freq, double* headings) {
   if (!c) return -1;

@@ -27,7 +27,7 @@ EXPORTS = [
     "hg_solve_sweep", "hg_gmres_iterations", "hg_solve_footprint", "hg_server_create", "hg_server_submit",
     "hg_server_wait", "hg_server_stats", "hg_server_last_error", "hg_server_destroy", "hg_field_points",
     "hg_case_read", "hg_case_free", "hg_case_info", "hg_case_arrays", "hg_case_run", "hg_case_write",
-    "hg_iter_info",
+    "hg_iter_info", "hg_case_options",
 ]
 
 
@@ -127,6 +127,7 @@ def load(build_if_missing: bool = True):
     L.hg_case_free.argtypes = [c_void_p]
     L.hg_case_free.restype = None
     L.hg_case_info.argtypes = [c_void_p, c_void_p, c_void_p]
+    L.hg_case_options.argtypes = [c_void_p, P(c_int), P(c_int)]
     L.hg_case_arrays.argtypes = [c_void_p] + [c_void_p] * 11
     L.hg_case_run.argtypes = [c_void_p, ctypes.c_char_p, P(HgOpts), c_int, ctypes.c_char_p, c_int]
     L.hg_case_write.argtypes = [c_void_p, ctypes.c_char_p, c_void_p, c_void_p, c_void_p, c_double, c_double,
@@ -516,6 +517,9 @@ class Case:
         keys = ["n", "nl", "ntnd", "nbody", "nper", "nbeta", "irsp", "isol", "nfp", "sybo", "inft", "ouft"]
         self.info = {k: int(v) for k, v in zip(keys, info)}
         self.info["h"], self.info["refl"] = float(dinfo[0]), float(dinfo[1])
+        isolv, sep = ctypes.c_int(), ctypes.c_int()
+        self.L.hg_case_options(self.h, ctypes.byref(isolv), ctypes.byref(sep))
+        self.info["isolv"], self.info["separate"] = isolv.value, sep.value
 
     def arrays(self):
         i = self.info

@@ -387,6 +387,8 @@ typedef struct hg_case hg_case;
 int hg_case_read(const char *input_dir, hg_case **out, char *err, int errlen);
 void hg_case_free(hg_case *c);
 int hg_case_info(const hg_case *c, int *info, double *dinfo);
+/* The deck's Solver_type (ISOLV, 1 or 2) and separate-files flag (0 or 1; always 0 for one body). */
+int hg_case_options(const hg_case *c, int *isolv, int *separate);
 int hg_case_arrays(const hg_case *c, double *nodes, int *ncon, int *ncn, double *xyz_p, double *ds, double *pnsz,
                    double *dxyz_p, double *lid_xyz_p, int *body_ranges, double *freq, double *headings);
 int hg_case_run(hg_case *c, const char *output_dir, const hg_opts *opts, int nslots, char *err, int errlen);

@@ -158,3 +158,41 @@ def test_writer_reproduces_golden_files(pkg, oracle, name, tmp_path):
 def test_case_read_errors(pkg, tmp_path):
     with pytest.raises(pkg.hamsgpu.HamsGpuError):
         pkg.hamsgpu.Case(str(tmp_path))  # no ControlFile.in
+
+
+def _deck_with(tmp_path, name, control_from=None, separate=None):
+    import shutil
+    d = os.path.join(tmp_path, "deck_%s_%s_%s" % (name, bool(control_from), separate))
+    shutil.copytree(os.path.join(GOLDEN, name, "input"), d)
+    if control_from:
+        shutil.copy(control_from, os.path.join(d, "ControlFile.in"))
+    if separate is not None:
+        with open(os.path.join(d, "ControlFile.in")) as f:
+            lines = f.read().split("\n")
+        k = next(i for i, ln in enumerate(lines) if ln.startswith("    Number_of_field_points"))
+        flag = "    Separate_wamit_diffraction_radiation_files"
+        # ReadControlFile skips the two records after the field points, then reads this one
+        lines[k + 1:k + 3] = [lines[k + 1], "   #WAMIT output", flag + " " * (50 - len(flag)) + "%16d" % separate]
+        with open(os.path.join(d, "ControlFile.in"), "w") as f:
+            f.write("\n".join(lines))
+    return d
+
+
+def test_case_read_solver_type_and_separate_files(pkg, tmp_path):
+    """Solver_type (src/InputFiles.f90:177-191) and the separate-files flag
+    (:204-220: read with an I edit descriptor into a LOGICAL, odd = true;
+    always false for one body)."""
+    hg = pkg.hamsgpu
+    c = hg.Case(_deck_with(tmp_path, "config1"))
+    assert c.info["isolv"] == 1 and c.info["separate"] == 0
+    c.close()
+    c = hg.Case(_deck_with(tmp_path, "config1", os.path.join(GOLDEN, "config1_gmres", "ControlFile.in")))
+    assert c.info["isolv"] == 2 and c.info["separate"] == 0
+    c.close()
+    for flag, want in ((1, 1), (0, 0), (3, 1), (2, 0)):
+        c = hg.Case(_deck_with(tmp_path, "config1", separate=flag))
+        assert c.info["separate"] == want, flag
+        c.close()
+    c = hg.Case(_deck_with(tmp_path, "example5", separate=1))
+    assert c.info["nbody"] == 1 and c.info["separate"] == 0
+    c.close()
