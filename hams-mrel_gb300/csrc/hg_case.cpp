@@ -609,6 +609,18 @@ void write_results(const hg_case* c, const std::string& out, const double* amas,
   make_dir(out);
   make_dir(hd);
   make_dir(wd);
+  {  // the pressure/elevation files CreateWamitFiles opens in every run (InputFiles.f90:318-338),
+     // empty until field points are written into them
+    std::vector<std::string> pe;
+    if (nb > 1 && c->sep) {
+      pe.push_back("PressureElevationDiffraction.6p");
+      for (int b = 0; b < nb; ++b) pe.push_back("PressureElevationRadiation_" + std::to_string(b + 1) + ".6p");
+    } else {
+      pe.push_back("PressureElevation.6p");
+    }
+    if (nb > 1) pe.push_back("PressureElevationIncidence.6p");
+    for (const auto& name : pe) Out empty(wd + "/" + name);
+  }
   const double amp = 1.0;
   auto A = [&](int k, int i, int j) { return amas[(size_t)k * nd * nd + i + (size_t)j * nd]; };
   auto B = [&](int k, int i, int j) { return bdmp[(size_t)k * nd * nd + i + (size_t)j * nd]; };

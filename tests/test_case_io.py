@@ -196,3 +196,28 @@ def test_case_read_solver_type_and_separate_files(pkg, tmp_path):
     c = hg.Case(_deck_with(tmp_path, "example5", separate=1))
     assert c.info["nbody"] == 1 and c.info["separate"] == 0
     c.close()
+
+
+@pytest.mark.parametrize("name,separate,files", [
+    ("example5", None, ["PressureElevation.6p"]),
+    ("config1", None, ["PressureElevation.6p", "PressureElevationIncidence.6p"]),
+    ("config1", 1, ["PressureElevationDiffraction.6p", "PressureElevationRadiation_1.6p",
+                    "PressureElevationRadiation_2.6p", "PressureElevationRadiation_3.6p",
+                    "PressureElevationIncidence.6p"]),
+])
+def test_writer_creates_the_pressure_elevation_files(pkg, tmp_path, name, separate, files):
+    """CreateWamitFiles (src/InputFiles.f90:318-338) opens the pressure and
+    elevation files in every run; without field points they stay empty (as in
+    the reference's shipped example outputs)."""
+    d = _deck_with(tmp_path, name, separate=separate)
+    c = pkg.hamsgpu.Case(d)
+    i = c.info
+    nd, nb = 6 * i["nbody"], i["nbeta"]
+    out = os.path.join(tmp_path, "out")
+    c.write(out, np.zeros((i["nper"], nd, nd)), np.zeros((i["nper"], nd, nd)),
+            np.zeros((i["nper"], nb, nd), dtype=complex))
+    c.close()
+    wd = os.path.join(out, "Wamit_format")
+    got = sorted(f for f in os.listdir(wd) if f.startswith("PressureElevation"))
+    assert got == sorted(files)
+    assert all(os.path.getsize(os.path.join(wd, f)) == 0 for f in files)
