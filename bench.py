@@ -200,12 +200,40 @@ def cpu_reference(steps, warmup, rank, world):
 
 
 def _cpu_baseline_sample():
-    """One full frequency-solve of the workload by the oracle on all host cores."""
+    """One full frequency-solve of the workload by the oracle on all host
+    cores: (cpu_baseline entry, the oracle's result or None)."""
     try:
         return _cpu_baseline_sample_inner()
     except Exception as e:  # reported, never silently dropped
         return {"value": None, "unit": "freq-solves/s", "cores": os.cpu_count(), "kind": "port",
-                "sample": f"failed: {e}"}
+                "sample": f"failed: {e}"}, None
+
+
+def _vs_oracle(pkg, mesh, s, ref, betas, local, prec):
+    """Max-normalised error of the plain and the mixed form against the
+    oracle's solve of the CPU sample's frequency: A, B, F and the motions
+    (RAOs) of the freely floating bodies that these give."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import max_norm_err, motions, rigid_body_matrices
+    hg = pkg.hamsgpu
+    w = FREQS[17]
+    fv, fwk, fw1 = _frequency_inputs(pkg, w)
+    M, C = rigid_body_matrices(mesh)
+    xr = motions(ref.amas, ref.bdmp, ref.exfc, w, M, C)
+
+    def errs(res):
+        a, b, f = res[0], res[1], res[2]
+        return {"A": max_norm_err(a, ref.amas), "B": max_norm_err(b, ref.bdmp), "F": max_norm_err(f, ref.exfc),
+                "RAO": max_norm_err(motions(a, b, f, w, M, C), xr)}
+
+    out = {"w_rad_s": float(w)}
+    sp = hg.Solver(precision=hg.HG_PREC_FP64, device=local)
+    sp.set_mesh(mesh.nodes, mesh.ncon, mesh.ncn, mesh.xyz_p, mesh.ds, mesh.pnsz, mesh.dxyz_p, mesh.body_ranges)
+    out["plain"] = errs(sp.solve_frequency(fv, fwk, fw1, -1.0, None, betas, want_potentials=False))
+    sp.close()
+    if prec == hg.HG_PREC_MIXED:
+        out["mixed"] = errs(s.solve_frequency(fv, fwk, fw1, -1.0, None, betas, want_potentials=False))
+    return out
 
 
 def _cpu_baseline_sample_inner():
@@ -217,11 +245,11 @@ def _cpu_baseline_sample_inner():
     case = case_from_mesh(oracle, mesh, h=-1.0, headings_deg=list(BETAS_DEG))
     cores = os.cpu_count()
     t0 = time.perf_counter()
-    oracle.solve_frequency(case, FREQS[17], nthreads=cores)
+    ref = oracle.solve_frequency(case, FREQS[17], nthreads=cores)
     dt = time.perf_counter() - t0
     return {"value": 1.0 / dt, "unit": "freq-solves/s", "cores": cores, "kind": "port",
             "sample": "1 full frequency-solve (w = %.3f rad/s) of the 6048-panel workload: C oracle with OpenMP "
-                      "over field rows + scipy/OpenBLAS zgetrf/zgetrs" % FREQS[17]}
+                      "over field rows + scipy/OpenBLAS zgetrf/zgetrs" % FREQS[17]}, ref
 
 
 def ours(args, dist, rank, world, local):
@@ -242,12 +270,16 @@ def ours(args, dist, rank, world, local):
                  solver=2 if args.solver == "gmres" else 1)
     s = hg.Solver(precision=prec, device=local, **sopts)
     s.set_mesh(mesh.nodes, mesh.ncon, mesh.ncn, mesh.xyz_p, mesh.ds, mesh.pnsz, mesh.dxyz_p, mesh.body_ranges)
-    # warm-up: at least one frequency per slot, so that every slot has its buffers
-    warm = max(args.warmup, nslots)
-    v, wk, w1 = inputs(warm, 0)
+    # set-up (not a step): one frequency per slot creates every slot and its device buffers
+    v, wk, w1 = inputs(nslots, 0)
     s.solve_sweep(v, wk, w1, -1.0, None, betas, nslots=nslots)
+    # warm-up: exactly the requested steps
+    warm = args.warmup
+    if warm > 0:
+        v, wk, w1 = inputs(warm, nslots)
+        s.solve_sweep(v, wk, w1, -1.0, None, betas, nslots=nslots)
     # ---- device-timed region: one sweep of `steps` frequencies, inputs resident ----
-    v, wk, w1 = inputs(args.steps, warm)
+    v, wk, w1 = inputs(args.steps, nslots + warm)
     _barrier(dist)
     with ClockSampler(local) as clk:
         s.mark(0)
@@ -306,6 +338,12 @@ def ours(args, dist, rank, world, local):
     roof = None
     if rank == 0 and args.solver == "lu":
         roof = _roofline(s, mesh.n, prec, hg)
+    # ---- the CPU oracle on one frequency (the CPU baseline sample), and both GPU forms against it ----
+    cpu, vs_oracle = None, None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu, ref = _cpu_baseline_sample()
+        if ref is not None:
+            vs_oracle = _vs_oracle(pkg, mesh, s, ref, betas, local, prec)
     s.close()
     if rank != 0:
         return
@@ -332,8 +370,9 @@ def ours(args, dist, rank, world, local):
                              "iterations": iters[0], "restarts": iters[1], "unconverged": iters[2],
                              "residual": iters[3]}
         del line["refine"]
-    if not args.no_cpu_baseline:
-        line["cpu_baseline"] = _cpu_baseline_sample()
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+        line["vs_oracle"] = vs_oracle
     print(json.dumps(line), flush=True)
 
 
@@ -517,7 +556,8 @@ def field_map(args):
     line = {"metric": "field points/s (free-surface elevation, all 38 columns per point)",
             "value": len(pts) / (ms / 1e3), "unit": "points/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "complex128", "data": "synthetic",
+            "vs_baseline": None,
+            "dtype": "complex64+fp64-refine" if prec == hg.HG_PREC_MIXED else "complex128", "data": "synthetic",
             "config": {"workload": "5-body array, 6048 panels, deep water, w 0.8 rad/s, 8 headings, 30 modes; "
                                    "%d free-surface points" % len(pts), "solve_form": args.precision,
                        "timing": "host coordinates in, host results out (hg_field_points), CUDA events"},

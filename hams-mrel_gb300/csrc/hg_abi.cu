@@ -1051,10 +1051,19 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
                        (c->o.fin_table == 1 || (c->o.fin_table < 0 && (long long)tn * n >= 1000000LL));
     if (table) {
       CK(c->tab.ensure(hg::fintab_floats() + (size_t)6 * n));
+      // pairs below R/h = 0.05 (LINTON, PIDCOCK) per pair in FP64 after the
+      // tables (the reference's values there are not smooth enough to
+      // interpolate), which then hold only the bands above
+      const bool near = (long long)tn * n < 2147483647LL;
       hg::FinTab tab;
-      CK(hg::fintab_build(c->st, fs, 1.02 * c->rmax + 1.0, c->tab.p, &tab));
+      CK(hg::fintab_build(c->st, fs, 1.02 * c->rmax + 1.0, c->tab.p, &tab, near ? 2 : 0));
       CK(hg::launch_green_fill_mixed_fin(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, tab, c->ox, c->oy, c->pgauss.p,
                                          c->tab.p + hg::fintab_floats(), c->Af.p, c->Sf.p, tn, c->status.p));
+      if (near) {
+        CK(c->bins.ensure(hg::fin_bins_ints(n, tn)));
+        CK(hg::launch_fin_near(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, c->o.grn_kind, c->Af.p, c->Sf.p, tn,
+                               c->bins.p, tn));
+      }
     } else if (!deep) {
       const bool binned = (long long)tn * n < 2147483647LL;
       if (binned) CK(c->bins.ensure(hg::fin_bins_ints(n, tn)));
@@ -1409,6 +1418,7 @@ int hg_green_points(hg_ctx* c, int npts, const double* pts, const int* flags, do
   if (npts <= 0) return fail(c, -2, "npts must be positive");
   if (!pts || !flags || !out) return fail(c, -3, "NULL array");
   if (!c->freq_set) return fail(c, HG_ERR_STATE, "hg_set_frequency must come first");
+  CK(cudaSetDevice(c->o.device));
   DevBuf<double> dp, dout;
   DevBuf<int> df;
   CK(dp.ensure((size_t)6 * npts));

@@ -391,7 +391,14 @@ __global__ void k_fin_diag(int n, const double* __restrict__ rec, FinState fs, f
 cudaError_t launch_green_fill_mixed_fin(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
                                         const FinState& fs, const FinTab& tab, double ox, double oy,
                                         const float4* pg, float* diag, float2* A, float2* S, long lda, int* status) {
-  k_fin_diag<<<(n + 31) / 32, 32, 0, st>>>(n, rec, fs, diag);
+  // the coincident pairs' FP64 values; with the per-pair pass below R/h = 0.05
+  // (tab.gmin = 2) that pass writes them, and the table fill reads zeros
+  if (tab.gmin < 2) {
+    k_fin_diag<<<(n + 31) / 32, 32, 0, st>>>(n, rec, fs, diag);
+  } else {
+    cudaError_t e = cudaMemsetAsync(diag, 0, (size_t)6 * n * sizeof(float), st);
+    if (e != cudaSuccess) return e;
+  }
   dim3 grid((tn + FILL_ROWS - 1) / FILL_ROWS, (n + FILL_COLS - 1) / FILL_COLS);
   k_green_fill_mixed<true><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, (float)fs.v, ox, oy, pg, tab, diag, A, S,
                                                         lda, status, tn);

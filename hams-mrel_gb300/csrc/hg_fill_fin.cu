@@ -26,6 +26,19 @@ template cudaError_t launch_green_fill_fin<double2>(cudaStream_t, const double*,
 template cudaError_t launch_green_fill_fin<float2>(cudaStream_t, const double*, const double*, int, int, int,
                                                    const FinState&, int, float2*, float2*, long, int*, int*, int);
 
+// The pairs below R/h = 0.05 (FINGREEN3D's LINTON and PIDCOCK methods,
+// FinGreen3D.f90:182-191) evaluated per pair with the reference's
+// arithmetic and written over what A and S hold; the other pairs are left
+// alone.  The mixed form's tabulated fill calls this after the tables:
+// LINTON's adaptive quadrature and PIDCOCK's epsilon-extrapolated series
+// make the reference's values in those bands jump with R and depth by far
+// more than a smooth interpolation can follow, so only a per-pair
+// evaluation reproduces them.
+cudaError_t launch_fin_near(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
+                            const FinState& fs, int grn_kind, float2* A, float2* S, long lda, int* bins, int ndiag) {
+  return launch_fin_binned<float2, 0>(st, rec, fx, ldf, n, tn, fs, grn_kind, A, S, lda, bins, ndiag, kFinNearBins);
+}
+
 cudaError_t launch_green_points_fin(cudaStream_t st, int npts, const double* pts, const int* flags, const FinState& fs,
                                     double* out) {
   k_green_points<false><<<(npts + 63) / 64, 64, 0, st>>>(npts, pts, flags, fs, out);

@@ -97,6 +97,7 @@ k_green_fill(const double* __restrict__ rec, const double* __restrict__ fx /* ld
 // (set by atomics) does not affect the matrices.
 // ---------------------------------------------------------------------------
 constexpr int kFinBins = 16;
+constexpr int kFinNearBins = 8;  // bins 0..7: LINTON and PIDCOCK (R/h < 0.05)
 
 __device__ __forceinline__ int fin_bin(const FinState& fs, double rr) {
   const double v = fs.v;
@@ -116,21 +117,22 @@ __device__ __forceinline__ int fin_bin(const FinState& fs, double rr) {
 
 // Pass 1 (scatter = false): bin counts; pass 2 (scatter = true): pair index
 // i + j * tn appended to its bin at cursor[bin] (warp-aggregated atomics).
+// Pairs whose bin is maxbin or above are left out of both passes.
 template <bool SCATTER>
 __global__ void k_fin_bins(const double* __restrict__ rec, const double* __restrict__ fx, int ldf, int n, int tn,
-                           FinState fs, int* __restrict__ counts, int* __restrict__ list) {
+                           FinState fs, int maxbin, int* __restrict__ counts, int* __restrict__ list) {
   __shared__ int hist[kFinBins];
   if (!SCATTER && threadIdx.x < kFinBins) hist[threadIdx.x] = 0;
   if (!SCATTER) __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
-  const bool ok = i < tn;
-  int b = 0;
-  if (ok) {
+  int b = kFinBins;
+  if (i < tn) {
     const double* pr = rec + (size_t)j * PR_SIZE;
     const double dx = pr[PR_XQ] - fx[i], dy = pr[PR_XQ + 1] - fx[i + ldf];
     b = fin_bin(fs, sqrt(dx * dx + dy * dy));
   }
+  const bool ok = b < maxbin;
   const unsigned act = __ballot_sync(0xffffffffu, ok);
   if (ok) {
     const unsigned peers = __match_any_sync(act, b);
@@ -163,11 +165,14 @@ static __global__ void k_fin_scan(int* __restrict__ counts) {
   }
 }
 
+// npairs: list length, or (listed != nullptr) read from *listed, the last
+// bin's cursor after the scatter pass when only some bins were listed.
 template <typename OUT, int FAST>
 __global__ void __launch_bounds__(128)
 k_green_fill_binned(const double* __restrict__ rec, const double* __restrict__ fx, int ldf, int tn, long npairs,
-                    const int* __restrict__ list, FinState fs, int grn_kind, OUT* __restrict__ A,
-                    OUT* __restrict__ S, long lda, int ndiag) {
+                    const int* __restrict__ listed, const int* __restrict__ list, FinState fs, int grn_kind,
+                    OUT* __restrict__ A, OUT* __restrict__ S, long lda, int ndiag) {
+  if (listed) npairs = *listed;
   for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < npairs; k += (long)gridDim.x * blockDim.x) {
     const int p = list[k];
     const int i = p % tn, j = p / tn;
@@ -176,22 +181,26 @@ k_green_fill_binned(const double* __restrict__ rec, const double* __restrict__ f
   }
 }
 
+// maxbin < kFinBins evaluates only the pairs of bins below it (the others
+// keep what A and S hold).
 template <typename OUT, int FAST>
 cudaError_t launch_fin_binned(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
-                              const FinState& fs, int grn_kind, OUT* A, OUT* S, long lda, int* bins, int ndiag) {
+                              const FinState& fs, int grn_kind, OUT* A, OUT* S, long lda, int* bins, int ndiag,
+                              int maxbin = kFinBins) {
   int* counts = bins;
   int* list = bins + kFinBins;
   cudaError_t e = cudaMemsetAsync(counts, 0, kFinBins * sizeof(int), st);
   if (e != cudaSuccess) return e;
   const dim3 cg((tn + 127) / 128, n);
-  k_fin_bins<false><<<cg, 128, 0, st>>>(rec, fx, ldf, n, tn, fs, counts, list);
+  k_fin_bins<false><<<cg, 128, 0, st>>>(rec, fx, ldf, n, tn, fs, maxbin, counts, list);
   k_fin_scan<<<1, 32, 0, st>>>(counts);
-  k_fin_bins<true><<<cg, 128, 0, st>>>(rec, fx, ldf, n, tn, fs, counts, list);
+  k_fin_bins<true><<<cg, 128, 0, st>>>(rec, fx, ldf, n, tn, fs, maxbin, counts, list);
   const long np = (long)tn * n;
   long blocks = (np + 127) / 128;
   if (blocks > 152L * 64) blocks = 152L * 64;
-  k_green_fill_binned<OUT, FAST><<<(unsigned)blocks, 128, 0, st>>>(rec, fx, ldf, tn, np, list, fs, grn_kind, A, S, lda,
-                                                                  ndiag);
+  const int* listed = (maxbin < kFinBins) ? counts + (maxbin - 1) : nullptr;
+  k_green_fill_binned<OUT, FAST><<<(unsigned)blocks, 128, 0, st>>>(rec, fx, ldf, tn, np, listed, list, fs, grn_kind, A,
+                                                                  S, lda, ndiag);
   return cudaGetLastError();
 }
 

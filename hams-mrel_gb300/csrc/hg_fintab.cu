@@ -30,24 +30,27 @@ __device__ __forceinline__ void f_minus_prop(const FinState& fs, const FinTab& T
   for (int q = 0; q < 6; ++q) out[q] = f[q] - p[q];
 }
 
+// Nodes of the R segments from T.gmin on (the first i0 = T.so[T.gmin] R
+// nodes are not built).
 __global__ void k_fintab_build(FinState fs, FinTab T, float* __restrict__ tp, float* __restrict__ tq) {
-  const long ntp = (long)T.nr * T.nw, ntq = (long)T.nr * T.nu;
+  const int i0 = T.so[T.gmin];
+  const long ntp = (long)(T.nr - i0) * T.nw, ntq = (long)(T.nr - i0) * T.nu;
   const long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (e >= ntp + ntq) return;
   const double h = fs.h;
   double f[6];
   float* out;
   if (e < ntp) {
-    const int i = (int)(e / T.nw), j = (int)(e % T.nw);
+    const int i = i0 + (int)(e / T.nw), j = (int)(e % T.nw);
     double r;
     int g;
     node_r(T, i, &r, &g);
     const double w = -h + (j + 0.5) * 2.0 * h / T.nw;
     f_minus_prop(fs, T, r, w, -h, g, f);
-    out = tp + (size_t)e * 8;
+    out = tp + ((size_t)i * T.nw + j) * 8;
   } else {
     const long e2 = e - ntp;
-    const int i = (int)(e2 / T.nu), k = (int)(e2 % T.nu);
+    const int i = i0 + (int)(e2 / T.nu), k = (int)(e2 % T.nu);
     double r;
     int g;
     node_r(T, i, &r, &g);
@@ -57,7 +60,7 @@ __global__ void k_fintab_build(FinState fs, FinTab T, float* __restrict__ tp, fl
     f_minus_prop(fs, T, r, wr, u, g, f);
     f_minus_prop(fs, T, r, wr, -h, g, f2);
     for (int q = 0; q < 6; ++q) f[q] -= f2[q];
-    out = tq + (size_t)e2 * 8;
+    out = tq + ((size_t)i * T.nu + k) * 8;
   }
   for (int q = 0; q < 6; ++q) out[q] = (float)f[q];
   out[6] = 0.f;
@@ -68,8 +71,10 @@ __global__ void k_fintab_build(FinState fs, FinTab T, float* __restrict__ tp, fl
 
 size_t fintab_floats() { return (size_t)8 * kFinTabR * (kFinTabW + kFinTabU); }
 
-cudaError_t fintab_build(cudaStream_t st, const FinState& fs, double rmax, float* buf, FinTab* out) {
+cudaError_t fintab_build(cudaStream_t st, const FinState& fs, double rmax, float* buf, FinTab* out, int gmin) {
+  if (gmin < 0 || gmin >= kFinSegs) return cudaErrorInvalidValue;
   FinTab T = {};
+  T.gmin = gmin;
   const double h = fs.h;
   T.nr = kFinTabR;
   T.nw = kFinTabW;
@@ -98,7 +103,7 @@ cudaError_t fintab_build(cudaStream_t st, const FinState& fs, double rmax, float
   float* tq = tp + (size_t)8 * T.nr * T.nw;
   T.tp = tp;
   T.tq = tq;
-  const long total = (long)T.nr * (T.nw + T.nu);
+  const long total = (long)(T.nr - T.so[gmin]) * (T.nw + T.nu);
   k_fintab_build<<<(unsigned)((total + 63) / 64), 64, 0, st>>>(fs, T, tp, tq);
   *out = T;
   return cudaGetLastError();

@@ -22,6 +22,8 @@
 // are cell-centred (W = 0 is never a node); the U nodes are uniform in
 // t = log(1 + |U|/u0), shifted by half a step (U = 0 is never a node).
 // Pairs interpolate both tables bicubically (Catmull-Rom) in single precision.
+// Below R/h = 0.05 the fill evaluates the pairs again per pair in FP64
+// (launch_fin_near): LINTON's and PIDCOCK's values are not smooth in R.
 // The propagating-wave term of F (the k0 mode: p0 (-Y0, J0)(k0 R) with
 // p0 = pi/N0 cosh(k0(zq+h)) cosh(k0(zp+h)), and its derivatives; the
 // d_prop_part of FinGreen3D.f90:281-362) oscillates on the wavelength scale
@@ -49,6 +51,7 @@ struct FinTab {
   float k0;      // wave number WK
   float pk;      // pi e^(2 k0 h) / N0, N0 = h/2 (1 + sinh(2 k0 h) / (2 k0 h))
   double pk_d;   // the same in double (table build)
+  int gmin;      // first segment built: 2 when the pairs below R/h = 0.05 are evaluated per pair
 };
 
 // Propagating term, T = double (table build) or float (pairs): f = [re, im]
@@ -115,9 +118,31 @@ __device__ __forceinline__ void cr_weights(float t, float w[4]) {
   w[3] = 0.5f * (t3 - t2);
 }
 
+// Catmull-Rom weights of the end intervals of an axis with nodes lo..hi: the
+// stencil's node beyond the end is a ghost extrapolated from the nodes
+// inside (quadratically, f(lo-1) = 3 f(lo) - 3 f(lo+1) + f(lo+2), or
+// linearly on a 2-node axis), folded into their weights.  A ghost equal to
+// the end node instead would make the end intervals first-order accurate
+// (an error of about an eighth of the node spacing times the slope).
+__device__ __forceinline__ void cr_fold_ends(float w[4], int i0, int lo, int hi) {
+  const bool quad = hi - lo >= 2;
+  if (i0 == lo) {
+    const float g = w[0];
+    w[0] = 0.f;
+    if (quad) { w[1] += 3.f * g; w[2] -= 3.f * g; w[3] += g; }
+    else { w[1] += 2.f * g; w[2] -= g; }
+  }
+  if (i0 == hi - 1) {
+    const float g = w[3];
+    w[3] = 0.f;
+    if (quad) { w[2] += 3.f * g; w[1] -= 3.f * g; w[0] += g; }
+    else { w[2] += 2.f * g; w[1] -= g; }
+  }
+}
+
 // Bicubic Catmull-Rom interpolation of one table at fractional indices x
 // (first axis, nodes lo..hi of one R segment) and y (second axis, size n2);
-// stencil indices beyond the ends are clamped.
+// the end intervals use extrapolated ghost nodes (cr_fold_ends).
 __device__ __forceinline__ void cr_interp(const float* __restrict__ T, int lo, int hi, int n2, float x, float y,
                                           float f[6]) {
   x = fminf(fmaxf(x, (float)lo), (float)hi);
@@ -126,6 +151,8 @@ __device__ __forceinline__ void cr_interp(const float* __restrict__ T, int lo, i
   float wx[4], wy[4];
   cr_weights(x - (float)i0, wx);
   cr_weights(y - (float)j0, wy);
+  cr_fold_ends(wx, i0, lo, hi);
+  cr_fold_ends(wy, j0, 0, n2 - 1);
 #pragma unroll
   for (int q = 0; q < 6; ++q) f[q] = 0.f;
 #pragma unroll
@@ -149,7 +176,7 @@ __device__ __forceinline__ void cr_interp(const float* __restrict__ T, int lo, i
 // F(R, zq, zp) from the tables (see above).
 __device__ __forceinline__ void fintab_eval(const FinTab& T, float R, float zq, float zp, float f[6]) {
   const float rh = R / T.h;
-  const int g = (rh < 0.0005f) ? 0 : (rh < 0.05f) ? 1 : (rh < 0.5f) ? 2 : 3;  // the reference's switches
+  const int g = max(T.gmin, (rh < 0.0005f) ? 0 : (rh < 0.05f) ? 1 : (rh < 0.5f) ? 2 : 3);  // the reference's switches
   const float a = T.sa[g], b = T.sb[g], c = T.sc[g];
   const float v = fminf(fmaxf((R - a) / (b - a), 0.f), 1.f);
   const float u = (c > 0.f) ? log1pf(v * T.sx[g]) / c : v;

@@ -32,12 +32,18 @@ cudaError_t launch_green_fill_fin(cudaStream_t st, const double* rec, const doub
 cudaError_t launch_green_fill_fin_fma(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
                                       const FinState& fs, int grn_kind, float2* A, float2* S, long lda, int* status,
                                       int* bins);
+// Finite depth, complex64 output, only the pairs with R/h < 0.05 (LINTON and
+// PIDCOCK), written over A and S with the reference's arithmetic (no FMA);
+// bins: scratch of fin_bins_ints(n, tn) ints.
+cudaError_t launch_fin_near(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
+                            const FinState& fs, int grn_kind, float2* A, float2* S, long lda, int* bins, int ndiag);
 // Tabulated finite-depth Green function of the mixed form (hg_fintab.cu):
 // fintab_floats() floats of device scratch; rmax = largest horizontal
-// distance between a field point and a source.
+// distance between a field point and a source; gmin = first R segment built
+// and used (2: the pairs below R/h = 0.05 come from launch_fin_near).
 struct FinTab;
 size_t fintab_floats();
-cudaError_t fintab_build(cudaStream_t st, const FinState& fs, double rmax, float* buf, FinTab* out);
+cudaError_t fintab_build(cudaStream_t st, const FinState& fs, double rmax, float* buf, FinTab* out, int gmin = 0);
 // diag: device scratch of 6 n floats (the coincident pairs' FP64 values).
 cudaError_t launch_green_fill_mixed_fin(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
                                         const FinState& fs, const FinTab& tab, double ox, double oy,

@@ -212,13 +212,16 @@ void copy_in(std::vector<T>& dst, const T* src, size_t count) {
 
 // Device memory of the GMRES paths beyond hg_solve_footprint: the Krylov
 // and preconditioned bases (restart 8 for the refinement, 25 for solver 2),
-// and for solver 2 the preconditioner (the diagonal, or the per-body
-// diagonal blocks and their pivots).
+// for solver 2 the preconditioner (the diagonal, or the per-body diagonal
+// blocks and their pivots), and in the FP64 form without lids the n x nc
+// right-hand-side block of the square system, which hg_solve_footprint
+// counts only for the mixed form and for lids.
 static size_t iter_bytes(const hg_opts& o, const hg_request& q) {
   const size_t n = (size_t)q.n, nc = (size_t)6 * q.nbody + (size_t)(q.nbeta > 0 ? q.nbeta : 0);
   size_t b = 0;
   if (o.solver == 2) {
     b += (size_t)(2 * 25 + 2) * n * nc * 16;
+    if (o.precision != HG_PREC_MIXED && q.irsp != 1) b += n * nc * 16;
     if (q.nbody <= 1) {
       b += n * 16;
     } else {

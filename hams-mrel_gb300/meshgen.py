@@ -120,6 +120,32 @@ def cylinder(radius, draft, n_az, n_vert, n_ring, cx=0.0, cy=0.0, lid_rings=0) -
     return body
 
 
+def hemisphere(radius, n_az, n_lat, cx=0.0, cy=0.0) -> Body:
+    """Floating hemisphere (the submerged half of a sphere centred on the
+    waterline): n_az x n_lat panels between latitude circles spaced evenly in
+    polar angle, nodes on the sphere, triangles at the bottom pole."""
+    nodes, panels = [], []
+    for i in range(n_lat):
+        th = 0.5 * math.pi * i / n_lat  # 0 at the waterline
+        for k in range(n_az):
+            t = 2.0 * math.pi * k / n_az
+            nodes.append((cx + radius * math.cos(th) * math.cos(t), cy + radius * math.cos(th) * math.sin(t),
+                          -radius * math.sin(th)))
+    pole = len(nodes)
+    nodes.append((cx, cy, -radius))
+    for i in range(n_lat):
+        for k in range(n_az):
+            k1 = (k + 1) % n_az
+            a, b = i * n_az + k, i * n_az + k1
+            if i + 1 < n_lat:
+                panels.append([a, b, b + n_az, a + n_az])
+            else:
+                panels.append([a, b, pole])
+    body = Body(np.array(nodes, dtype=np.float64), panels, (cx, cy, 0.0))
+    _orient_inward(body.nodes, body.panels, np.array([cx, cy, -radius / 2.0]))
+    return body
+
+
 def box(lx, ly, draft, dx, cx=0.0, cy=0.0) -> Body:
     """Rectangular barge centred at (cx, cy) with panels of side ~dx."""
     nx, ny, nz = max(1, round(lx / dx)), max(1, round(ly / dx)), max(1, round(draft / dx))

@@ -57,9 +57,10 @@ typedef struct {
                             the complex64 LU); both stop on refine_tol / max_refine */
     int fin_table;       /* mixed form, finite depth: Green function from per-frequency tables of
                             FINGREEN3D's own values (exact split into functions of (R, zq-zp)
-                            and (R, zq+zp), bicubic interpolation in FP32; ~50x faster than FP64
-                            per pair from a few thousand panels; A, B, F within 1e-5..6e-4 of the
-                            FP64 form, the worst where PIDCOCK's near-surface values are noisy):
+                            and (R, zq+zp), bicubic interpolation in FP32) for the pairs with
+                            R/h >= 0.05; the pairs below (LINTON and PIDCOCK, whose values jump
+                            with R) are evaluated per pair in FP64 after the tables; A, B, F
+                            within 1e-4 of the FP64 oracle (measured 5e-6..4e-5):
                             1 on, 0 off (FP64 per pair), -1 automatic (on from 1e6 pairs; default) */
     int solver;          /* linear solver, the ControlFile's Solver_type (ISOLV, src/HAMS_Prog.f90:161):
                             1 = LU and triangular solves (default); 2 = restarted GMRES(25) of
@@ -293,6 +294,10 @@ int hg_panel_geometry(int n, int ntnd, const double *nodes, const int *ncon, con
  *   - All calls on a device share the array, and each call overwrites the
  *     part it uses: calls that overlap on the GPU (several host threads or
  *     contexts at once) race and must be serialised by the caller.
+ *   - The looked-up address is kept for the life of the process.  A caller
+ *     that resets a device (cudaDeviceReset) must not call this entry point
+ *     on that device again in the same process: the kept address would no
+ *     longer be valid.
  * Arguments, results and errors are those of hg_green_points. */
 #define HG_NOALLOC_MAX_POINTS 65536
 int hg_green_points_noalloc(hg_ctx *ctx, int npts, const double *pts, const int *flags, double *out);
@@ -381,7 +386,10 @@ int hg_stage_times(const hg_ctx *ctx, float *ms4);
  * hg_solve_sweep; one at a time when field points are written); the deck's
  * Solver_type (src/InputFiles.f90:177-191) sets opts->solver.
  * hg_case_write writes the result files from given A, B, F (per entry
- * blocks as hg_solve_sweep returns them).  Errors: non-zero return, message
+ * blocks as hg_solve_sweep returns them); it also (re)creates the
+ * pressure/elevation .6p files of the run empty, as the reference's
+ * CreateWamitFiles does, so a driver writing its own field-point output to
+ * output_dir must call it first.  Errors: non-zero return, message
  * in err[errlen].  Symmetry planes (ISX/ISY) are rejected. */
 typedef struct hg_case hg_case;
 int hg_case_read(const char *input_dir, hg_case **out, char *err, int errlen);

@@ -130,3 +130,58 @@ def compare_result_file(got_path, exp_path, nlines=None, floor=1e-6, scale_by="c
             assert excess <= 1.0, f"{got_path}:{i + 1} field {j + 1}: {a} vs {b} (tol {tol:.3g})\n{lg}\n{le}"
             worst = max(worst, excess)
     return worst, nlines
+
+
+def rigid_body_matrices(mesh, rho=1000.0, g=9.80665):
+    """Mass and hydrostatic restoring matrices (6 nbody square) of freely
+    floating rigid bodies, from the hull panels alone (divergence theorem
+    with the inward panel normals of the reference meshes): displaced
+    volume V, centre of buoyancy, waterplane area and moments about each
+    body's reference point (x, y of its panels' mean, z = 0).  The centre of
+    gravity is put below the waterline at 1.5 z_b (so every body is stable)
+    and the radii of gyration at 0.35 of the body's largest extent.  These
+    stand in for the Hydrostatic.in decks of the reference (read by
+    ReadHydroStatic, src/HydroStatic.f90) in the motion equations of
+    SolveMotion (src/SolveMotion.f90:25-111)."""
+    nb = len(mesh.body_ranges)
+    M = np.zeros((6 * nb, 6 * nb))
+    C = np.zeros((6 * nb, 6 * nb))
+    for b, (f, l) in enumerate(mesh.body_ranges):
+        sl = slice(f - 1, l)
+        p = mesh.xyz_p[sl]
+        nz = mesh.dxyz_p[sl, 2]
+        ds = mesh.ds[sl]
+        ref = np.array([p[:, 0].mean(), p[:, 1].mean(), 0.0])
+        x, y, z = p[:, 0] - ref[0], p[:, 1] - ref[1], p[:, 2]
+        vol = -np.sum(z * nz * ds)
+        zb = -np.sum(0.5 * z * z * nz * ds) / vol
+        awp = np.sum(nz * ds)
+        sx, sy = np.sum(x * nz * ds), np.sum(y * nz * ds)
+        ixx, iyy, ixy = np.sum(y * y * nz * ds), np.sum(x * x * nz * ds), np.sum(x * y * nz * ds)
+        m = rho * vol
+        zg = 1.5 * zb
+        span = max(np.ptp(p[:, 0]), np.ptp(p[:, 1]), np.ptp(p[:, 2]))
+        kg = 0.35 * span
+        o = 6 * b
+        Mb = np.diag([m, m, m, m * kg * kg, m * kg * kg, m * kg * kg])
+        Mb[0, 4] = Mb[4, 0] = m * zg
+        Mb[1, 3] = Mb[3, 1] = -m * zg
+        Cb = np.zeros((6, 6))
+        Cb[2, 2] = rho * g * awp
+        Cb[2, 3] = Cb[3, 2] = rho * g * sy
+        Cb[2, 4] = Cb[4, 2] = -rho * g * sx
+        Cb[3, 3] = rho * g * (ixx + vol * zb) - m * g * zg
+        Cb[4, 4] = rho * g * (iyy + vol * zb) - m * g * zg
+        Cb[3, 4] = Cb[4, 3] = -rho * g * ixy
+        M[o:o + 6, o:o + 6] = Mb
+        C[o:o + 6, o:o + 6] = Cb
+    return M, C
+
+
+def motions(amas, bdmp, exfc, w, M, C):
+    """Response amplitude operators of SolveMotion (src/SolveMotion.f90:45-50,
+    linear damping only): [-w^2 (M + A) + i w B + C] x = -Im F - i Re F for
+    every heading (rows of exfc); returns (nbeta, 6 nbody) complex."""
+    left = -w * w * (M + amas) + 1j * w * bdmp + C
+    right = -np.imag(exfc) - 1j * np.real(exfc)
+    return np.linalg.solve(left, right.T).T

@@ -2,17 +2,38 @@
 
 The tables hold FINGREEN3D's own FP64 values on grids of (R, zq - zp) and
 (R, zq + zp) (an exact split of the function); pairs interpolate them in
-FP32.  Checked against the per-pair FP64 evaluation of the same mixed form
-(fin_table = 0) through added mass, damping and excitation force, for two
-depths, two frequencies and, with waterplane lids, the irregular-frequency
-form (lid field points sit on the free surface).
+FP32.  Below R/h = 0.05 (FINGREEN3D's LINTON and PIDCOCK methods) the
+reference's values are not smooth: LINTON's adaptive quadrature and the
+series length of PIDCOCK (an integer function of R/h, with Wynn's epsilon
+extrapolation on top) make them jump with R and depth by up to several per
+cent of the function at large k h (measured with the oracle at h = 150 m,
+w = 2.0 rad/s, k h = 61), so those pairs are evaluated per pair in FP64 after
+the table fill and only the EIGENE / EIGEN bands come from the tables.
+
+The mixed form's target holds here: added mass, damping and excitation
+force within 1e-4 (max-normalised) of the FP64 oracle, for two depths, two
+frequencies each and, with waterplane lids, the irregular-frequency form
+(lid field points sit on the free surface).
+
+The influence-matrix entries the tables supply (R/h >= 0.05) are held
+element-wise too, relative to the matrix's largest entry: 99.9 % of them
+within 2e-5 (measured on the CPU with the tables restated in numpy: 1e-8 to
+6e-6), and every one within 5e-4.  The few entries between those bounds are
+where the reference's epsilon-extrapolated EIGENE series lands on noise at
+the start of its band: at h = 40 m, w = 2 rad/s, R = 2.147 m its dG/dR is
+0.0111 where R = 2.14 m and 2.16 m give 0.0075 (measured with the oracle);
+no interpolation of a smooth function reproduces such points, and A, B, F
+above show they do not matter at 1e-4.
 """
 import numpy as np
 import pytest
 
-from helpers import max_norm_err
+from helpers import case_from_mesh, max_norm_err
 
 pytestmark = pytest.mark.gpu
+
+MIXED_TOL = 1e-4
+BETAS = (0.0, 0.6)  # radians
 
 
 def _run(pkg, mesh, h, w, table, irsp=0):
@@ -20,8 +41,9 @@ def _run(pkg, mesh, h, w, table, irsp=0):
     s = hg.Solver(precision=hg.HG_PREC_MIXED, fin_table=table)
     s.set_mesh(mesh.nodes, mesh.ncon, mesh.ncn, mesh.xyz_p, mesh.ds, mesh.pnsz, mesh.dxyz_p, mesh.body_ranges,
                mesh.lid_xyz_p if irsp == 1 else None)
+    s.keep_matrices(True)
     v, wk, w1, wvn = hg.wave_properties(3, w, h)
-    a, b, f, _ = s.solve_frequency(v, wk, w1, h, wvn, np.array([0.0, 0.6]), irsp=irsp, want_potentials=False)
+    a, b, f, _ = s.solve_frequency(v, wk, w1, h, wvn, np.array(BETAS), irsp=irsp, want_potentials=False)
     rows = mesh.n + (len(mesh.lid_xyz_p) if irsp == 1 else 0)
     A = s.get_matrix(0, rows)
     S = s.get_matrix(1, rows)
@@ -29,29 +51,35 @@ def _run(pkg, mesh, h, w, table, irsp=0):
     return a.copy(), b.copy(), f.copy(), A, S
 
 
-# A, B, F of the table path against the per-pair FP64 evaluation of the same
-# mixed form.  The reference's PIDCOCK values near the free surface carry
-# rounding noise of O(1e-2) in single derivatives (its epsilon extrapolation
-# of nearly converged sums); the tables interpolate noisy node values while
-# the per-pair path reproduces the noise point by point, so the two differ by
-# 1e-5 to 6e-4 (max-normalised) depending on depth and frequency, more than
-# the 4e-5 by which two FP64 builds of the reference differ here.  The bound
-# tested is that measured spread.
+def _far_mask(mesh, h, irsp):
+    """Pairs (field row, source column) with R/h >= 0.05: the table's bands."""
+    fp = mesh.xyz_p if irsp == 0 else np.vstack([mesh.xyz_p, mesh.lid_xyz_p])
+    dx = mesh.xyz_p[None, :, 0] - fp[:, None, 0]
+    dy = mesh.xyz_p[None, :, 1] - fp[:, None, 1]
+    return np.sqrt(dx * dx + dy * dy) / h >= 0.05
+
+
+def _check(pkg, oracle, mesh, h, w, irsp):
+    got = _run(pkg, mesh, h, w, 1, irsp)
+    case = case_from_mesh(oracle, mesh, h=h, headings_deg=[b * 180.0 / np.pi for b in BETAS], irsp=irsp)
+    ref = oracle.solve_frequency(case, w)
+    errs = [max_norm_err(got[0], ref.amas), max_norm_err(got[1], ref.bdmp), max_norm_err(got[2], ref.exfc)]
+    assert max(errs) < MIXED_TOL, errs
+    v, wk, w1, wvn = oracle.wave_properties(case.ctl, w)
+    Ao, So = oracle.assemble(case, v, wvn)
+    far = _far_mask(mesh, h, irsp)
+    for M, Mo in ((got[3], Ao), (got[4], So)):
+        e = np.abs(M - Mo)[far] / np.abs(Mo).max()
+        assert np.percentile(e, 99.9) < 2e-5 and e.max() < 5e-4, (np.percentile(e, 99.9), e.max())
+
+
 CASES = [(40.0, 0.8), (40.0, 2.0), (150.0, 0.8), (150.0, 2.0)]
 
 
 @pytest.mark.parametrize("h,w", CASES)
-def test_table_matches_per_pair_fp64(pkg, h, w):
-    mesh = pkg.meshgen.three_cylinders(with_lid=False)
-    ref = _run(pkg, mesh, h, w, 0)
-    got = _run(pkg, mesh, h, w, 1)
-    errs = [max_norm_err(got[k], ref[k]) for k in range(3)]
-    assert max(errs) < 1e-3, errs
+def test_table_matches_fp64_oracle(pkg, oracle, h, w):
+    _check(pkg, oracle, pkg.meshgen.three_cylinders(with_lid=False), h, w, 0)
 
 
-def test_table_with_lids(pkg):
-    mesh = pkg.meshgen.three_cylinders(with_lid=True)
-    ref = _run(pkg, mesh, 40.0, 1.3, 0, irsp=1)
-    got = _run(pkg, mesh, 40.0, 1.3, 1, irsp=1)
-    for k in range(3):
-        assert max_norm_err(got[k], ref[k]) < 1e-3
+def test_table_with_lids_matches_fp64_oracle(pkg, oracle):
+    _check(pkg, oracle, pkg.meshgen.three_cylinders(with_lid=True), 40.0, 1.3, 1)
