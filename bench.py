@@ -337,7 +337,7 @@ def ours(args, dist, rank, world, local):
     # ---- roofline of the dominant kernel (the LU trailing-update GEMM) ----
     roof = None
     if rank == 0 and args.solver == "lu":
-        roof = _roofline(s, mesh.n, prec, hg)
+        roof = _roofline(s, mesh.n, prec, hg, ms_max / args.steps)
     # ---- the CPU oracle on one frequency (the CPU baseline sample), and both GPU forms against it ----
     cpu, vs_oracle = None, None
     if rank == 0 and not args.no_cpu_baseline:
@@ -600,7 +600,57 @@ def _launch_count(n, prec, sweeps=1, nd=30, nbeta=8):
     return fill + lu + 5 + s1 * getrs + 3 * s1 + (1 + s1) + 2 * s1 + sweeps + forces
 
 
-def _roofline(s, n, prec, hg):
+# Counted per-pair work of the deep-water fill (oracle/opcount.py on the 6048-panel array): mean
+# over the 0.1-2.5 rad/s sweep, in operations per pair.
+F_PAIR_MEAN = 590.0
+
+
+def _roofline(s, n, prec, hg, ms_per_step, nd=30, nbeta=8):
+    """Roofline of the dominant kernel, the 32-column complex64 LU panel
+    (k_getf2_cluster_reg: 52 % of one solve's kernel time in the ncu launch
+    list), timed with CUDA events on the library's stream at the height of the
+    first panel (N rows): algorithmic bytes = the panel read once and written
+    once, 2 x N x 32 x 8 B.  Beside it the LU trailing update (the tcgen05
+    GEMM, timed at the first outer panel's shape m = n = N - 256, k = 256) and
+    the whole step (the algorithmic flops of one frequency-solve over the
+    measured time per step)."""
+    peaks, kind = _peaks()
+    out = None
+    if prec == hg.HG_PREC_MIXED:
+        try:
+            pms = s.bench_panel(n, 16)
+            pbytes = 2.0 * n * 32 * 8
+            gbs = pbytes / (pms / 1e3) / 1e9
+            out = {"kernel": "k_getf2_cluster_reg (32-column complex64 panel LU of the blocked factorisation, "
+                             "16-CTA cluster, rows in registers)",
+                   "bound": "hbm", "achieved": gbs, "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
+                   "frac": gbs / peaks.get("hbm_gbs", 6800.0), "peak_source": f"hbm_gbs of {kind} peaks",
+                   "bytes_per_launch": pbytes, "ms_per_launch": pms,
+                   # DRAM bytes of one 6048-row panel launch from the committed ncu capture
+                   "traffic": 1.668608e6 if n == 6048 else None,
+                   "note": "latency-bound: 32 dependent column steps, each a cluster-wide pivot search and one "
+                           "DSMEM message round; bytes/time is far below the HBM peak by construction, and the "
+                           "7 solves in flight hide it behind other solves' fills and tensor-core updates"}
+        except Exception:
+            out = None
+    gemm = _gemm_roofline(s, n, prec, hg)
+    flops = 8.0 / 3.0 * n ** 3 + 8.0 * n * n * (nd + nbeta) + F_PAIR_MEAN * n * n
+    tf = flops / (ms_per_step / 1e3) / 1e12
+    whole = {"flops_per_step": flops, "achieved_tflops": tf, "peak_tflops": peaks.get("bf16_tflops", 1900.0),
+             "frac": tf / peaks.get("bf16_tflops", 1900.0),
+             "what": "LU (8/3) N^3 + solves 8 N^2 (30 modes + 8 headings) + fill N^2 x 590 counted operations per "
+                     "pair, over ms_per_step, against the bf16 tensor peak"}
+    if out is None:
+        out = gemm
+        if out is not None:
+            out["whole_step"] = whole
+        return out
+    out["lu_trailing_update"] = gemm
+    out["whole_step"] = whole
+    return out
+
+
+def _gemm_roofline(s, n, prec, hg):
     """Roofline of the LU trailing update, the path's dense contraction: the
     library's tcgen05 GEMM (mixed form, split TF32) or its complex128 SIMT
     GEMM (FP64 form), timed with CUDA events on the library's stream at the

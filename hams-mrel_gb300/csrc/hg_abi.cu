@@ -68,6 +68,21 @@ struct hg_ctx {
   DevBuf<int> bins;                      // finite depth: pairs binned by the cost of their Green function
   DevBuf<float> tab;                     // finite depth, mixed form: tabulated Green function
   DevBuf<float4> pgauss;                 // mixed form: Gauss points of the panel integrals (relative to ox, oy)
+  // finite depth, mixed form: the near pairs (R/h < 0.05) keyed by (R, zq, zp), built once per mesh and
+  // depth (hg_fill_kernel / hg_fill_fin.cu); z-levels: the mesh's distinct depths (at most 2048)
+  bool zlev_ok = false;
+  DevBuf<double> zlev;
+  DevBuf<short> zsrc, zfld;
+  double near_h = 0.0;
+  int near_tn = -1, near_np = 0, near_nu = 0;
+  DevBuf<unsigned long long> near_tabr, near_tabk;
+  DevBuf<longlong2> near_keys;
+  DevBuf<int> near_cnt, near_slot;
+  DevBuf<int2> near_pairs;
+  DevBuf<double> near_F;
+  // deep water, mixed form: the self and adjacent pairs (FP64 Newman integrals) listed once per mesh
+  int mnear_tn = -1, mnear_np = 0;
+  DevBuf<int> mnear_list, mnear_cnt;
   // frequency
   double v = 0, wk = 0, w1 = 0, h = -1, nm0 = 0;
   int nk = 0;
@@ -163,6 +178,46 @@ FinState fin_state(const hg_ctx* c) {
 }
 
 bool mixed(const hg_ctx* c) { return c->o.precision == HG_PREC_MIXED; }
+
+// The mixed form's finite-depth pairs below R/h = 0.05 with their region-
+// method values computed once per distinct (R, zq, zp): the map of near
+// pairs to keys is built on the first frequency of a mesh and depth (one
+// host synchronisation for its size) and kept; every frequency evaluates
+// the keys and assembles the pairs from them.
+int near_pairs_dedup(hg_ctx* c, int tn) {
+  const int n = c->n;
+  if (c->near_tn != tn || c->near_h != c->h) {
+    CK(c->near_cnt.ensure(1 + 16));
+    if (hg::near_count(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, c->h, c->zsrc.p, c->zfld.p, c->near_cnt.p))
+      return fail(c, HG_ERR_CUDA, "near-pair count failed: %s", cudaGetErrorString(cudaGetLastError()));
+    int np = 0;
+    CK(cudaMemcpyAsync(&np, c->near_cnt.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    const unsigned cap = hg::near_table_size(np);
+    CK(c->near_tabr.ensure(cap));
+    CK(c->near_tabk.ensure(cap));
+    CK(c->near_slot.ensure(cap));
+    CK(c->near_pairs.ensure(np > 0 ? np : 1));
+    CK(c->near_keys.ensure(np > 0 ? np : 1));
+    CK(hg::near_build(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, c->h, c->zsrc.p, c->zfld.p, c->near_tabr.p,
+                      c->near_tabk.p, cap, c->near_cnt.p, c->near_slot.p, c->near_pairs.p, c->near_keys.p));
+    CK(hg::near_map(c->st, np, c->near_pairs.p, c->near_slot.p));
+    int nu = 0;
+    CK(cudaMemcpyAsync(&nu, c->near_cnt.p + 16, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    CK(c->near_F.ensure((size_t)6 * (nu > 0 ? nu : 1)));
+    c->near_tabr.release();  // the hash tables are needed only to build the map
+    c->near_tabk.release();
+    c->near_slot.release();
+    c->near_np = np;
+    c->near_nu = nu;
+    c->near_tn = tn;
+    c->near_h = c->h;
+  }
+  CK(hg::near_fill(c->st, c->rec.p, c->fx.p, c->tnf, tn, c->near_np, c->near_nu, c->near_pairs.p, c->near_keys.p,
+                   c->zlev.p, c->near_F.p, fin_state(c), c->o.grn_kind, c->Af.p, c->Sf.p, tn, tn));
+  return 0;
+}
 
 // Ensure the B/X/R buffers hold 6*nbody + nbeta columns.
 int ensure_rhs(hg_ctx* c, int nbeta) {
@@ -966,6 +1021,30 @@ int hg_set_mesh(hg_ctx* c, int n, int ntnd, const double* nodes, const int* ncon
   }
   CK(c->pgauss.ensure((size_t)n * hg::kPanelGauss));
   CK(hg::launch_panel_gauss(c->st, n, c->rec.p, c->ox, c->oy, c->pgauss.p));
+  {
+    // distinct depths of the sources (hull centroids) and field points (hull, then lid centroids)
+    std::vector<double> z;
+    z.reserve((size_t)n + nl);
+    for (int e = 0; e < n; ++e) z.push_back(xyz_p[e + 2 * (size_t)n]);
+    for (int e = 0; e < nl; ++e) z.push_back(lid_xyz_p[e + 2 * (size_t)nl]);
+    std::vector<double> lev(z);
+    std::sort(lev.begin(), lev.end());
+    lev.erase(std::unique(lev.begin(), lev.end()), lev.end());
+    c->zlev_ok = lev.size() <= 2048;
+    if (c->zlev_ok) {
+      std::vector<short> zi(z.size());
+      for (size_t k = 0; k < z.size(); ++k)
+        zi[k] = (short)(std::lower_bound(lev.begin(), lev.end(), z[k]) - lev.begin());
+      CK(c->zlev.ensure(lev.size()));
+      CK(c->zsrc.ensure(n));
+      CK(c->zfld.ensure((size_t)n + nl));
+      CK(cudaMemcpyAsync(c->zlev.p, lev.data(), lev.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
+      CK(cudaMemcpyAsync(c->zsrc.p, zi.data(), (size_t)n * sizeof(short), cudaMemcpyHostToDevice, c->st));
+      CK(cudaMemcpyAsync(c->zfld.p, zi.data(), ((size_t)n + nl) * sizeof(short), cudaMemcpyHostToDevice, c->st));
+    }
+    c->near_tn = -1;  // the near-pair maps belong to the previous mesh
+    c->mnear_tn = -1;
+  }
   CK(cudaStreamSynchronize(c->st));
   c->slots_mesh = false;
   c->mesh_set = true;
@@ -1059,7 +1138,10 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
       CK(hg::fintab_build(c->st, fs, 1.02 * c->rmax + 1.0, c->tab.p, &tab, near ? 2 : 0));
       CK(hg::launch_green_fill_mixed_fin(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, tab, c->ox, c->oy, c->pgauss.p,
                                          c->tab.p + hg::fintab_floats(), c->Af.p, c->Sf.p, tn, c->status.p));
-      if (near) {
+      if (near && c->zlev_ok) {
+        const int r = near_pairs_dedup(c, tn);
+        if (r) return r;
+      } else if (near) {
         CK(c->bins.ensure(hg::fin_bins_ints(n, tn)));
         CK(hg::launch_fin_near(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, c->o.grn_kind, c->Af.p, c->Sf.p, tn,
                                c->bins.p, tn));
@@ -1069,9 +1151,24 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
       if (binned) CK(c->bins.ensure(hg::fin_bins_ints(n, tn)));
       CK(hg::launch_green_fill_fin_fma(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, c->o.grn_kind, c->Af.p, c->Sf.p, tn,
                                        c->status.p, binned ? c->bins.p : nullptr));
-    } else if (!special && c->o.grn_kind == 8)
+    } else if (!special && c->o.grn_kind == 8) {
+      if (c->mnear_tn != tn) {
+        // the self and adjacent pairs, once per mesh: one synchronisation for their number
+        CK(c->mnear_cnt.ensure(1));
+        if (hg::mixed_near_count(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, c->ox, c->oy, c->mnear_cnt.p))
+          return fail(c, HG_ERR_CUDA, "near-pair count failed: %s", cudaGetErrorString(cudaGetLastError()));
+        int np = 0;
+        CK(cudaMemcpyAsync(&np, c->mnear_cnt.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        CK(c->mnear_list.ensure(np > 0 ? np : 1));
+        CK(hg::mixed_near_build(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, c->ox, c->oy, c->mnear_cnt.p,
+                                c->mnear_list.p));
+        c->mnear_np = np;
+        c->mnear_tn = tn;
+      }
       CK(hg::launch_green_fill_mixed(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, c->v, c->ox, c->oy, c->pgauss.p, c->Af.p,
-                                     c->Sf.p, tn, c->status.p));
+                                     c->Sf.p, tn, c->status.p, -1, c->mnear_list.p, c->mnear_np));
+    }
     else
       CK(hg::launch_green_fill<float2>(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, deep, c->o.grn_kind, c->Af.p,
                                        c->Sf.p, tn, c->status.p));
@@ -1447,8 +1544,11 @@ size_t hg_solve_footprint(int precision, int n, int nl, int nbody, int nbeta, in
   size_t b = 0;
   // mesh: node and panel arrays, 288-byte panel records, field points
   b += nn * (4 * sizeof(int) + 12 * sizeof(double) + 36 * sizeof(double)) + (nn + nl) * 3 * sizeof(double);
-  // finite depth: one int per pair for the cost-binned fill
+  // finite depth: one int per pair for the cost-binned fill; in the mixed form also the near pairs'
+  // map (pair index and key slot, 8 bytes per pair, and the keys, 16 bytes each, at most one per pair; their
+  // values are 48 bytes per distinct key)
   b += sizeof(int) * tn * nn;
+  if (precision == HG_PREC_MIXED) b += 24 * tn * nn;
   // right-hand sides, solutions, source weights, split-K workspace
   b += sizeof(double2) * (tn * nc + nn * nc + nn * (nbeta > 0 ? nbeta : 1) + 16 * tn * nc);
   b += hg::rhs_work_bytes(n, (int)tn, nbody, nbeta);
@@ -1651,6 +1751,63 @@ int hg_bench_gemm(hg_ctx* c, int precision, int m, int n, int k, int iters, floa
   return check_status(c);
 }
 
+namespace {
+// Pseudo-random complex64 entries in [-1, 1) (a hash of the index).
+__global__ void k_fill_hash(long count, unsigned seed, float2* __restrict__ a) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < count; e += (long)gridDim.x * blockDim.x) {
+    unsigned h = (unsigned)e * 2654435761u ^ seed;
+    h ^= h >> 15; h *= 2246822519u; h ^= h >> 13; h *= 3266489917u; h ^= h >> 16;
+    const unsigned g = h * 747796405u + 2891336453u;
+    a[e] = make_float2((float)(h >> 8) * (2.f / 16777216.f) - 1.f, (float)(g >> 8) * (2.f / 16777216.f) - 1.f);
+  }
+}
+}  // namespace
+
+int hg_bench_panel(hg_ctx* c, int m, int iters, float* ms_per_launch) {
+  if (!c) return -1;
+  if (m < 32) return fail(c, -2, "m must be at least 32");
+  if (iters <= 0 || iters > 64) return fail(c, -3, "iters must be in 1..64");
+  if (!ms_per_launch) return fail(c, -4, "ms_per_launch is NULL");
+  if (!hg::panel_cluster_supported<float>(m)) return fail(c, -2, "no cluster panel for %d rows", m);
+  cudaSetDevice(c->o.device);
+  const size_t count = (size_t)m * 32;
+  float2 *p = nullptr, *p0 = nullptr;
+  int *piv = nullptr, *inf = nullptr;
+  std::vector<cudaEvent_t> ev(2 * iters, nullptr);
+  cudaError_t e = cudaMalloc(&p, count * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMalloc(&p0, count * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMalloc(&piv, 32 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&inf, sizeof(int));
+  if (e == cudaSuccess) {
+    k_fill_hash<<<1216, 256, 0, c->st>>>((long)count, 12345u, p0);
+    e = cudaGetLastError();
+  }
+  for (int k = 0; k < 2 * iters && e == cudaSuccess; ++k) e = cudaEventCreate(&ev[k]);
+  for (int it = -1; it < iters && e == cudaSuccess; ++it) {
+    e = cudaMemcpyAsync(p, p0, count * sizeof(float2), cudaMemcpyDeviceToDevice, c->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(inf, 0, sizeof(int), c->st);
+    if (e == cudaSuccess && it >= 0) e = cudaEventRecord(ev[2 * it], c->st);
+    if (e == cudaSuccess) e = hg::panel_cluster<float>(c->st, p, m, m, 32, piv, 0, inf);
+    if (e == cudaSuccess && it >= 0) e = cudaEventRecord(ev[2 * it + 1], c->st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  float total = 0.f;
+  for (int it = 0; it < iters && e == cudaSuccess; ++it) {
+    float ms = 0.f;
+    e = cudaEventElapsedTime(&ms, ev[2 * it], ev[2 * it + 1]);
+    total += ms;
+  }
+  int info = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&info, inf, sizeof(int), cudaMemcpyDeviceToHost);
+  for (auto x : ev)
+    if (x) cudaEventDestroy(x);
+  cudaFree(p); cudaFree(p0); cudaFree(piv); cudaFree(inf);
+  if (e != cudaSuccess) return fail(c, HG_ERR_CUDA, "hg_bench_panel: %s", cudaGetErrorString(e));
+  if (info < 0) return fail(c, HG_ERR_DEVICE, "hg_bench_panel: a bounded cluster wait ran out");
+  *ms_per_launch = total / iters;
+  return check_status(c);
+}
+
 int hg_gemm_check(hg_ctx* c, int variant, int m, int n, int k, const double* a, int lda, const double* b, int ldb,
                   double* cm, int ldc) {
   if (!c) return -1;
@@ -1697,6 +1854,18 @@ int hg_mark(hg_ctx* c, int slot) {
   CK(cudaEventRecord(c->user_ev[slot], c->st));
   return 0;
 }
+
+}  // extern "C"
+
+// For the serving loop's device timeline (hg_serve.cpp): milliseconds from
+// ref, recorded earlier on this context's device, to event slot of hg_mark.
+int hg_mark_since(const hg_ctx* c, int slot, cudaEvent_t ref, float* ms) {
+  if (!c || !ref || !ms || slot < 0 || slot >= 16 || !c->user_ev[slot]) return -1;
+  if (cudaEventSynchronize(c->user_ev[slot]) != cudaSuccess) return -1;
+  return cudaEventElapsedTime(ms, ref, c->user_ev[slot]) == cudaSuccess ? 0 : -1;
+}
+
+extern "C" {
 
 int hg_elapsed(hg_ctx* c, int s0, int s1, float* ms) {
   if (!c) return -1;

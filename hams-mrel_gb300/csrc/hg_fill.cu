@@ -233,7 +233,20 @@ __device__ __forceinline__ void panel_gauss_points(const double* __restrict__ pr
 // distance zp + zq needs them).  FIN: finite depth, the Green function from
 // the tables of hg_fintab.cuh plus FINGREEN3D's Rankine pair (FinGreen3D.f90
 // :120-150) in FP32; otherwise deep water (inf_green_f).
-template <bool FIN>
+// Squared FP32 distance of a pair, with the multiply-adds spelled out so
+// that the tile kernel and the near-pair kernel round it alike.
+__device__ __forceinline__ float pair_d2f(float dxf, float dyf, float dzf) {
+  return fmaf(dzf, dzf, fmaf(dyf, dyf, dxf * dxf));
+}
+
+// The self and adjacent pairs (FP32 squared distance within 0.0016 of the
+// squared FLAG radius: 2 panel sizes), whose Newman integrals the mixed form
+// computes in FP64.
+__device__ __forceinline__ bool mixed_near(float d2f, float fl2) { return d2f <= 0.0016f * fl2; }
+
+// SKIPNEAR: leave the mixed_near pairs to k_green_fill_mixed_near (deep
+// water), so that no warp of this FP32 kernel runs the FP64 Newman integral.
+template <bool FIN, bool SKIPNEAR = false>
 __global__ void __launch_bounds__(FILL_ROWS)
 k_green_fill_mixed(const double* __restrict__ rec, const double* __restrict__ fx, int ldf, int n, int tn, float vf,
                    double ox, double oy, const float4* __restrict__ pg, FinTab tab, const float* __restrict__ diag,
@@ -291,8 +304,9 @@ k_green_fill_mixed(const double* __restrict__ rec, const double* __restrict__ fx
     const int j = col0 + jj;
     const float dxf = px[0] - xpf, dyf = px[1] - ypf, zqf = px[2];
     const float dzf = zpf - zqf;
-    const float d2f = dxf * dxf + dyf * dyf + dzf * dzf;
+    const float d2f = pair_d2f(dxf, dyf, dzf);
     const float fl2 = px[3];
+    if (SKIPNEAR && mixed_near(d2f, fl2)) continue;
     int flag;
     if (fabsf(d2f - fl2) > 1e-3f * fl2) {
       flag = d2f < fl2 ? 1 : 0;
@@ -303,7 +317,7 @@ k_green_fill_mixed(const double* __restrict__ rec, const double* __restrict__ fx
     }
     float sij = 0.f, d0 = 0.f, d1 = 0.f, d2 = 0.f;
     if (flag) {
-      if (d2f <= 0.0016f * fl2) {
+      if (mixed_near(d2f, fl2)) {
         double s64, e0, e1, e2;
         newman_pair(tile + jj * PR_SIZE, xp, yp, zp, s64, e0, e1, e2);
         sij = (float)s64; d0 = (float)e0; d1 = (float)e1; d2 = (float)e2;
@@ -366,15 +380,96 @@ k_green_fill_mixed(const double* __restrict__ rec, const double* __restrict__ fx
   }
 }
 
+// The mixed_near pairs of the deep-water mixed fill, listed once per mesh as
+// i + j tn (COUNT = true: counted only).  The FP32 quantities are those of
+// k_green_fill_mixed, computed the same way.
+template <bool COUNT>
+__global__ void k_mixed_near_list(const double* __restrict__ rec, const double* __restrict__ fx, int ldf, int n,
+                                  int tn, double ox, double oy, int* __restrict__ counter, int* __restrict__ list) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  bool near = false;
+  if (i < tn) {
+    const double* pr = rec + (size_t)j * PR_SIZE;
+    const float xqf = (float)(pr[PR_XQ] - ox), yqf = (float)(pr[PR_XQ + 1] - oy), zqf = (float)pr[PR_XQ + 2];
+    const float fl2 = (float)(pr[PR_FLAGD] * pr[PR_FLAGD]);
+    const float xpf = (float)(fx[i] - ox), ypf = (float)(fx[i + ldf] - oy), zpf = (float)fx[i + 2 * (size_t)ldf];
+    near = mixed_near(pair_d2f(xqf - xpf, yqf - ypf, zpf - zqf), fl2);
+  }
+  const unsigned act = __ballot_sync(0xffffffffu, near);
+  if (!act) return;
+  const int lane = threadIdx.x & 31, leader = __ffs(act) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(counter, __popc(act));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (!COUNT && near) list[base + __popc(act & ((1u << lane) - 1u))] = i + j * tn;
+}
+
+// The listed pairs with the arithmetic of k_green_fill_mixed's near branch:
+// FLAG = 1, the FP64 Newman integral, the FP32 Green function and assembly.
+__global__ void __launch_bounds__(128)
+k_green_fill_mixed_near(const double* __restrict__ rec, const double* __restrict__ fx, int ldf, int tn, int np,
+                        const int* __restrict__ list, float vf, double ox, double oy, float2* __restrict__ A,
+                        float2* __restrict__ S, long lda, int ndiag) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < np; k += gridDim.x * blockDim.x) {
+    const int p = list[k];
+    const int i = p % tn, j = p / tn;
+    const double* pr = rec + (size_t)j * PR_SIZE;
+    const double xp = fx[i], yp = fx[i + ldf], zp = fx[i + 2 * (size_t)ldf];
+    const float xpf = (float)(xp - ox), ypf = (float)(yp - oy), zpf = (float)zp;
+    const float dxf = (float)(pr[PR_XQ] - ox) - xpf, dyf = (float)(pr[PR_XQ + 1] - oy) - ypf, zqf = (float)pr[PR_XQ + 2];
+    const float dzf = zpf - zqf;
+    double s64, e0, e1, e2;
+    newman_pair(pr, xp, yp, zp, s64, e0, e1, e2);
+    const float sij = (float)s64, d0 = (float)e0, d1 = (float)e1, d2 = (float)e2;
+    float2 g[4];
+    inf_green_f(dxf, dyf, zpf + zqf, dzf, vf, 1, g);
+    const float ear = (float)pr[PR_DS], n0 = (float)pr[PR_N], n1 = (float)pr[PR_N + 1], n2 = (float)pr[PR_N + 2];
+    float ar = (d0 + g[1].x * ear) * n0 + (d1 + g[2].x * ear) * n1 + (d2 + g[3].x * ear) * n2;
+    const float ai = (g[1].y * ear) * n0 + (g[2].y * ear) * n1 + (g[3].y * ear) * n2;
+    const float sr = sij + g[0].x * ear;
+    if (i == j && i < ndiag) ar += 6.28318530717959f;
+    A[i + (long)j * lda] = make_float2(ar, ai);
+    S[i + (long)j * lda] = make_float2(sr, g[0].y * ear);
+  }
+}
+
 cudaError_t launch_green_fill_mixed(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
                                     double v, double ox, double oy, const float4* pg, float2* A, float2* S, long lda,
-                                    int* status, int ndiag) {
+                                    int* status, int ndiag, const int* near_list, int near_np) {
   cudaError_t e = upload_cheb_constants();
   if (e != cudaSuccess) return e;
   dim3 grid((tn + FILL_ROWS - 1) / FILL_ROWS, (n + FILL_COLS - 1) / FILL_COLS);
   FinTab none = {};
-  k_green_fill_mixed<false><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, (float)v, ox, oy, pg, none, nullptr, A, S,
-                                                         lda, status, ndiag < 0 ? tn : ndiag);
+  const int nd = ndiag < 0 ? tn : ndiag;
+  if (!near_list) {
+    k_green_fill_mixed<false><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, (float)v, ox, oy, pg, none, nullptr, A,
+                                                           S, lda, status, nd);
+    return cudaGetLastError();
+  }
+  k_green_fill_mixed<false, true><<<grid, FILL_ROWS, 0, st>>>(rec, fx, ldf, n, tn, (float)v, ox, oy, pg, none, nullptr,
+                                                               A, S, lda, status, nd);
+  if (near_np > 0) {
+    int blocks = (near_np + 127) / 128;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_green_fill_mixed_near<<<blocks, 128, 0, st>>>(rec, fx, ldf, tn, near_np, near_list, (float)v, ox, oy, A, S, lda,
+                                                     nd);
+  }
+  return cudaGetLastError();
+}
+
+int mixed_near_count(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn, double ox,
+                     double oy, int* counter) {
+  if (cudaMemsetAsync(counter, 0, sizeof(int), st) != cudaSuccess) return -1;
+  k_mixed_near_list<true><<<dim3((tn + 127) / 128, n), 128, 0, st>>>(rec, fx, ldf, n, tn, ox, oy, counter, nullptr);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+cudaError_t mixed_near_build(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn, double ox,
+                             double oy, int* counter, int* list) {
+  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  k_mixed_near_list<false><<<dim3((tn + 127) / 128, n), 128, 0, st>>>(rec, fx, ldf, n, tn, ox, oy, counter, list);
   return cudaGetLastError();
 }
 

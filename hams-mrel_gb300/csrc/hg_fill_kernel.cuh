@@ -21,10 +21,12 @@ constexpr int FILL_COLS = 16;
 // function, assembly of A(i, j) and S(i, j) (the loop body of k_green_fill).
 // ndiag: rows below it are collocation points (row i is panel i's centroid)
 // and get the free term 2 pi on the diagonal; field points (ndiag = 0) none.
+// fpre (finite depth): FINGREEN3D's region-method values at this pair when
+// already evaluated (fin_green).
 template <bool DEEP, typename OUT>
 __device__ __forceinline__ void fill_pair(const double* __restrict__ pr, double xp, double yp, double zp, int i, int j,
                                           const FinState& fs, int grn_kind, OUT* __restrict__ A,
-                                          OUT* __restrict__ S, long lda, int ndiag) {
+                                          OUT* __restrict__ S, long lda, int ndiag, const double* fpre = nullptr) {
   const double xq = pr[PR_XQ], yq = pr[PR_XQ + 1], zq = pr[PR_XQ + 2];
   const double dist = sqrt((xp - xq) * (xp - xq) + (yp - yq) * (yp - yq) + (zp - zq) * (zp - zq));
   const int flag = (dist <= pr[PR_FLAGD]) ? 1 : 0;
@@ -32,7 +34,7 @@ __device__ __forceinline__ void fill_pair(const double* __restrict__ pr, double 
   if (flag) newman_pair(pr, xp, yp, zp, sij, d0, d1, d2);
   double2 g[4];
   if (DEEP) inf_green(xq, yq, zq, xp, yp, zp, fs.v, flag, g);
-  else fin_green(fs, xq, yq, zq, xp, yp, zp, flag, g);
+  else fin_green(fs, xq, yq, zq, xp, yp, zp, flag, g, fpre);
   if (grn_kind == 4) {
     sij = (float)sij; d0 = (float)d0; d1 = (float)d1; d2 = (float)d2;
 #pragma unroll

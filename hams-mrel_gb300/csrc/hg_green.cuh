@@ -850,8 +850,11 @@ HGD inline void fin_regions(const FinState& st, double rr, double zq, double zp,
 }
 
 // FINGREEN3D (FinGreen3D.f90:81-155) for source (xq,yq,zq) and field (xp,yp,zp).
+// fpre: the region methods' result f at this pair when already known (the
+// de-duplicated near pairs of the mixed form), else nullptr; the arithmetic
+// around it is the same either way.
 HGD inline void fin_green(const FinState& st, double xq, double yq, double zq, double xp,
-                                 double yp, double zp, int flag, double2 g[4]) {
+                                 double yp, double zp, int flag, double2 g[4], const double* fpre = nullptr) {
   const double xpq = xq - xp, ypq = yq - yp, zpq = zq + zp;
   const double rr = sqrt(xpq * xpq + ypq * ypq);
   const double r = sqrt(rr * rr + (zp - zq) * (zp - zq));
@@ -866,7 +869,11 @@ HGD inline void fin_green(const FinState& st, double xq, double yq, double zq, d
   }
   if (!(fabs(v) < SPD(1.e-8))) {
     double f[6];
-    fin_regions(st, rr, zq, zp, f);
+    if (fpre) {
+      for (int q = 0; q < 6; ++q) f[q] = fpre[q];
+    } else {
+      fin_regions(st, rr, zq, zp, f);
+    }
     if (rr > SPD(1.e-6)) {
       const double cx = xpq / rr, cy = ypq / rr;
       g[1] = make_double2(f[2] * cx, f[3] * cx);

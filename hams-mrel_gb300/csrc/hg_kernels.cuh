@@ -37,6 +37,27 @@ cudaError_t launch_green_fill_fin_fma(cudaStream_t st, const double* rec, const 
 // bins: scratch of fin_bins_ints(n, tn) ints.
 cudaError_t launch_fin_near(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
                             const FinState& fs, int grn_kind, float2* A, float2* S, long lda, int* bins, int ndiag);
+// The same pairs with their region-method values computed once per distinct
+// (R, zq, zp), keyed exactly (hg_fill_fin.cu).  zsrc[n] / zfld[tn]: index of
+// each source's / field point's depth in the mesh's distinct depths zlev (at
+// most 2048).  near_count: number of near pairs into *counter (device).
+// near_build: two hash tables of near_table_size(np) slots (cap) - R's bits,
+// then the keys -, the pairs listed as (i + j tn, key slot), the distinct
+// keys grouped by cost into ukeys (R's bits, depth indices) with
+// slot2u[slot] = key index; counters[1 + 15] = number of keys afterwards.
+// near_map: pair slots to key indices.  near_fill (per frequency): the
+// region methods per key into F (6 doubles each), then A(i, j), S(i, j) of
+// every near pair.
+int near_count(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn, double h,
+               const short* zsrc, const short* zfld, int* counter);
+unsigned near_table_size(int npairs);
+cudaError_t near_build(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn, double h,
+                       const short* zsrc, const short* zfld, unsigned long long* tabr, unsigned long long* tabk,
+                       unsigned cap, int* counters, int* slot2u, int2* pairs, longlong2* ukeys);
+cudaError_t near_map(cudaStream_t st, int np, int2* pairs, const int* slot2u);
+cudaError_t near_fill(cudaStream_t st, const double* rec, const double* fx, int ldf, int tn, int np, int nu,
+                      const int2* pairs, const longlong2* ukeys, const double* zlev, double* F, const FinState& fs,
+                      int grn_kind, float2* A, float2* S, long lda, int ndiag);
 // Tabulated finite-depth Green function of the mixed form (hg_fintab.cu):
 // fintab_floats() floats of device scratch; rmax = largest horizontal
 // distance between a field point and a source; gmin = first R segment built
@@ -53,9 +74,20 @@ inline size_t fin_bins_ints(int n, int tn) { return 16 + (size_t)n * tn; }
 cudaError_t launch_green_points_fin(cudaStream_t st, int npts, const double* pts, const int* flags, const FinState& fs,
                                     double* out);
 
+// ndiag: rows with the 2 pi free term (-1: all).  near_list (optional): the
+// self and adjacent pairs (i + j tn, from mixed_near_build, near_np of them),
+// evaluated by a kernel of their own after the FP32 tile kernel, which then
+// skips them; without it the tile kernel evaluates every pair.
 cudaError_t launch_green_fill_mixed(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn,
                                     double v, double ox, double oy, const float4* pg, float2* A, float2* S, long lda,
-                                    int* status, int ndiag = -1);  // ndiag: rows with the 2 pi free term (-1: all)
+                                    int* status, int ndiag = -1, const int* near_list = nullptr, int near_np = 0);
+// The deep-water mixed fill's self and adjacent pairs for the field points fx
+// (tn rows): mixed_near_count into *counter (device), mixed_near_build lists
+// them (list of *counter ints).
+int mixed_near_count(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn, double ox,
+                     double oy, int* counter);
+cudaError_t mixed_near_build(cudaStream_t st, const double* rec, const double* fx, int ldf, int n, int tn, double ox,
+                             double oy, int* counter, int* list);
 
 cudaError_t launch_incident(cudaStream_t st, int n, const double* xyz_p, const double* dxyz_p, int nbeta,
                             const double* betas, double v, double wk, double w1, double h, double2* w);

@@ -36,6 +36,10 @@
 
 #include "../../include/hamsgpu.h"
 
+// Milliseconds from ref (an event recorded earlier on the context's device)
+// to the context's hg_mark event in slot (hg_abi.cu).
+int hg_mark_since(const hg_ctx* c, int slot, cudaEvent_t ref, float* ms);
+
 namespace {
 
 typedef std::chrono::steady_clock Clock;
@@ -88,6 +92,10 @@ struct hg_server {
   int max_active = 0;
   bool stop = false;
   std::string err;
+  // device timeline: ref recorded at creation; per finished frequency-solve
+  // (ticket, frequency, start, end) in milliseconds since ref
+  cudaEvent_t ref = nullptr;
+  std::vector<double> timeline;
 };
 
 namespace {
@@ -183,17 +191,27 @@ void worker(hg_server* s, int k) {
       if (rc) msg = hg_last_error(sl.ctx);
       else sl.mesh_of = r->id;
     }
+    float t0 = 0.f, t1 = 0.f;
+    bool timed = false;
     if (!rc) {
       const int nd = 6 * r->nbody;
+      hg_mark(sl.ctx, 14);
       rc = hg_solve_frequency(sl.ctx, r->v[f], r->wk[f], r->w1[f], r->h, r->h > 0 ? &r->wvn[(size_t)f * r->nk] : nullptr,
                               r->h > 0 ? r->nk : 0, r->irsp, r->betas.data(), r->nbeta, r->isol,
                               &r->amas[(size_t)f * nd * nd], &r->bdmp[(size_t)f * nd * nd],
                               r->nbeta > 0 ? &r->exfc[(size_t)f * r->nbeta * nd * 2] : nullptr, nullptr, 0);
       if (rc) msg = hg_last_error(sl.ctx);
       sl.holds = std::max(sl.holds, r->slot_bytes);
+      if (!rc && s->ref && hg_mark(sl.ctx, 15) == 0 && hg_mark_since(sl.ctx, 14, s->ref, &t0) == 0 &&
+          hg_mark_since(sl.ctx, 15, s->ref, &t1) == 0)
+        timed = true;
     }
     {
       std::lock_guard<std::mutex> lk(s->mu);
+      if (timed) {
+        const double e[4] = {(double)r->id, (double)f, (double)t0, (double)t1};
+        s->timeline.insert(s->timeline.end(), e, e + 4);
+      }
       if (rc && r->rc == 0) {
         r->rc = rc;
         r->err = "frequency " + std::to_string(f) + ": " + msg;
@@ -251,6 +269,13 @@ int hg_server_create(hg_server** out, const hg_opts* opts, int nslots, double bu
   if (opts) s->opts = *opts;
   s->nslots = nslots;
   s->budget = (size_t)budget_bytes;
+  if (cudaSetDevice(s->opts.device) == cudaSuccess && cudaEventCreate(&s->ref) == cudaSuccess) {
+    if (cudaEventRecord(s->ref, 0) != cudaSuccess || cudaEventSynchronize(s->ref) != cudaSuccess) {
+      cudaEventDestroy(s->ref);
+      s->ref = nullptr;
+    }
+  }
+  cudaGetLastError();
   s->slots.resize(nslots);
   for (int k = 0; k < nslots; ++k) s->slots[k].th = std::thread(worker, s, k);
   *out = s;
@@ -268,6 +293,7 @@ void hg_server_destroy(hg_server* s) {
     if (sl.th.joinable()) sl.th.join();
   for (auto& sl : s->slots)
     if (sl.ctx) hg_destroy(sl.ctx);
+  if (s->ref) cudaEventDestroy(s->ref);
   delete s;
 }
 
@@ -373,6 +399,16 @@ int hg_server_stats(hg_server* s, double* stats) {
   stats[6] = (double)s->active.size();
   stats[7] = (double)s->budget;
   return 0;
+}
+
+int hg_server_timeline(hg_server* s, int max_entries, double* out) {
+  if (!s) return -1;
+  if (max_entries < 0 || (max_entries > 0 && !out)) return -2;
+  std::lock_guard<std::mutex> lk(s->mu);
+  const int count = (int)(s->timeline.size() / 4);
+  const int m = std::min(count, max_entries);
+  if (m > 0) std::memcpy(out, s->timeline.data(), (size_t)4 * m * sizeof(double));
+  return count;
 }
 
 }  // extern "C"

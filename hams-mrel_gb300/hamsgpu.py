@@ -27,7 +27,7 @@ EXPORTS = [
     "hg_solve_sweep", "hg_gmres_iterations", "hg_solve_footprint", "hg_server_create", "hg_server_submit",
     "hg_server_wait", "hg_server_stats", "hg_server_last_error", "hg_server_destroy", "hg_field_points",
     "hg_case_read", "hg_case_free", "hg_case_info", "hg_case_arrays", "hg_case_run", "hg_case_write",
-    "hg_iter_info", "hg_case_options",
+    "hg_iter_info", "hg_case_options", "hg_server_timeline", "hg_bench_panel",
 ]
 
 
@@ -109,11 +109,13 @@ def load(build_if_missing: bool = True):
     L.hg_server_submit.argtypes = [c_void_p, P(HgRequest), P(ctypes.c_longlong)]
     L.hg_server_wait.argtypes = [c_void_p, ctypes.c_longlong, c_double, c_void_p, c_void_p, c_void_p, c_void_p]
     L.hg_server_stats.argtypes = [c_void_p, c_void_p]
+    L.hg_server_timeline.argtypes = [c_void_p, c_int, c_void_p]
     L.hg_server_last_error.argtypes = [c_void_p]
     L.hg_server_last_error.restype = ctypes.c_char_p
     L.hg_server_destroy.argtypes = [c_void_p]
     L.hg_server_destroy.restype = None
     L.hg_bench_gemm.argtypes = [c_void_p, c_int, c_int, c_int, c_int, c_int, P(ctypes.c_float)]
+    L.hg_bench_panel.argtypes = [c_void_p, c_int, c_int, P(ctypes.c_float)]
     L.hg_gemm_check.argtypes = [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_void_p,
                                 c_int]
     L.hg_mark.argtypes = [c_void_p, c_int]
@@ -381,6 +383,12 @@ class Solver:
         self._check(self.L.hg_bench_gemm(self.h, variant, m, n, k, iters, ctypes.byref(ms)))
         return ms.value
 
+    def bench_panel(self, m, iters=16):
+        """Average ms of one complex64 32-column cluster panel LU of m rows."""
+        ms = ctypes.c_float()
+        self._check(self.L.hg_bench_panel(self.h, m, iters, ctypes.byref(ms)))
+        return ms.value
+
     def gmres_iterations(self):
         it = ctypes.c_int()
         self.L.hg_gmres_iterations(self.h, ctypes.byref(it))
@@ -485,6 +493,17 @@ class Server:
         keys = ["requests_done", "solves_done", "reserved_bytes", "peak_reserved_bytes", "max_admitted",
                 "queued", "admitted", "budget_bytes"]
         return dict(zip(keys, st.tolist()))
+
+    def timeline(self):
+        """Device intervals of the finished frequency-solves: array of rows
+        (ticket, frequency index, start ms, end ms), the times from CUDA
+        events on each slot's stream, relative to the server's creation."""
+        n = self.L.hg_server_timeline(self.h, 0, None)
+        if n < 0:
+            raise HamsGpuError(n, "hg_server_timeline failed")
+        out = np.zeros((max(n, 1), 4))
+        n = self.L.hg_server_timeline(self.h, n, _ptr(out))
+        return out[:n]
 
     def close(self):
         if getattr(self, "h", None):

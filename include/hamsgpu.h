@@ -252,6 +252,13 @@ int hg_server_submit(hg_server *srv, const hg_request *req, long long *ticket);
 int hg_server_wait(hg_server *srv, long long ticket, double timeout_s, double *amas, double *bdmp, double *exfc,
                    double *latency_ms);
 int hg_server_stats(hg_server *srv, double *stats);
+/* Device timeline of the finished frequency-solves (for showing that the
+ * solves of different requests overlap on the GPU): out[4 k .. 4 k + 3] =
+ * ticket, frequency index, start and end in milliseconds since the server
+ * was created, from CUDA events recorded on the slot's stream around the
+ * solve.  Copies min(max_entries, count) entries; returns count (all
+ * entries so far), or < 0 on a bad argument. */
+int hg_server_timeline(hg_server *srv, int max_entries, double *out);
 const char *hg_server_last_error(const hg_server *srv);
 void hg_server_destroy(hg_server *srv);
 
@@ -342,6 +349,14 @@ int hg_elapsed(hg_ctx *ctx, int slot0, int slot1, float *ms);
  * 2 complex64 tensor cores split TF32 (3 products), 3 complex64 tensor
  * cores TF32 (1 product); 2 and 3 include their operand packing. */
 int hg_bench_gemm(hg_ctx *ctx, int precision, int m, int n, int k, int iters, float *ms_per_launch);
+
+/* Average device time (ms, CUDA events around each launch) of the
+ * complex64 32-column panel LU of the blocked factorisation (the 16-CTA
+ * cluster kernel; the IZAMAX pivot search, interchange, scaling and rank-1
+ * updates of ZGETF2 inside ZGETRF, src/AssbMatx.f90:111) on an m x 32 panel
+ * of pseudo-random entries, restored before each of iters (<= 64) launches;
+ * used to report the roofline of the panel. */
+int hg_bench_panel(hg_ctx *ctx, int m, int iters, float *ms_per_launch);
 
 /* C = C - A B through one of those kernel variants on host arrays (all
  * COMPLEX*16, column-major; variants 1-3 round A, B, C to complex64 on the

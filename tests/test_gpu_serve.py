@@ -73,6 +73,17 @@ def test_mix_equals_alone(pkg, requests_and_alone):
     assert st["solves_done"] == sum(len(r[2]) for r in reqs)
     assert st["max_admitted"] >= 2  # the requests ran in the mix
     assert st["reserved_bytes"] == 0
+    # their work overlapped on the device: the CUDA-event intervals of solves of
+    # two different requests intersect
+    tl = srv.timeline()
+    assert len(tl) == st["solves_done"]
+    assert np.all(tl[:, 3] > tl[:, 2])
+    overlap = 0.0
+    for a in range(len(tl)):
+        for b in range(len(tl)):
+            if tl[a, 0] != tl[b, 0]:
+                overlap = max(overlap, min(tl[a, 3], tl[b, 3]) - max(tl[a, 2], tl[b, 2]))
+    assert overlap > 0.0, tl
     srv.close()
 
 
