@@ -431,14 +431,17 @@ __device__ __forceinline__ void load_row(float2 (&a)[kClusterNB], const float2* 
   }
 }
 
+// The cluster has as many CTAs (up to 16) as the panel needs at one row per
+// thread: ncta = ceil(m / 512), rpc = ceil(m / ncta).
 __global__ void __launch_bounds__(kClusterThreads, 1)
 k_getf2_cluster_reg(float2* __restrict__ P, long lda, int m, int jb, int rpc, int* __restrict__ ipiv, int k0,
                     int* __restrict__ info) {
   constexpr int kWarps = kClusterThreads / 32;
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
+  const int ncta = (int)cluster.num_blocks();
   __shared__ PanelMsgR sendbuf[2];
-  __shared__ PanelMsgR recv[2][kClusterCTAs];
+  __shared__ PanelMsgR recv[2][kClusterCTAs];  // ncta <= 16 slots used
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ float red_v[kWarps];
   __shared__ int red_i[kWarps];
@@ -459,8 +462,8 @@ k_getf2_cluster_reg(float2* __restrict__ P, long lda, int m, int jb, int rpc, in
     s_bad = 0;
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
-    mbar_expect_tx(&mbar[0], kClusterCTAs * kMsgBytes);
-    if (jb > 1) mbar_expect_tx(&mbar[1], kClusterCTAs * kMsgBytes);
+    mbar_expect_tx(&mbar[0], ncta * kMsgBytes);
+    if (jb > 1) mbar_expect_tx(&mbar[1], ncta * kMsgBytes);
   }
   cluster.sync();  // barriers initialised and armed everywhere before any copy
 
@@ -498,21 +501,21 @@ k_getf2_cluster_reg(float2* __restrict__ P, long lda, int m, int jb, int rpc, in
     }
     fence_proxy_async_smem();
     __syncthreads();
-    if (warp == 0 && lane < kClusterCTAs) {
+    if (warp == 0 && lane < ncta) {
       const uint32_t dst = mapa_shared(smem_addr(&recv[q][rank]), lane);
       const uint32_t bar = mapa_shared(smem_addr(&mbar[q]), lane);
       bulk_s2s_cluster(dst, smem_addr(&msg), kMsgBytes, bar);
     }
-    // (c) wait for the 16 messages of this column
+    // (c) wait for the ncta messages of this column
     if (!mbar_wait_timed(&mbar[q], (jj >> 1) & 1, kPanelWaitNs)) bad = true;
     if (__syncthreads_or(bad)) {
       if (tid == 0) s_bad = 1;
       break;
     }
-    if (tid == 0 && jj + 2 < jb) mbar_expect_tx(&mbar[q], kClusterCTAs * kMsgBytes);
-    // (d) the pivot: every warp reduces the 16 local messages
-    float pmax = (lane < kClusterCTAs) ? recv[q][lane].val : -1.f;
-    int p = (lane < kClusterCTAs) ? recv[q][lane].idx : INT_MAX;
+    if (tid == 0 && jj + 2 < jb) mbar_expect_tx(&mbar[q], ncta * kMsgBytes);
+    // (d) the pivot: every warp reduces the ncta local messages
+    float pmax = (lane < ncta) ? recv[q][lane].val : -1.f;
+    int p = (lane < ncta) ? recv[q][lane].idx : INT_MAX;
     warp_best(pmax, p);
     if (p == INT_MAX) p = jj;
     const int op = p / rpc;
@@ -610,19 +613,23 @@ cudaError_t panel_cluster<float>(cudaStream_t st, float2* P, long lda, int m, in
   if (rpc <= kClusterThreads) {  // one row per thread: the register-resident panel
     cudaError_t e = cudaFuncSetAttribute(k_getf2_cluster_reg, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
+    // as few CTAs as hold the panel at one row per thread: shorter panels
+    // (later in the factorisation) occupy fewer SMs and exchange fewer messages
+    const int ncta = (m + kClusterThreads - 1) / kClusterThreads;
+    const int rpcr = (m + ncta - 1) / ncta;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(kClusterCTAs, 1, 1);
+    cfg.gridDim = dim3(ncta, 1, 1);
     cfg.blockDim = dim3(kClusterThreads, 1, 1);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = kClusterCTAs;
+    attr[0].val.clusterDim.x = ncta;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_getf2_cluster_reg, P, lda, m, jb, rpc, ipiv, k0, info);
+    return cudaLaunchKernelEx(&cfg, k_getf2_cluster_reg, P, lda, m, jb, rpcr, ipiv, k0, info);
   }
   const size_t smem = (size_t)rpc * jb * sizeof(float2);
   if (smem > (size_t)(kPanelSmemMax - kPushStaticSmem)) return panel_cluster_smem<float>(st, P, lda, m, jb, ipiv, k0, info);
