@@ -405,6 +405,8 @@ def served(args):
             freqs = np.array([w])
         else:
             mesh, h, freqs, heads = mg.serving_case(rng)
+            if args.freq_cap:
+                freqs = freqs[:: max(1, -(-len(freqs) // args.freq_cap))][: args.freq_cap]
         v, wk, w1, wvn = _request_inputs(hg, freqs, h)
         reqs.append((mesh, h, v, wk, w1, wvn, np.array(heads) * math.pi / 180.0))
     nsolves = sum(len(r[2]) for r in reqs)
@@ -427,18 +429,25 @@ def served(args):
         return total, sorted(lat), st
 
     with ClockSampler(0) as clk:
-        total, lat, st = run([0.0] * len(reqs))
         rate = None
         if args.workload == "serve":
-            rate = 0.8 * len(reqs) / total  # requests per second at ~80 % of the measured capacity
+            # calibration: the first (up to) 24 requests submitted at once give the capacity in requests/s
+            full = reqs
+            reqs = full[:24]
+            t_cal, _, _ = run([0.0] * len(reqs))
+            rate = 0.8 * len(reqs) / t_cal  # requests per second at ~80 % of the measured capacity
+            reqs = full
             gaps = rng.exponential(1.0 / rate, size=len(reqs))
             total, lat, st = run(np.cumsum(gaps) - gaps[0])
+        else:
+            total, lat, st = run([0.0] * len(reqs))
     p = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))]  # noqa: E731
     line = {"metric": "freq-solves/s (%s form, mixed precision); p50/p99 request latency" % args.workload,
             "value": nsolves / total, "unit": "freq-solves/s", "n_gpus": 1, "steps": nsolves, "warmup": 0,
             "ms_per_step": 1e3 * total / nsolves, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "complex64+fp64-refine", "data": "synthetic",
             "config": {"workload": args.workload, "requests": len(reqs), "freq_solves": nsolves,
+                       "freqs_per_request_cap": args.freq_cap,
                        "panels_min_max": [min(r[0].n for r in reqs), max(r[0].n for r in reqs)],
                        "slots": args.slots, "hbm_budget_bytes": 150e9,
                        "arrival_rate_per_s": rate, "timing": "host wall clock, submission to last result"},
@@ -572,9 +581,9 @@ def _launch_count(n, prec, sweeps=1, nd=30, nbeta=8):
     """Kernels the library launches per frequency-solve, from its launch
     sequence (checked against the ncu launch list of one solve)."""
     nb, nbo = 32, 256
-    def inner(jb):  # 32-wide panels: panel + fused interchanges / L11 solve, then the update while columns remain
-        p = (jb + nb - 1) // nb
-        return 2 * p + (p - 1)
+    def inner(jb):  # 32-wide panels: panel + fused interchanges / L11 solve, then the update while columns remain,
+        p = (jb + nb - 1) // nb  # split into the next panel's columns and (on the side stream) the others
+        return 2 * p + (2 * p - 3 if p >= 2 else 0)
     tc = prec == 1 and n >= 1024
     if tc:
         outer = (n + nbo - 1) // nbo
@@ -588,7 +597,7 @@ def _launch_count(n, prec, sweeps=1, nd=30, nbeta=8):
     # right-hand sides permuted (gather + copy with the block inverses, else one interchange kernel), then
     # (block-inverse product or trsm, gemm) down and up
     getrs = (2 if tc else 1) + 2 * (2 * blocks - 1)
-    fill = 1
+    fill = 2 if prec == 1 else 1  # mixed deep water: the FP32 tile kernel and the self/adjacent-pair kernel
     forces = 1
     if prec == 0:
         return fill + lu + 3 + getrs + forces      # incident weights, source columns, S W product
@@ -699,6 +708,8 @@ def main():
     ap.add_argument("--workload", default="array", choices=["array", "batch", "serve", "three", "field"],
                     help="array: the 6048-panel frequency sweep (headline); batch / serve: the request server")
     ap.add_argument("--requests", type=int, default=None, help="batch / serve: number of requests")
+    ap.add_argument("--freq-cap", type=int, default=0,
+                    help="serve: at most this many of each request's frequencies (evenly spaced; 0: all)")
     args = ap.parse_args()
     if args.impl == "reference":
         rank = int(os.environ.get("RANK", "0"))

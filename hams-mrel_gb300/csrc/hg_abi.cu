@@ -131,6 +131,8 @@ struct hg_ctx {
   std::vector<hg_ctx*> slots;
   bool slots_mesh = false;  // slots hold the current mesh
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  // LU look-ahead: a lower-priority side stream for the updates behind the next panel
+  hg::LuAux lu_aux;
 };
 
 namespace {
@@ -874,7 +876,14 @@ int hg_create(hg_ctx** out, const hg_opts* opts) {
   if (c->o.fin_table < -1 || c->o.fin_table > 1) { delete c; return -2; }
   if (c->o.solver != 1 && c->o.solver != 2) { delete c; return -2; }
   cudaError_t e = cudaSetDevice(c->o.device);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+  // the context's stream carries the LU's critical path (the panels): it gets the higher priority,
+  // the look-ahead's side stream the lower one
+  int prio_low = 0, prio_high = 0;
+  if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->st, cudaStreamNonBlocking, prio_high);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->lu_aux.side, cudaStreamNonBlocking, prio_low);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->lu_aux.ev_main, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->lu_aux.ev_side, cudaEventDisableTiming);
   for (int k = 0; k < 5 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
   if (e == cudaSuccess) e = c->status.ensure(1);
   if (e == cudaSuccess) e = c->info.ensure(1);
@@ -916,6 +925,12 @@ void hg_destroy(hg_ctx* c) {
   }
   for (cudaEvent_t e : c->pev) cudaEventDestroy(e);
   if (c->pfork) cudaEventDestroy(c->pfork);
+  if (c->lu_aux.side) {
+    cudaStreamSynchronize(c->lu_aux.side);
+    cudaStreamDestroy(c->lu_aux.side);
+  }
+  if (c->lu_aux.ev_main) cudaEventDestroy(c->lu_aux.ev_main);
+  if (c->lu_aux.ev_side) cudaEventDestroy(c->lu_aux.ev_side);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -1118,9 +1133,9 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
       const int r = setup_iter_precond(c);
       if (r) return r;
     } else if (irsp == 1) {
-      CK(hg::getrf<double>(c->st, n, c->C.p, n, c->ipiv.p, c->info.p, nullptr));
+      CK(hg::getrf<double>(c->st, n, c->C.p, n, c->ipiv.p, c->info.p, nullptr, 0, 0, &c->lu_aux));
     } else {
-      CK(hg::getrf<double>(c->st, n, c->A.p, tn, c->ipiv.p, c->info.p, nullptr));
+      CK(hg::getrf<double>(c->st, n, c->A.p, tn, c->ipiv.p, c->info.p, nullptr, 0, 0, &c->lu_aux));
     }
   } else {
     CK(c->Af.ensure((size_t)tn * n));
@@ -1189,9 +1204,9 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
       const int r = setup_iter_precond(c);
       if (r) return r;
     } else if (irsp == 1) {
-      CK(hg::getrf<float>(c->st, n, c->Cf.p, n, c->ipiv.p, c->info.p, c->luws.p, lwb, c->o.lu_tensor));
+      CK(hg::getrf<float>(c->st, n, c->Cf.p, n, c->ipiv.p, c->info.p, c->luws.p, lwb, c->o.lu_tensor, &c->lu_aux));
     } else {
-      CK(hg::getrf<float>(c->st, n, c->Af.p, tn, c->ipiv.p, c->info.p, c->luws.p, lwb, c->o.lu_tensor));
+      CK(hg::getrf<float>(c->st, n, c->Af.p, tn, c->ipiv.p, c->info.p, c->luws.p, lwb, c->o.lu_tensor, &c->lu_aux));
     }
   }
   CK(cudaEventRecord(c->ev[2], c->st));

@@ -489,25 +489,53 @@ cudaError_t panel(cudaStream_t st, bool use_cluster, int n, typename cx<R>::T* A
 }
 
 // Columns [c0, c1) of A through one level of right-looking blocking with
-// 32-wide panels (pivots applied only inside [c0, c1)).
+// 32-wide panels (pivots applied only inside [c0, c1)).  With aux, the
+// update of the columns beyond the next panel runs on aux->side (see getrf).
 template <typename R>
 cudaError_t factor_columns(cudaStream_t st, bool use_cluster, int n, typename cx<R>::T* A, long lda, int c0, int c1,
-                           int* ipiv, int* info, int* perm = nullptr) {
+                           int* ipiv, int* info, int* perm = nullptr, const LuAux* aux = nullptr) {
   typedef typename cx<R>::T T;
   T mone, one;
   mone.x = -1; mone.y = 0; one.x = 1; one.y = 0;
+  bool side_pending = false;
+  cudaError_t e = cudaSuccess;
   for (int k = c0; k < c1; k += kNB) {
     const int jb = (c1 - k < kNB) ? c1 - k : kNB;
-    cudaError_t e = panel<R>(st, use_cluster, n, A, lda, k, jb, ipiv, info);
+    e = panel<R>(st, use_cluster, n, A, lda, k, jb, ipiv, info);
     if (e != cudaSuccess) return e;
+    // the interchanges touch every other column of [c0, c1): the side update must be done
+    if (side_pending) {
+      e = cudaStreamWaitEvent(st, aux->ev_side, 0);
+      if (e != cudaSuccess) return e;
+      side_pending = false;
+    }
     const int other = c1 - c0 - jb + (perm ? 1 : 0);
     if (other > 0) k_swap_trsm<T><<<(other + 7) / 8, 256, 0, st>>>(A, lda, c0, c1, k, jb, ipiv, perm);
     const int rest = c1 - k - jb;
-    if (rest > 0) {
-      e = gemm<R>(st, false, n - k - jb, rest, jb, mone, A + (k + jb) + (long)k * lda, lda,
-                  A + k + (long)(k + jb) * lda, lda, one, A + (k + jb) + (long)(k + jb) * lda, lda);
+    if (rest <= 0) continue;
+    const int m = n - k - jb;
+    const T* L21 = A + (k + jb) + (long)k * lda;
+    const T* U12 = A + k + (long)(k + jb) * lda;
+    T* A22 = A + (k + jb) + (long)(k + jb) * lda;
+    if (aux && rest > kNB) {
+      // the next panel's columns here, the others on the side stream
+      e = gemm<R>(st, false, m, kNB, jb, mone, L21, lda, U12, lda, one, A22, lda);
+      if (e == cudaSuccess) e = cudaEventRecord(aux->ev_main, st);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(aux->side, aux->ev_main, 0);
+      if (e == cudaSuccess)
+        e = gemm<R>(aux->side, false, m, rest - kNB, jb, mone, L21, lda, U12 + (long)kNB * lda, lda, one,
+                    A22 + (long)kNB * lda, lda);
+      if (e == cudaSuccess) e = cudaEventRecord(aux->ev_side, aux->side);
+      if (e != cudaSuccess) return e;
+      side_pending = true;
+    } else {
+      e = gemm<R>(st, false, m, rest, jb, mone, L21, lda, U12, lda, one, A22, lda);
       if (e != cudaSuccess) return e;
     }
+  }
+  if (side_pending) {
+    e = cudaStreamWaitEvent(st, aux->ev_side, 0);
+    if (e != cudaSuccess) return e;
   }
   return cudaGetLastError();
 }
@@ -579,13 +607,14 @@ k_apply_inv(int jb, int nc, const float2* __restrict__ M, const float2* __restri
 
 template <typename R>
 cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* ipiv, int* info, void* work,
-                  size_t work_bytes, int tc_passes) {
+                  size_t work_bytes, int tc_passes, const LuAux* aux) {
+  if (aux && (!aux->side || !aux->ev_main || !aux->ev_side)) aux = nullptr;
   cudaError_t e = cudaMemsetAsync(info, 0, sizeof(int), st);
   if (e != cudaSuccess) return e;
   const bool use_cluster = panel_cluster_supported<R>(n);
   const bool tc = sizeof(R) == 4 && tc_passes != 0 && n >= kTcMinN && work &&
                   work_bytes >= lu_work_bytes(n, tc_passes) && cgemm_tc_supported();
-  if (!tc) return factor_columns<R>(st, use_cluster, n, A, lda, 0, n, ipiv, info);
+  if (!tc) return factor_columns<R>(st, use_cluster, n, A, lda, 0, n, ipiv, info, nullptr, aux);
   // Two levels: 256-wide outer panels factorised by the 32-wide loop above,
   // then U12 = L11^-1 A12 and the tensor-core update A22 -= L21 U12.  U12
   // is formed as A12 - (I - L11^-1) A12 on the tensor cores too, with
@@ -601,7 +630,7 @@ cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* i
   const size_t blk = (size_t)kOuterNB * kOuterNB;
   for (int K = 0; K < n; K += kOuterNB) {
     const int jbo = (n - K < kOuterNB) ? n - K : kOuterNB;
-    e = factor_columns<R>(st, use_cluster, n, A, lda, K, K + jbo, ipiv, info, perm);
+    e = factor_columns<R>(st, use_cluster, n, A, lda, K, K + jbo, ipiv, info, perm, aux);
     if (e != cudaSuccess) return e;
     k_laswp<T><<<(n + 127) / 128, 128, 0, st>>>(A, lda, n, ipiv, K, K + jbo, K, K + jbo);
     // inverse of this diagonal block's unit-lower triangle (for U12 here and
@@ -710,8 +739,8 @@ cudaError_t getrs(cudaStream_t st, int n, int nrhs, const typename cx<R>::T* LU,
   return cudaGetLastError();
 }
 
-template cudaError_t getrf<double>(cudaStream_t, int, double2*, long, int*, int*, void*, size_t, int);
-template cudaError_t getrf<float>(cudaStream_t, int, float2*, long, int*, int*, void*, size_t, int);
+template cudaError_t getrf<double>(cudaStream_t, int, double2*, long, int*, int*, void*, size_t, int, const LuAux*);
+template cudaError_t getrf<float>(cudaStream_t, int, float2*, long, int*, int*, void*, size_t, int, const LuAux*);
 template cudaError_t getrs<double>(cudaStream_t, int, int, const double2*, long, const int*, double2*, long);
 template cudaError_t getrs<float>(cudaStream_t, int, int, const float2*, long, const int*, float2*, long);
 

@@ -49,9 +49,20 @@ cudaError_t cgemm_skinny(cudaStream_t st, int m, int n, int k, float2 alpha, con
 // 3xTF32 or TF32) with work a 256-byte aligned device scratch of at least
 // lu_work_bytes(n, tc_passes) bytes; tc_passes = 0 keeps every update on the
 // SIMT kernels (work unused).
+//
+// Look-ahead (aux, optional): a second stream of lower priority and two
+// events.  After each 32-column panel only the next panel's 32 columns are
+// updated on st; the update of the remaining columns runs on aux->side while
+// the next panel is factorised on st (the interchanges of that panel wait for
+// it).  The arithmetic of every entry is that of the same update in one
+// launch split by columns.
+struct LuAux {
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_main = nullptr, ev_side = nullptr;
+};
 template <typename R>
 cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* ipiv, int* info, void* work,
-                  size_t work_bytes = 0, int tc_passes = 0);
+                  size_t work_bytes = 0, int tc_passes = 0, const LuAux* aux = nullptr);
 
 // Solve A X = B with the factors of getrf; B is n x nrhs (ldb), overwritten.
 template <typename R>
