@@ -581,9 +581,9 @@ def _launch_count(n, prec, sweeps=1, nd=30, nbeta=8):
     """Kernels the library launches per frequency-solve, from its launch
     sequence (checked against the ncu launch list of one solve)."""
     nb, nbo = 32, 256
-    def inner(jb):  # 32-wide panels: panel + fused interchanges / L11 solve, then the update while columns remain,
-        p = (jb + nb - 1) // nb  # split into the next panel's columns and (on the side stream) the others
-        return 2 * p + (2 * p - 3 if p >= 2 else 0)
+    def inner(jb, split=False):  # 32-wide panels: panel + fused interchanges / L11 solve, then the update
+        p = (jb + nb - 1) // nb   # while columns remain (the FP64 form splits it: next panel's columns, the rest)
+        return 2 * p + ((2 * p - 3 if p >= 2 else 0) if split else p - 1)
     tc = prec == 1 and n >= 1024
     if tc:
         outer = (n + nbo - 1) // nbo
@@ -592,7 +592,7 @@ def _launch_count(n, prec, sweeps=1, nd=30, nbeta=8):
         # then one batched U_kk^-1
         lu = 1 + sum(inner(min(nbo, n - k)) for k in range(0, n, nbo)) + 2 * outer + 7 * (outer - 1) + 1
     else:
-        lu = inner(n)
+        lu = inner(n, split=prec == 0)
     blocks = (n + nbo - 1) // nbo
     # right-hand sides permuted (gather + copy with the block inverses, else one interchange kernel), then
     # (block-inverse product or trsm, gemm) down and up

@@ -131,7 +131,9 @@ struct hg_ctx {
   std::vector<hg_ctx*> slots;
   bool slots_mesh = false;  // slots hold the current mesh
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
-  // LU look-ahead: a lower-priority side stream for the updates behind the next panel
+  // LU look-ahead of the FP64 form: a lower-priority side stream for the updates behind the next
+  // panel (measured: FP64 LU 569 ms against 640 ms; the complex64 LU, whose updates are short, lost
+  // throughput with it: 78 against 85 freq-solves/s with 7 solves in flight, so it runs without)
   hg::LuAux lu_aux;
 };
 
@@ -1204,9 +1206,9 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
       const int r = setup_iter_precond(c);
       if (r) return r;
     } else if (irsp == 1) {
-      CK(hg::getrf<float>(c->st, n, c->Cf.p, n, c->ipiv.p, c->info.p, c->luws.p, lwb, c->o.lu_tensor, &c->lu_aux));
+      CK(hg::getrf<float>(c->st, n, c->Cf.p, n, c->ipiv.p, c->info.p, c->luws.p, lwb, c->o.lu_tensor));
     } else {
-      CK(hg::getrf<float>(c->st, n, c->Af.p, tn, c->ipiv.p, c->info.p, c->luws.p, lwb, c->o.lu_tensor, &c->lu_aux));
+      CK(hg::getrf<float>(c->st, n, c->Af.p, tn, c->ipiv.p, c->info.p, c->luws.p, lwb, c->o.lu_tensor));
     }
   }
   CK(cudaEventRecord(c->ev[2], c->st));
