@@ -631,12 +631,13 @@ def _roofline(s, n, prec, hg, ms_per_step, nd=30, nbeta=8):
             pbytes = 2.0 * n * 32 * 8
             gbs = pbytes / (pms / 1e3) / 1e9
             out = {"kernel": "k_getf2_cluster_reg (32-column complex64 panel LU of the blocked factorisation, "
-                             "16-CTA cluster, rows in registers)",
+                             "cluster of ceil(rows / 512) CTAs, rows in registers)",
                    "bound": "hbm", "achieved": gbs, "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
                    "frac": gbs / peaks.get("hbm_gbs", 6800.0), "peak_source": f"hbm_gbs of {kind} peaks",
                    "bytes_per_launch": pbytes, "ms_per_launch": pms,
-                   # DRAM bytes of one 6048-row panel launch from the committed ncu capture
-                   "traffic": 1.668608e6 if n == 6048 else None,
+                   # DRAM bytes of one panel launch from the committed ncu capture (a 5408-row panel,
+                   # 1.63 MB read), scaled to N rows by the panel's size
+                   "traffic": 1.625856e6 * n / 5408.0 if n == 6048 else None,
                    "note": "latency-bound: 32 dependent column steps, each a cluster-wide pivot search and one "
                            "DSMEM message round; bytes/time is far below the HBM peak by construction, and the "
                            "7 solves in flight hide it behind other solves' fills and tensor-core updates"}
@@ -680,11 +681,11 @@ def _gemm_roofline(s, n, prec, hg):
            "peak_source": f"bf16_tflops of {kind} peaks", "flops_per_launch": flops, "ms_per_launch": ms,
            "traffic": None}
     if variant == 2:
-        # DRAM bytes of one launch of this shape from the committed ncu capture (6016 x 6016 x 256)
-        out["traffic"] = (510.149888 + 259.160576) * 1e6 if n == 6048 else None
+        # DRAM bytes of one launch of this shape (5792 x 5792 x 256) from the committed ncu capture
+        out["traffic"] = (486.998528 + 235.5008) * 1e6 if n == 6048 else None
         out["note"] = ("algorithmic complex flops; the hardware does 3 TF32 products per real product and TF32 "
                        "runs at half the bf16 rate, so the tensor-pipe utilisation is about 6 x frac "
-                       "(ncu: 73 % tensor-pipe activity at this shape)")
+                       "(ncu: 72 % tensor-pipe activity at this shape)")
     return out
 
 
