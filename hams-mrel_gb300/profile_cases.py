@@ -14,7 +14,7 @@ repository root, e.g.
                              triangular solves, refinement residuals
   step [PREC]                one frequency-solve of the 6048-panel 5-body
                              benchmark array (fill, LU, solves, forces)
-  fill N H PREC              one Green fill + LU of a cylinder array of about N
+  fill N H PREC              two Green fills + LUs of a cylinder array of about N
                              panels at depth H metres (H <= 0: deep water)
 """
 from __future__ import annotations
@@ -75,11 +75,12 @@ def case_fill(n, h, prec):
     s.set_mesh(mesh.nodes, mesh.ncon, mesh.ncn, mesh.xyz_p, mesh.ds, mesh.pnsz, mesh.dxyz_p, mesh.body_ranges)
     hh = float(h) if h > 0 else -1.0
     v, wk, w1, wvn = hamsgpu.wave_properties(3, 1.0, hh)
-    s.set_frequency(v, wk, w1, hh, wvn)
-    s.fill_factor(0)
-    t = s.stage_times()
-    print(f"fill n={len(mesh.ncn)} h={hh} prec={prec}: fill {t[0]:.2f} ms ({len(mesh.ncn) ** 2 / t[0] / 1e3:.3f} "
-          f"Mpairs/s), lu {t[1]:.2f} ms")
+    for rep in range(2):  # the second fill reuses what the first built once per mesh
+        s.set_frequency(v, wk, w1, hh, wvn)
+        s.fill_factor(0)
+        t = s.stage_times()
+        print(f"fill {rep + 1} n={len(mesh.ncn)} h={hh} prec={prec}: fill {t[0]:.2f} ms "
+              f"({len(mesh.ncn) ** 2 / t[0] / 1e3:.3f} Mpairs/s), lu {t[1]:.2f} ms")
     s.close()
 
 
