@@ -129,7 +129,11 @@ struct hg_ctx {
   std::vector<int> h_ncon, h_ncn, h_ranges;
   // solve slots: child contexts with their own stream and buffers
   std::vector<hg_ctx*> slots;
-  bool slots_mesh = false;  // slots hold the current mesh
+  unsigned mesh_gen = 0;   // counts hg_set_mesh calls on this context
+  unsigned slot_gen = ~0u;  // a slot: the parent's mesh_gen of the mesh it holds
+  // pinned staging of the potentials read back to the caller's (pageable) arrays
+  double2* pin_out = nullptr;
+  size_t pin_cap = 0;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   // LU look-ahead of the FP64 form: a lower-priority side stream for the updates behind the next
   // panel (measured: FP64 LU 569 ms against 640 ms; the complex64 LU, whose updates are short, lost
@@ -838,10 +842,24 @@ int build_rhs(hg_ctx* c, int nbeta, const double* betas_h, bool modes) {
   return 0;
 }
 
+// Columns c0 .. c0 + nc - 1 of the potentials to the caller's array (leading
+// dimension ldm): one device copy into a pinned staging buffer of this
+// context, then the columns by this host thread (the solve slots of a sweep
+// read back side by side instead of queueing on the driver's pageable path).
 int copy_out(hg_ctx* c, int c0, int nc, double* host, int ldm) {
   if (!host || nc <= 0) return 0;
-  CK(cudaMemcpy2DAsync(host, (size_t)ldm * sizeof(double2), c->X.p + (size_t)c0 * c->n, (size_t)c->n * sizeof(double2),
-                       (size_t)c->n * sizeof(double2), nc, cudaMemcpyDeviceToHost, c->st));
+  const size_t cnt = (size_t)c->n * nc;
+  if (c->pin_cap < cnt) {
+    if (c->pin_out) CK(cudaFreeHost(c->pin_out));
+    c->pin_out = nullptr;
+    c->pin_cap = 0;
+    CK(cudaMallocHost((void**)&c->pin_out, cnt * sizeof(double2)));
+    c->pin_cap = cnt;
+  }
+  CK(cudaMemcpyAsync(c->pin_out, c->X.p + (size_t)c0 * c->n, cnt * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  for (int j = 0; j < nc; ++j)
+    std::memcpy(host + (size_t)2 * ldm * j, c->pin_out + (size_t)c->n * j, (size_t)c->n * sizeof(double2));
   return 0;
 }
 
@@ -915,6 +933,7 @@ void hg_destroy(hg_ctx* c) {
   c->rws.release();
   for (hg_ctx* sl : c->slots) hg_destroy(sl);
   c->slots.clear();
+  if (c->pin_out) cudaFreeHost(c->pin_out);
   for (int k = 0; k < 5; ++k)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   for (int k = 0; k < 16; ++k)
@@ -973,6 +992,10 @@ int hg_set_mesh(hg_ctx* c, int n, int ntnd, const double* nodes, const int* ncon
     prev = t;
   }
   if (prev != n) return fail(c, -14, "body ranges cover %d of %d panels", prev, n);
+  // from here the previous mesh is gone: a failure below leaves no mesh set,
+  // and the solve slots re-take the mesh at their next sweep
+  c->mesh_set = false;
+  ++c->mesh_gen;
   cudaSetDevice(c->o.device);
   c->n = n; c->nl = nl; c->tn = n + nl; c->tnf = n + nl; c->ntnd = ntnd; c->nbody = nbody;
   c->bstart = bs; c->bend = be;
@@ -1063,7 +1086,6 @@ int hg_set_mesh(hg_ctx* c, int n, int ntnd, const double* nodes, const int* ncon
     c->mnear_tn = -1;
   }
   CK(cudaStreamSynchronize(c->st));
-  c->slots_mesh = false;
   c->mesh_set = true;
   c->factored = false;
   c->rad_done = c->dif_done = false;
@@ -1426,25 +1448,14 @@ int hg_solve_sweep(hg_ctx* c, int nfreq, const double* v, const double* wk, cons
   if (mxpot && ldm < c->n) return fail(c, -18, "ldm %d < n %d", ldm, c->n);
   if (!c->mesh_set) return fail(c, HG_ERR_STATE, "hg_set_mesh must come first");
   if (nfreq == 0) return 0;
-  if (!c->slots_mesh) {
-    for (hg_ctx* sl : c->slots) hg_destroy(sl);
-    c->slots.clear();
-  }
+  // Slots keep their buffers across sweeps; a slot that does not hold the
+  // current mesh takes it in its own worker thread, before its first solve.
   while ((int)c->slots.size() < nslots) {
     hg_ctx* sl = nullptr;
     int r = hg_create(&sl, &c->o);
     if (r) return fail(c, r, "creating solve slot %d failed", (int)c->slots.size());
-    r = hg_set_mesh(sl, c->n, c->ntnd, c->h_nodes.data(), c->h_ncon.data(), c->h_ncn.data(), c->h_xyz.data(),
-                    c->h_ds.data(), c->h_pnsz.data(), c->h_dxyz.data(), c->nl, c->nl ? c->h_lid.data() : nullptr,
-                    c->nbody, c->h_ranges.data());
-    if (r) {
-      std::string msg = sl->err;
-      hg_destroy(sl);
-      return fail(c, r, "mesh of solve slot %d: %s", (int)c->slots.size(), msg.c_str());
-    }
     c->slots.push_back(sl);
   }
-  c->slots_mesh = true;
   const int nd = 6 * c->nbody;
   const size_t mx_cols = (size_t)nd + nbeta;
   // Fork/join on the device: the slots' streams wait for the work queued on
@@ -1455,9 +1466,22 @@ int hg_solve_sweep(hg_ctx* c, int nfreq, const double* v, const double* wk, cons
   for (int k = 0; k < nslots; ++k) CK(cudaStreamWaitEvent(c->slots[k]->st, c->fork_ev, 0));
   std::atomic<int> next(0);
   std::vector<int> slot_rc(nslots, 0), slot_freq(nslots, -1);
+  std::vector<char> mesh_failed(nslots, 0);
   auto worker = [&](int k) {
     hg_ctx* sl = c->slots[k];
     cudaSetDevice(sl->o.device);
+    if (sl->slot_gen != c->mesh_gen) {
+      const int r = hg_set_mesh(sl, c->n, c->ntnd, c->h_nodes.data(), c->h_ncon.data(), c->h_ncn.data(),
+                                c->h_xyz.data(), c->h_ds.data(), c->h_pnsz.data(), c->h_dxyz.data(), c->nl,
+                                c->nl ? c->h_lid.data() : nullptr, c->nbody, c->h_ranges.data());
+      if (r) {
+        slot_rc[k] = r;
+        mesh_failed[k] = 1;
+        next.store(nfreq);
+        return;
+      }
+      sl->slot_gen = c->mesh_gen;
+    }
     for (;;) {
       const int i = next.fetch_add(1);
       if (i >= nfreq) break;
@@ -1492,6 +1516,7 @@ int hg_solve_sweep(hg_ctx* c, int nfreq, const double* v, const double* wk, cons
   int sw = 0;
   double res = 0.0;
   for (int k = 0; k < nslots; ++k) {
+    if (mesh_failed[k]) return fail(c, slot_rc[k], "mesh of solve slot %d: %s", k, c->slots[k]->err.c_str());
     if (slot_rc[k]) return fail(c, slot_rc[k], "frequency %d (slot %d): %s", slot_freq[k], k, c->slots[k]->err.c_str());
     sw = std::max(sw, c->slots[k]->sweeps);
     res = std::fmax(res, c->slots[k]->resid);

@@ -16,6 +16,8 @@ repository root, e.g.
                              benchmark array (fill, LU, solves, forces)
   fill N H PREC              two Green fills + LUs of a cylinder array of about N
                              panels at depth H metres (H <= 0: deep water)
+  panel M [ITERS]            the 32-column complex64 cluster panel LU of M rows
+                             (hg_bench_panel), ITERS timed launches
 """
 from __future__ import annotations
 
@@ -84,6 +86,13 @@ def case_fill(n, h, prec):
     s.close()
 
 
+def case_panel(m, iters=4):
+    s = hamsgpu.Solver(precision=hamsgpu.HG_PREC_MIXED)
+    ms = s.bench_panel(m, iters)
+    print(f"panel m={m}: {1e3 * ms:.1f} us/launch")
+    s.close()
+
+
 def main(argv):
     if not argv:
         print(__doc__)
@@ -97,6 +106,8 @@ def main(argv):
         case_step(*args)
     elif cmd == "fill":
         case_fill(*args)
+    elif cmd == "panel":
+        case_panel(*args)
     else:
         print(__doc__)
         return 2

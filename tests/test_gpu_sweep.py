@@ -57,3 +57,39 @@ def test_sweep_reports_errors(pkg):
     with pytest.raises(hg.HamsGpuError):
         s.solve_sweep(v, wk, w1, 40.0, None, [0.0], nslots=2)
     s.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_sweep_after_mesh_change_matches_fresh_context(pkg, precision):
+    """Slots keep their buffers across sweeps and take a new mesh in their own
+    worker thread: a sweep after set_mesh with another mesh (and with more
+    slots than before, so old and new slots mix) gives exactly what a fresh
+    context gives on that mesh."""
+    hg = pkg.hamsgpu
+    m1 = pkg.meshgen.single_cylinder()
+    m2 = pkg.meshgen.combine([pkg.meshgen.hemisphere(5.0, 24, 8)])
+    freqs = np.linspace(0.4, 1.6, 5)
+    betas = np.array([0.0, 0.9])
+    v, wk, w1, _ = _inputs(hg, freqs, -1.0)
+
+    def mesh_args(m):
+        return (m.nodes, m.ncon, m.ncn, m.xyz_p, m.ds, m.pnsz, m.dxyz_p, m.body_ranges)
+
+    fresh = hg.Solver(precision=precision)
+    fresh.set_mesh(*mesh_args(m2))
+    ref = fresh.solve_sweep(v, wk, w1, -1.0, None, betas, nslots=1, want_potentials=True)
+    fresh.close()
+    s = hg.Solver(precision=precision)
+    s.set_mesh(*mesh_args(m1))
+    s.solve_sweep(v[:2], wk[:2], w1[:2], -1.0, None, betas, nslots=2)
+    s.set_mesh(*mesh_args(m2))
+    got = s.solve_sweep(v, wk, w1, -1.0, None, betas, nslots=3, want_potentials=True)
+    # back to the first mesh with fewer slots, then the second again with all of them
+    s.set_mesh(*mesh_args(m1))
+    s.solve_sweep(v[:1], wk[:1], w1[:1], -1.0, None, betas, nslots=1)
+    s.set_mesh(*mesh_args(m2))
+    again = s.solve_sweep(v, wk, w1, -1.0, None, betas, nslots=3, want_potentials=True)
+    s.close()
+    for k in (0, 1, 2, 4):
+        np.testing.assert_array_equal(got[k], ref[k])
+        np.testing.assert_array_equal(again[k], ref[k])
