@@ -740,33 +740,20 @@ __device__ __forceinline__ void trsm_stage(T* buf, const T* __restrict__ A, long
   }
 }
 
-// Batched form (gridDim.y > 1): block b solves with the diagonal block at
-// A + b a_bstride (order min(jb, ntot - b jb)) for X + b x_bstride.
-// ident: X is taken as the identity (not read), so the solve produces the
-// inverse; sub-blocks where column `col` of the result is known to be zero
-// (above the diagonal for lower, below it for upper) are skipped.
 template <typename T, bool UPPER>
 __global__ void __launch_bounds__(kTrsmBlock)
-k_trsm_col(const T* __restrict__ A, long lda, int jb, T* __restrict__ X, long ldx, long a_bstride, long x_bstride,
-           int ntot, int ident) {
+k_trsm_col(const T* __restrict__ A, long lda, int jb, T* __restrict__ X, long ldx) {
   constexpr int SB = TrsmSub<T>::SB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* bufs = reinterpret_cast<T*>(smem_raw);  // 2 x [SB][kTrsmBlock]
   __shared__ T x[kTrsmBlock];
   const int col = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  A += blockIdx.y * a_bstride;
-  X += blockIdx.y * x_bstride;
-  jb = min(jb, ntot - (int)blockIdx.y * jb);
-  if (ident && col >= jb) return;  // whole CTA: the inverse of a smaller last block has fewer columns
   T* xc = X + (long)col * ldx;
   T zero;
   zero.x = 0; zero.y = 0;
   const int nsb = (jb + SB - 1) / SB;
-  if (tid < jb) {
-    if (ident) { x[tid] = zero; if (tid == col) x[tid].x = 1; }
-    else x[tid] = xc[tid];
-  }
-  int s = ident ? col / SB : (UPPER ? nsb - 1 : 0);
+  if (tid < jb) x[tid] = xc[tid];
+  int s = UPPER ? nsb - 1 : 0;
   const int iters = UPPER ? s + 1 : nsb - s;
   trsm_stage<T, UPPER>(bufs, A, lda, jb, s, tid);
   cp_async_commit();
@@ -819,27 +806,127 @@ cudaError_t trsm_cols(cudaStream_t st, bool upper, const typename cx<R>::T* A, l
   auto kern = upper ? k_trsm_col<T, true> : k_trsm_col<T, false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  kern<<<ncols, kTrsmBlock, smem, st>>>(A, lda, jb, X, ldx, 0, 0, jb, 0);
+  kern<<<ncols, kTrsmBlock, smem, st>>>(A, lda, jb, X, ldx);
   return cudaGetLastError();
 }
 template cudaError_t trsm_cols<float>(cudaStream_t, bool, const float2*, long, int, float2*, long, int);
 template cudaError_t trsm_cols<double>(cudaStream_t, bool, const double2*, long, int, double2*, long, int);
 
+// ---------------------------------------------------------------------------
+// Inverses of the diagonal blocks (order <= 256) of the complex64 factors:
+// the unit-lower L_bb or the upper U_bb.  One CTA per (8 columns of the
+// inverse, block): thread r holds row r of those 8 columns in registers and
+// the block is walked in 32-wide sub-blocks (forward for L, backward for U):
+//  1. the warp holding the sub-block's rows solves with its 32 x 32 diagonal
+//     triangle (staged in shared memory; the new rows broadcast by shuffles);
+//  2. the solved rows go to shared memory and every thread below (L) or
+//     above (U) them subtracts their product with its own row segment of the
+//     triangle, all threads at once.
+// Eight columns per CTA keep the walk short (the lower inverses sit on the
+// LU's critical path, one block after each outer panel) while every CTA
+// still reads its part of the triangle once for eight columns.
+// ---------------------------------------------------------------------------
+constexpr int kInvRows = 256, kInvSub = 32, kInvW = 8;
+
+template <bool UPPER>
+__global__ void __launch_bounds__(kInvRows)
+k_trinv(const float2* __restrict__ A, long lda, int nb, int ntot, float2* __restrict__ X, long ldx) {
+  __shared__ __align__(16) float2 Ts[kInvSub][kInvSub];  // the diagonal triangle, Ts[j][i] = T(c0 + i, c0 + j)
+  __shared__ __align__(16) float2 Xs[kInvSub][kInvW];    // the sub-block's solved rows
+  const int q = blockIdx.x, b = blockIdx.y;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int jbb = min(nb, ntot - b * nb);
+  const int qc = q * kInvW;
+  if (qc >= jbb) return;
+  A += (long)b * nb * (1 + lda);
+  X += (long)b * nb * ldx;
+  const int r = tid;
+  float2 x[kInvW];
+#pragma unroll
+  for (int c = 0; c < kInvW; ++c) x[c] = make_float2(r == qc + c ? 1.f : 0.f, 0.f);
+  const int ns = (jbb + kInvSub - 1) / kInvSub, sq = qc / kInvSub;
+  for (int it = 0; it < (UPPER ? sq + 1 : ns - sq); ++it) {
+    const int s = UPPER ? sq - it : sq + it;
+    const int c0 = s * kInvSub, w = min(kInvSub, jbb - c0);
+    __syncthreads();  // the previous sub-block's Ts and Xs are no longer read
+    for (int e = tid; e < kInvSub * kInvSub; e += kInvRows) {
+      const int i = e % kInvSub, j = e / kInvSub;
+      Ts[j][i] = (i < w && j < w) ? A[(c0 + i) + (long)(c0 + j) * lda] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    if (warp == s) {
+      if (!UPPER) {
+        for (int j = 0; j < w; ++j) {
+          const float2 l = Ts[j][lane];
+          const bool upd = lane > j && lane < w;
+#pragma unroll
+          for (int c = 0; c < kInvW; ++c) {
+            const float2 xj = make_float2(__shfl_sync(0xffffffffu, x[c].x, j), __shfl_sync(0xffffffffu, x[c].y, j));
+            if (upd) x[c] = c_sub(x[c], c_mul(l, xj));
+          }
+        }
+      } else {
+        const float2 rd = (lane < w) ? c_recip(Ts[lane][lane]) : make_float2(0.f, 0.f);
+        for (int j = w - 1; j >= 0; --j) {
+          if (lane == j) {
+#pragma unroll
+            for (int c = 0; c < kInvW; ++c) x[c] = c_mul(x[c], rd);
+          }
+          const float2 u = Ts[j][lane];
+          const bool upd = lane < j;
+#pragma unroll
+          for (int c = 0; c < kInvW; ++c) {
+            const float2 xj = make_float2(__shfl_sync(0xffffffffu, x[c].x, j), __shfl_sync(0xffffffffu, x[c].y, j));
+            if (upd) x[c] = c_sub(x[c], c_mul(u, xj));
+          }
+        }
+      }
+      float4* d4 = reinterpret_cast<float4*>(&Xs[lane][0]);
+#pragma unroll
+      for (int c2 = 0; c2 < kInvW / 2; ++c2) d4[c2] = make_float4(x[2 * c2].x, x[2 * c2].y, x[2 * c2 + 1].x, x[2 * c2 + 1].y);
+    }
+    __syncthreads();
+    const bool mine = UPPER ? r < c0 : (r >= c0 + w && r < jbb);
+    if (mine) {
+      const float2* trow = A + r + (long)c0 * lda;
+#pragma unroll 8
+      for (int j = 0; j < w; ++j) {
+        const float2 t = trow[(long)j * lda];
+        const float4* xs4 = reinterpret_cast<const float4*>(&Xs[j][0]);
+#pragma unroll
+        for (int c2 = 0; c2 < kInvW / 2; ++c2) {
+          const float4 v = xs4[c2];
+          x[2 * c2].x = fmaf(-t.x, v.x, fmaf(t.y, v.y, x[2 * c2].x));
+          x[2 * c2].y = fmaf(-t.x, v.y, fmaf(-t.y, v.x, x[2 * c2].y));
+          x[2 * c2 + 1].x = fmaf(-t.x, v.z, fmaf(t.y, v.w, x[2 * c2 + 1].x));
+          x[2 * c2 + 1].y = fmaf(-t.x, v.w, fmaf(-t.y, v.z, x[2 * c2 + 1].y));
+        }
+      }
+    }
+  }
+  if (r < jbb) {
+    float2* o = X + r + (long)qc * ldx;
+#pragma unroll
+    for (int c = 0; c < kInvW; ++c)
+      if (qc + c < jbb) o[(long)c * ldx] = x[c];
+  }
+}
+
 template <typename R>
 cudaError_t trsm_inverse_blocks(cudaStream_t st, bool upper, const typename cx<R>::T* A, long lda, int n, int nb,
                                 typename cx<R>::T* X, long ldx, int nblk_first, int nblk) {
-  typedef typename cx<R>::T T;
-  if (nb > kTrsmBlock) return cudaErrorInvalidValue;
+  static_assert(sizeof(R) == 4, "the diagonal-block inverses serve the complex64 LU");
+  if (nb > kInvRows) return cudaErrorInvalidValue;
   if (nblk <= 0) return cudaSuccess;
-  const int smem = 2 * TrsmSub<T>::SB * kTrsmBlock * (int)sizeof(T);
-  auto kern = upper ? k_trsm_col<T, true> : k_trsm_col<T, false>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return e;
   const long k0 = (long)nblk_first * nb;
-  kern<<<dim3(nb, nblk), kTrsmBlock, smem, st>>>(A + k0 + k0 * lda, lda, nb, X + (long)nblk_first * nb * ldx, ldx,
-                                                 (long)nb * (1 + lda), (long)nb * ldx, n - (int)k0, 1);
+  const dim3 grid((nb + kInvW - 1) / kInvW, nblk);
+  if (upper)
+    k_trinv<true><<<grid, kInvRows, 0, st>>>(A + k0 + k0 * lda, lda, nb, n - (int)k0, X + (long)nblk_first * nb * ldx, ldx);
+  else
+    k_trinv<false><<<grid, kInvRows, 0, st>>>(A + k0 + k0 * lda, lda, nb, n - (int)k0, X + (long)nblk_first * nb * ldx, ldx);
   return cudaGetLastError();
 }
+
 template cudaError_t trsm_inverse_blocks<float>(cudaStream_t, bool, const float2*, long, int, int, float2*, long, int,
                                                 int);
 
