@@ -19,10 +19,13 @@
 //
 // A cheaper mode (exact = false) serves products whose operands carry single
 // precision anyway (the mixed form's right-hand sides, B = S W with S from the
-// single-precision fill): products a * yh in FP32, summed in FP32 within each
-// 32-deep stage, and the stage sums accumulated with TwoSum as above, so the
-// error is that of a 32-term single-precision sum (~1e-7 of sum |a||y|), not
-// of an n-term one.
+// single-precision fill, and the refinement's updated residual r - A d): products
+// a * yh in FP32, summed in FP32 within each 32-deep stage, and the stage sums
+// accumulated with TwoSum as above, so the error is that of a 32-term
+// single-precision sum (~1e-7 of sum |a||y|), not of an n-term one.  With four
+// FMAs per complex product this mode would be bound by its shared-memory reads
+// at one row per thread, so it has its own kernel (k_resid_sp): two rows per
+// thread and y's high parts only, 7 reads per 80 FMAs instead of 11 per 40.
 //
 // Tiling: 64 rows x CW = 4*CPT columns per CTA, 256 threads (64 rows x 4
 // column groups of CPT), 32-deep stages of A (complex64) and of the split y
@@ -201,6 +204,140 @@ k_resid_df(int m, int nc, int k, int kchunk, const float2* __restrict__ A, long 
   }
 }
 
+// The single-product mode: 64 rows x CW = 4*CPT columns per CTA, 128
+// threads (32 lanes x 4 column groups), each thread rows lane and lane + 32
+// of the tile and CPT columns; y's high parts as complex64 [cb][k][CW].
+constexpr int kSpThreads = 128;
+constexpr size_t kSpYTile = (size_t)kRK * kRMaxCW * sizeof(float2);  // 10 KB
+constexpr size_t kSpStage = kRATile + kSpYTile;
+constexpr size_t kSpSmem = 2 * kSpStage;
+
+__global__ void k_split_yh(int k, int nc, int cw, int ncb, const double2* __restrict__ Y, long ldy,
+                           float2* __restrict__ Ys) {
+  const long total = (long)ncb * k * cw;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const int c = (int)(e % cw);
+    const long rest = e / cw;
+    const int l = (int)(rest % k), cb = (int)(rest / k);
+    const int col = cb * cw + c;
+    float2 o = make_float2(0.f, 0.f);
+    if (col < nc) {
+      const double2 y = Y[l + (long)col * ldy];
+      o = make_float2((float)y.x, (float)y.y);
+    }
+    Ys[e] = o;
+  }
+}
+
+template <int CPT, bool VEC>
+__device__ __forceinline__ void sp_stage(float2* As, float2* Yt, const float2* __restrict__ A, long lda,
+                                         const float2* __restrict__ Ycb, int m, int m0, int k0, int kend, int tid) {
+  constexpr int CW = 4 * CPT;
+  if (VEC) {
+#pragma unroll
+    for (int it = 0; it < kRK * kRRows / 2 / kSpThreads; ++it) {
+      const int e = tid + it * kSpThreads;
+      const int i = (e % (kRRows / 2)) * 2, l = e / (kRRows / 2);
+      const int gm = m0 + i, gk = k0 + l;
+      int bytes = 0;
+      if (gk < kend) bytes = (gm + 1 < m) ? 16 : (gm < m ? 8 : 0);
+      cp_async16(As + l * kRRows + i, bytes ? A + gm + (long)gk * lda : A, bytes);
+    }
+  } else {
+#pragma unroll
+    for (int it = 0; it < kRK * kRRows / kSpThreads; ++it) {
+      const int e = tid + it * kSpThreads;
+      const int i = e % kRRows, l = e / kRRows;
+      const int gm = m0 + i, gk = k0 + l;
+      const bool ok = gm < m && gk < kend;
+      cp_async8(As + l * kRRows + i, ok ? A + gm + (long)gk * lda : A, ok);
+    }
+  }
+  // CW complex per k row: CW / 2 16-byte pieces
+  for (int e = tid; e < kRK * CW / 2; e += kSpThreads) {
+    const int l = e / (CW / 2), c2 = e % (CW / 2);
+    const int gk = k0 + l;
+    const bool ok = gk < kend;
+    cp_async16(Yt + l * CW + 2 * c2, ok ? Ycb + (long)gk * CW + 2 * c2 : Ycb, ok ? 16 : 0);
+  }
+}
+
+template <int CPT, bool VEC>
+__global__ void __launch_bounds__(kSpThreads, 3)
+k_resid_sp(int m, int nc, int k, int kchunk, const float2* __restrict__ A, long lda, const float2* __restrict__ Ys,
+           double2* __restrict__ part) {
+  constexpr int CW = 4 * CPT;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int tid = threadIdx.x, lane = tid & 31, cg = tid >> 5;
+  const int m0 = blockIdx.x * kRRows, cb = blockIdx.y, z = blockIdx.z;
+  const int kbeg = z * kchunk, kend = min(k, kbeg + kchunk);
+  const float2* Ycb = Ys + (size_t)cb * k * CW;
+  float Sr[2][CPT], sr[2][CPT], Si[2][CPT], si[2][CPT];
+#pragma unroll
+  for (int h = 0; h < 2; ++h)
+#pragma unroll
+    for (int j = 0; j < CPT; ++j) { Sr[h][j] = 0.f; sr[h][j] = 0.f; Si[h][j] = 0.f; si[h][j] = 0.f; }
+  const int nst = (kend - kbeg + kRK - 1) / kRK;
+  if (nst > 0)
+    sp_stage<CPT, VEC>(reinterpret_cast<float2*>(smem), reinterpret_cast<float2*>(smem + kRATile), A, lda, Ycb, m, m0,
+                       kbeg, kend, tid);
+  cp_async_commit();
+  for (int s = 0; s < nst; ++s) {
+    unsigned char* cur = smem + (s & 1) * kSpStage;
+    if (s + 1 < nst) {
+      unsigned char* nxt = smem + ((s + 1) & 1) * kSpStage;
+      sp_stage<CPT, VEC>(reinterpret_cast<float2*>(nxt), reinterpret_cast<float2*>(nxt + kRATile), A, lda, Ycb, m, m0,
+                         kbeg + (s + 1) * kRK, kend, tid);
+    }
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    const float2* as = reinterpret_cast<const float2*>(cur);
+    const float4* yt = reinterpret_cast<const float4*>(cur + kRATile);
+    float pr[2][CPT], pi[2][CPT];
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+      for (int j = 0; j < CPT; ++j) { pr[h][j] = 0.f; pi[h][j] = 0.f; }
+#pragma unroll 2
+    for (int l = 0; l < kRK; ++l) {
+      const float2 a0 = as[l * kRRows + lane], a1 = as[l * kRRows + lane + 32];
+#pragma unroll
+      for (int j2 = 0; j2 < CPT / 2; ++j2) {
+        const float4 y = yt[(l * CW + cg * CPT) / 2 + j2];  // (yh_re, yh_im) of two columns
+        pr[0][2 * j2] = fmaf(-a0.y, y.y, fmaf(a0.x, y.x, pr[0][2 * j2]));
+        pi[0][2 * j2] = fmaf(a0.y, y.x, fmaf(a0.x, y.y, pi[0][2 * j2]));
+        pr[0][2 * j2 + 1] = fmaf(-a0.y, y.w, fmaf(a0.x, y.z, pr[0][2 * j2 + 1]));
+        pi[0][2 * j2 + 1] = fmaf(a0.y, y.z, fmaf(a0.x, y.w, pi[0][2 * j2 + 1]));
+        pr[1][2 * j2] = fmaf(-a1.y, y.y, fmaf(a1.x, y.x, pr[1][2 * j2]));
+        pi[1][2 * j2] = fmaf(a1.y, y.x, fmaf(a1.x, y.y, pi[1][2 * j2]));
+        pr[1][2 * j2 + 1] = fmaf(-a1.y, y.w, fmaf(a1.x, y.z, pr[1][2 * j2 + 1]));
+        pi[1][2 * j2 + 1] = fmaf(a1.y, y.z, fmaf(a1.x, y.w, pi[1][2 * j2 + 1]));
+      }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+      for (int j = 0; j < CPT; ++j) {
+        two_sum_acc(Sr[h][j], sr[h][j], pr[h][j]);
+        two_sum_acc(Si[h][j], si[h][j], pi[h][j]);
+      }
+    __syncthreads();
+  }
+  double2* pz = part + (size_t)z * m * nc;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int row = m0 + lane + 32 * h;
+    if (row >= m) continue;
+#pragma unroll
+    for (int j = 0; j < CPT; ++j) {
+      const int col = cb * CW + cg * CPT + j;
+      if (col < nc)
+        pz[row + (size_t)col * m] = make_double2((double)Sr[h][j] + (double)sr[h][j], (double)Si[h][j] + (double)si[h][j]);
+    }
+  }
+}
+
 __global__ void k_resid_reduce(int m, int nc, int slices, const double2* __restrict__ part,
                                const double2* __restrict__ Bin, long ldb, double sign, double2* __restrict__ out,
                                long ldo) {
@@ -267,6 +404,39 @@ cudaError_t launch_resid(cudaStream_t st, int m, int nc, int k, const float2* A,
   return cudaGetLastError();
 }
 
+template <int CPT, bool VEC>
+cudaError_t launch_sp(cudaStream_t st, int m, int nc, int k, const float2* A, long lda, const double2* Y, long ldy,
+                      const double2* Bin, long ldb, double sign, double2* out, long ldo, void* ws, size_t ws_bytes) {
+  constexpr int CW = 4 * CPT;
+  const int ncb = (nc + CW - 1) / CW;
+  const int gx = (m + kRRows - 1) / kRRows;
+  const size_t ys_bytes = align256((size_t)ncb * k * CW * sizeof(float4));  // the exact mode's layout size
+  // slices of the inner dimension as in launch_resid, for three CTAs per SM
+  const int kmax = min(kRMaxSlices, (k + kRK - 1) / kRK);
+  int slices = max(1, min((3 * 152 + gx * ncb - 1) / (gx * ncb), kmax));
+  {
+    double best = 0.0;
+    for (int s = slices; s <= kmax; ++s) {
+      const long ctas = (long)gx * ncb * s;
+      const double fill = (double)ctas / (double)(((ctas + 455) / 456) * 456);
+      if (fill > best + 1e-9) { best = fill; slices = s; }
+    }
+  }
+  while (slices > 1 && ys_bytes + (size_t)slices * m * nc * sizeof(double2) > ws_bytes) --slices;
+  if (ys_bytes + (size_t)slices * m * nc * sizeof(double2) > ws_bytes) return cudaErrorInvalidValue;
+  int kchunk = ((k + slices - 1) / slices + kRK - 1) / kRK * kRK;
+  slices = (k + kchunk - 1) / kchunk;
+  float2* Ys = static_cast<float2*>(ws);
+  double2* part = reinterpret_cast<double2*>(static_cast<unsigned char*>(ws) + ys_bytes);
+  k_split_yh<<<4 * 152, 256, 0, st>>>(k, nc, CW, ncb, Y, ldy, Ys);
+  auto kern = k_resid_sp<CPT, VEC>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSpSmem);
+  if (e != cudaSuccess) return e;
+  kern<<<dim3(gx, ncb, slices), kSpThreads, kSpSmem, st>>>(m, nc, k, kchunk, A, lda, Ys, part);
+  k_resid_reduce<<<dim3((m + 255) / 256, nc), 256, 0, st>>>(m, nc, slices, part, Bin, ldb, sign, out, ldo);
+  return cudaGetLastError();
+}
+
 template <int CPT>
 cudaError_t dispatch(cudaStream_t st, bool transa, bool vec, bool exact, int m, int nc, int k, const float2* A,
                      long lda, const double2* Y, long ldy, const double2* Bin, long ldb, double sign, double2* out,
@@ -275,8 +445,8 @@ cudaError_t dispatch(cudaStream_t st, bool transa, bool vec, bool exact, int m, 
   return launch_resid<CPT, TA, V, EX>(st, m, nc, k, A, lda, Y, ldy, Bin, ldb, sign, out, ldo, ws, ws_bytes)
   if (!exact) {
     if (transa) return cudaErrorNotSupported;
-    if (vec) HG_RES(false, true, false);
-    HG_RES(false, false, false);
+    if (vec) return launch_sp<CPT, true>(st, m, nc, k, A, lda, Y, ldy, Bin, ldb, sign, out, ldo, ws, ws_bytes);
+    return launch_sp<CPT, false>(st, m, nc, k, A, lda, Y, ldy, Bin, ldb, sign, out, ldo, ws, ws_bytes);
   }
   if (transa) HG_RES(true, false, true);
   if (vec) HG_RES(false, true, true);
