@@ -343,7 +343,7 @@ def ours(args, dist, rank, world, local):
     # ---- roofline of the dominant kernel (the LU trailing-update GEMM) ----
     roof = None
     if rank == 0 and args.solver == "lu":
-        roof = _roofline(s, mesh.n, prec, hg, ms_max / args.steps)
+        roof = _roofline(s, mesh.n, prec, hg, ms_max / args.steps, lu_tensor=args.lu_tensor)
     # ---- the CPU oracle on one frequency (the CPU baseline sample), and both GPU forms against it ----
     cpu, vs_oracle = None, None
     if rank == 0 and not args.no_cpu_baseline:
@@ -620,7 +620,7 @@ def _launch_count(n, prec, sweeps=1, nd=30, nbeta=8):
 F_PAIR_MEAN = 590.0
 
 
-def _roofline(s, n, prec, hg, ms_per_step, nd=30, nbeta=8):
+def _roofline(s, n, prec, hg, ms_per_step, nd=30, nbeta=8, lu_tensor=2):
     """Roofline of the dominant kernel, the 32-column complex64 LU panel
     (k_getf2_cluster_reg: 52 % of one solve's kernel time in the ncu launch
     list), timed with CUDA events on the library's stream at the height of the
@@ -649,7 +649,7 @@ def _roofline(s, n, prec, hg, ms_per_step, nd=30, nbeta=8):
                            "7 solves in flight hide it behind other solves' fills and tensor-core updates"}
         except Exception:
             out = None
-    gemm = _gemm_roofline(s, n, prec, hg)
+    gemm = _gemm_roofline(s, n, prec, hg, lu_tensor)
     flops = 8.0 / 3.0 * n ** 3 + 8.0 * n * n * (nd + nbeta) + F_PAIR_MEAN * n * n
     tf = flops / (ms_per_step / 1e3) / 1e12
     whole = {"flops_per_step": flops, "achieved_tflops": tf, "peak_tflops": peaks.get("bf16_tflops", 1900.0),
@@ -666,13 +666,15 @@ def _roofline(s, n, prec, hg, ms_per_step, nd=30, nbeta=8):
     return out
 
 
-def _gemm_roofline(s, n, prec, hg):
+def _gemm_roofline(s, n, prec, hg, lu_tensor=2):
     """Roofline of the LU trailing update, the path's dense contraction: the
-    library's tcgen05 GEMM (mixed form, split TF32) or its complex128 SIMT
-    GEMM (FP64 form), timed with CUDA events on the library's stream at the
-    shape of the first 256-wide outer panel (m = n = N - 256, k = 256)."""
+    library's tcgen05 GEMM (mixed form, the variant lu_tensor selects) or its
+    complex128 SIMT GEMM (FP64 form), timed with CUDA events on the library's
+    stream at the shape of the first 256-wide outer panel (m = n = N - 256,
+    k = 256)."""
     m, k = n - 256, 256
-    variant = 2 if prec == hg.HG_PREC_MIXED else 0
+    # hg_bench_gemm variants: 2 split TF32, 3 TF32, 4 split BF16
+    variant = {3: 2, 1: 3, 2: 4}.get(lu_tensor, 1) if prec == hg.HG_PREC_MIXED else 0
     try:
         ms = s.bench_gemm(variant, m, m, k, iters=10)
     except Exception:
@@ -681,11 +683,18 @@ def _gemm_roofline(s, n, prec, hg):
     achieved = flops / (ms / 1e3) / 1e12
     peaks, kind = _peaks()
     peak = peaks.get("bf16_tflops", 1900.0)
-    out = {"kernel": "k_cgemm_tc<3> (LU trailing update A22 -= L21 U12, complex64, tcgen05 split TF32)"
-           if variant == 2 else "k_gemm<double> (LU trailing update, complex128 SIMT)",
+    names = {2: "k_cgemm_tc<3> (LU trailing update A22 -= L21 U12, complex64, tcgen05 split TF32)",
+             3: "k_cgemm_tc<1> (LU trailing update A22 -= L21 U12, complex64, tcgen05 TF32)",
+             4: "k_cgemm_tc<2> (LU trailing update A22 -= L21 U12, complex64, tcgen05 split BF16)",
+             1: "k_cgemm_wide (LU trailing update, complex64 SIMT)",
+             0: "k_gemm<double> (LU trailing update, complex128 SIMT)"}
+    out = {"kernel": names[variant],
            "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
            "peak_source": f"bf16_tflops of {kind} peaks", "flops_per_launch": flops, "ms_per_launch": ms,
            "traffic": None}
+    if variant == 4:
+        out["note"] = ("algorithmic complex flops; the hardware does 3 BF16 products per real product at the bf16 "
+                       "rate, so the tensor-pipe utilisation is about 3 x frac")
     if variant == 2:
         # DRAM bytes of one launch of this shape (5792 x 5792 x 256) from the committed ncu capture
         out["traffic"] = (486.998528 + 235.5008) * 1e6 if n == 6048 else None
@@ -708,8 +717,8 @@ def main():
                     help="frequency-solves in flight (hg_solve_sweep slots); 0: at most 8, balanced over the steps")
     ap.add_argument("--refine", default="classical", choices=["classical", "gmres"],
                     help="mixed-form refinement: classical iterative refinement or GMRES-IR")
-    ap.add_argument("--lu-tensor", type=int, default=3, choices=[0, 1, 3],
-                    help="LU trailing updates: 3 split-TF32 tensor cores, 1 TF32, 0 FP32 SIMT")
+    ap.add_argument("--lu-tensor", type=int, default=2, choices=[0, 1, 2, 3],
+                    help="LU trailing updates: 2 split-BF16 tensor cores, 3 split-TF32, 1 TF32, 0 FP32 SIMT")
     ap.add_argument("--solver", default="lu", choices=["lu", "gmres"],
                     help="array workload: linear solver (gmres = the reference's Solver_type 2)")
     ap.add_argument("--workload", default="array", choices=["array", "batch", "serve", "three", "field"],

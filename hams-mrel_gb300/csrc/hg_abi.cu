@@ -131,6 +131,7 @@ struct hg_ctx {
   std::vector<hg_ctx*> slots;
   unsigned mesh_gen = 0;   // counts hg_set_mesh calls on this context
   unsigned slot_gen = ~0u;  // a slot: the parent's mesh_gen of the mesh it holds
+  int lu_used = 0;  // tensor variant (hg_opts.lu_tensor) of the current complex64 factorisation
   // pinned staging of the potentials read back to the caller's (pageable) arrays
   double2* pin_out = nullptr;
   size_t pin_cap = 0;
@@ -721,9 +722,44 @@ int solve_iter(hg_ctx* c, int c0, int c1) {
   return 0;
 }
 
+// Factor the mixed form's complex64 matrix again with split-TF32 updates,
+// from the unfactored copy (irsp = 0) or from A^T A formed anew (irsp = 1).
+int refactor_split_tf32(hg_ctx* c) {
+  const int n = c->n, tn = c->tn;
+  const size_t lwb = hg::lu_work_bytes(n, 3);
+  if (lwb) CK(c->luws.ensure(lwb));
+  if (c->irsp == 1) {
+    CK(hg::gemm<float>(c->st, true, n, n, tn, make_float2(1, 0), c->Af.p, tn, c->Af.p, tn, make_float2(0, 0), c->Cf.p,
+                       n));
+    CK(hg::getrf<float>(c->st, n, c->Cf.p, n, c->ipiv.p, c->info.p, c->luws.p, lwb, 3));
+  } else {
+    CK(cudaMemcpyAsync(c->Af.p, c->Aof.p, (size_t)tn * n * sizeof(float2), cudaMemcpyDeviceToDevice, c->st));
+    CK(hg::getrf<float>(c->st, n, c->Af.p, tn, c->ipiv.p, c->info.p, c->luws.p, lwb, 3));
+  }
+  int info = 0;
+  CK(cudaMemcpyAsync(&info, c->info.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (info < 0) return fail(c, HG_ERR_DEVICE, "LU panel: a bounded cluster wait ran out (info %d)", info);
+  if (info != 0) return fail(c, info, "zero pivot at row %d", info);
+  c->lu_used = 3;
+  return 0;
+}
+
+int solve_cols_once(hg_ctx* c, int c0, int c1);
+
 // Solve M X[:, c0:c1] = rhs for the current factorisation.  rhs is B (tn
 // rows) for irsp = 0, or the normal-equation right-hand side A^T B for irsp = 1.
+// Split-BF16 factors whose refinement stops short of the tolerance (an
+// ill-conditioned matrix) are replaced once by split-TF32 ones.
 int solve_cols(hg_ctx* c, int c0, int c1) {
+  int r = solve_cols_once(c, c0, c1);
+  if (r || !mixed(c) || c->o.solver == 2 || c->lu_used != 2 || c->resid <= c->o.refine_tol) return r;
+  r = refactor_split_tf32(c);
+  if (r) return r;
+  return solve_cols_once(c, c0, c1);
+}
+
+int solve_cols_once(hg_ctx* c, int c0, int c1) {
   const int n = c->n, tn = c->tn, nc = c1 - c0;
   if (nc <= 0) return 0;
   if (c->o.solver == 2) return solve_iter(c, c0, c1);
@@ -878,7 +914,7 @@ void hg_default_opts(hg_opts* o) {
   o->fin_table = -1;
   o->rho = 1000.0;
   o->g = 9.80665;
-  o->lu_tensor = 3;
+  o->lu_tensor = 2;
   o->solver = 1;
 }
 
@@ -891,7 +927,7 @@ int hg_create(hg_ctx** out, const hg_opts* opts) {
   if (opts) c->o = *opts;
   if (c->o.precision != HG_PREC_FP64 && c->o.precision != HG_PREC_MIXED) { delete c; return -2; }
   if (c->o.grn_kind != 4 && c->o.grn_kind != 8) { delete c; return -2; }
-  if (c->o.lu_tensor != 0 && c->o.lu_tensor != 1 && c->o.lu_tensor != 3) { delete c; return -2; }
+  if (c->o.lu_tensor < 0 || c->o.lu_tensor > 3) { delete c; return -2; }
   if (c->o.refine_method != 0 && c->o.refine_method != 1) { delete c; return -2; }
   if (c->o.fin_table < -1 || c->o.fin_table > 1) { delete c; return -2; }
   if (c->o.solver != 1 && c->o.solver != 2) { delete c; return -2; }
@@ -1232,6 +1268,7 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
     } else {
       CK(hg::getrf<float>(c->st, n, c->Af.p, tn, c->ipiv.p, c->info.p, c->luws.p, lwb, c->o.lu_tensor));
     }
+    c->lu_used = c->o.lu_tensor;
   }
   CK(cudaEventRecord(c->ev[2], c->st));
   int info = 0;
@@ -1659,54 +1696,61 @@ int hg_gesv(hg_ctx* c, int precision, int n, int nrhs, double* a, int lda, int* 
     CK(dR.ensure(nb));
     CK(ws.ensure((size_t)16 * nb));
     CK(norms.ensure(2 * (size_t)(nrhs > 0 ? nrhs : 1)));
-    CK(hg::convert_z2c(c->st, (long)nn, dA.p, dAf.p));
-    const size_t lwb = hg::lu_work_bytes(n, c->o.lu_tensor);
-    if (lwb) CK(luws.ensure(lwb));
-    CK(hg::getrf<float>(c->st, n, dAf.p, n, dpiv.p, dinfo.p, luws.p, lwb, c->o.lu_tensor));
-    const bool inv = hg::lu_has_inverses(n, c->o.lu_tensor, luws.cap);
-    auto lu_solve = [&](float2* rhs) -> cudaError_t {
-      if (inv) return hg::getrs_inv(c->st, n, nrhs, dAf.p, n, dpiv.p, rhs, n, luws.p);
-      return hg::getrs<float>(c->st, n, nrhs, dAf.p, n, dpiv.p, rhs, n);
-    };
-    CK(cudaMemcpyAsync(&inf, dinfo.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
-    CK(cudaStreamSynchronize(c->st));
-    if (inf < 0) return fail(c, HG_ERR_DEVICE, "LU panel: a bounded cluster wait ran out (info %d)", inf);
-    if (inf != 0) {
-      // a zero pivot in complex64: fall back to the complex128 factorisation
-      fp64 = true;
-      it = -31;
-    } else if (nrhs > 0) {
-      std::vector<double> bn(nrhs), rn(nrhs);
-      k_colmax<<<nrhs, 256, 0, c->st>>>(n, dB.p, n, norms.p);
-      CK(cudaMemcpyAsync(bn.data(), norms.p, nrhs * sizeof(double), cudaMemcpyDeviceToHost, c->st));
-      CK(hg::convert_z2c(c->st, (long)nb, dB.p, dBf.p));
-      CK(lu_solve(dBf.p));
-      CK(hg::convert_c2z(c->st, (long)nb, dBf.p, dX.p));
-      bool ok = false;
-      for (int sweep = 0;; ++sweep) {
-        CK(cudaMemcpyAsync(dR.p, dB.p, nb * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
-        CK(hg::gemm<double>(c->st, false, n, nrhs, n, mone, dA.p, n, dX.p, n, one, dR.p, n, (void*)ws.p,
-                            ws.cap * sizeof(double2)));
-        k_colmax<<<nrhs, 256, 0, c->st>>>(n, dR.p, n, norms.p + nrhs);
-        CK(cudaMemcpyAsync(rn.data(), norms.p + nrhs, nrhs * sizeof(double), cudaMemcpyDeviceToHost, c->st));
-        CK(cudaStreamSynchronize(c->st));
-        double worst = 0.0;
-        for (int k = 0; k < nrhs; ++k) worst = std::fmax(worst, bn[k] > 0 ? rn[k] / bn[k] : rn[k]);
-        if (worst <= c->o.refine_tol) { ok = true; it = sweep; break; }
-        if (sweep >= c->o.max_refine) break;
-        CK(hg::convert_z2c(c->st, (long)nb, dR.p, dBf.p));
-        CK(lu_solve(dBf.p));
-        CK(hg::add_c2z_2d(c->st, n, nrhs, dBf.p, n, dX.p, n));
-      }
-      if (ok) {
-        result = dX.p;
-        CK(hg::convert_c2z(c->st, (long)nn, dAf.p, dA.p));
-      } else {
+    // split-BF16 factors that do not refine (an ill-conditioned matrix) are
+    // redone once with split-TF32 updates before the complex128 fallback
+    for (int tcv = c->o.lu_tensor;; tcv = 3) {
+      CK(hg::convert_z2c(c->st, (long)nn, dA.p, dAf.p));
+      const size_t lwb = hg::lu_work_bytes(n, tcv);
+      if (lwb) CK(luws.ensure(lwb));
+      CK(hg::getrf<float>(c->st, n, dAf.p, n, dpiv.p, dinfo.p, luws.p, lwb, tcv));
+      const bool inv = hg::lu_has_inverses(n, tcv, luws.cap);
+      auto lu_solve = [&](float2* rhs) -> cudaError_t {
+        if (inv) return hg::getrs_inv(c->st, n, nrhs, dAf.p, n, dpiv.p, rhs, n, luws.p);
+        return hg::getrs<float>(c->st, n, nrhs, dAf.p, n, dpiv.p, rhs, n);
+      };
+      CK(cudaMemcpyAsync(&inf, dinfo.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+      if (inf < 0) return fail(c, HG_ERR_DEVICE, "LU panel: a bounded cluster wait ran out (info %d)", inf);
+      if (inf != 0) {
+        // a zero pivot in complex64: fall back to the complex128 factorisation
         fp64 = true;
         it = -31;
+      } else if (nrhs > 0) {
+        std::vector<double> bn(nrhs), rn(nrhs);
+        k_colmax<<<nrhs, 256, 0, c->st>>>(n, dB.p, n, norms.p);
+        CK(cudaMemcpyAsync(bn.data(), norms.p, nrhs * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+        CK(hg::convert_z2c(c->st, (long)nb, dB.p, dBf.p));
+        CK(lu_solve(dBf.p));
+        CK(hg::convert_c2z(c->st, (long)nb, dBf.p, dX.p));
+        bool ok = false;
+        for (int sweep = 0;; ++sweep) {
+          CK(cudaMemcpyAsync(dR.p, dB.p, nb * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
+          CK(hg::gemm<double>(c->st, false, n, nrhs, n, mone, dA.p, n, dX.p, n, one, dR.p, n, (void*)ws.p,
+                              ws.cap * sizeof(double2)));
+          k_colmax<<<nrhs, 256, 0, c->st>>>(n, dR.p, n, norms.p + nrhs);
+          CK(cudaMemcpyAsync(rn.data(), norms.p + nrhs, nrhs * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+          CK(cudaStreamSynchronize(c->st));
+          double worst = 0.0;
+          for (int k = 0; k < nrhs; ++k) worst = std::fmax(worst, bn[k] > 0 ? rn[k] / bn[k] : rn[k]);
+          if (worst <= c->o.refine_tol) { ok = true; it = sweep; break; }
+          if (sweep >= c->o.max_refine) break;
+          CK(hg::convert_z2c(c->st, (long)nb, dR.p, dBf.p));
+          CK(lu_solve(dBf.p));
+          CK(hg::add_c2z_2d(c->st, n, nrhs, dBf.p, n, dX.p, n));
+        }
+        if (ok) {
+          result = dX.p;
+          CK(hg::convert_c2z(c->st, (long)nn, dAf.p, dA.p));
+        } else if (tcv == 2) {
+          continue;
+        } else {
+          fp64 = true;
+          it = -31;
+        }
+      } else {
+        CK(hg::convert_c2z(c->st, (long)nn, dAf.p, dA.p));
       }
-    } else {
-      CK(hg::convert_c2z(c->st, (long)nn, dAf.p, dA.p));
+      break;
     }
   }
   if (fp64) {
@@ -1746,8 +1790,9 @@ cudaError_t gemm_variant(hg_ctx* c, int variant, int m, int n, int k, void* a, i
                              make_float2(1, 0), (float2*)cc, ldc);
     case 2:
     case 3:
-      return hg::cgemm_tc(c->st, variant == 2 ? 3 : 1, m, n, k, (float2*)a, lda, (float2*)b, ldb, (float2*)cc, ldc, ws,
-                          ws_bytes, status);
+    case 4:
+      return hg::cgemm_tc(c->st, variant == 2 ? 3 : (variant == 3 ? 1 : 2), m, n, k, (float2*)a, lda, (float2*)b, ldb,
+                          (float2*)cc, ldc, ws, ws_bytes, status);
   }
   return cudaErrorInvalidValue;
 }
@@ -1756,7 +1801,7 @@ cudaError_t gemm_variant(hg_ctx* c, int variant, int m, int n, int k, void* a, i
 
 int hg_bench_gemm(hg_ctx* c, int precision, int m, int n, int k, int iters, float* ms_per_launch) {
   if (!c) return -1;
-  if (precision < 0 || precision > 3) return fail(c, -2, "precision must be 0..3");
+  if (precision < 0 || precision > 4) return fail(c, -2, "precision must be 0..4");
   if ((precision >= 2) && !hg::cgemm_tc_supported()) return fail(c, -2, "tensor-core GEMM needs an sm_103 device");
   if (m <= 0 || n <= 0 || k <= 0) return fail(c, -3, "bad shape");
   if (iters <= 0) return fail(c, -6, "iters must be positive");
@@ -1853,7 +1898,7 @@ int hg_bench_panel(hg_ctx* c, int m, int iters, float* ms_per_launch) {
 int hg_gemm_check(hg_ctx* c, int variant, int m, int n, int k, const double* a, int lda, const double* b, int ldb,
                   double* cm, int ldc) {
   if (!c) return -1;
-  if (variant < 0 || variant > 3) return fail(c, -2, "variant must be 0..3");
+  if (variant < 0 || variant > 4) return fail(c, -2, "variant must be 0..4");
   if (variant >= 2 && !hg::cgemm_tc_supported()) return fail(c, -2, "tensor-core GEMM needs an sm_103 device");
   if (m <= 0 || n <= 0 || k <= 0) return fail(c, -3, "bad shape");
   if (!a || lda < m) return fail(c, -6, "bad a / lda");

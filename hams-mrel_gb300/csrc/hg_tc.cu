@@ -21,6 +21,11 @@
 //               k = 256 (the FP32 SIMT kernel 1e-6), enough for one
 //               refinement sweep of the mixed-form solve.
 //   passes = 1: C -= A_hi B_hi (TF32 products, measured 1e-3 of |C|).
+//   passes = 2: the three products of passes = 3 with BF16 parts
+//               (kind::f16, twice the TF32 rate): hi = rn_bf16(x),
+//               lo = rn_bf16(x - hi) keep 16 of x's 24 bits, so the products
+//               carry ~2^-16 relative error, of the order of the FP32
+//               accumulation's own; 64 real K per 128-byte stage row.
 //
 // Kernel: persistent, one CTA per SM, 192 threads in three roles:
 //   warp 0 (one thread)  TMA producer: per stage one 2-D tensor copy per
@@ -41,6 +46,7 @@
 #include <mutex>
 #include <cuda.h>
 #include <cudaTypedefs.h>
+#include <cuda_bf16.h>
 
 #include "hg_common.cuh"
 #include "hg_linalg.cuh"
@@ -63,11 +69,20 @@ template <int P> struct TcCfg;
 template <> struct TcCfg<3> {
   static constexpr int kStages = 2;
   static constexpr uint32_t kStageBytes = 2 * (kATile + kBTile);  // A_hi B_hi A_lo B_lo
+  static constexpr int kEB = 4;                                    // bytes per packed element
+};
+template <> struct TcCfg<2> {
+  static constexpr int kStages = 2;
+  static constexpr uint32_t kStageBytes = 2 * (kATile + kBTile);
+  static constexpr int kEB = 2;
 };
 template <> struct TcCfg<1> {
   static constexpr int kStages = 4;
   static constexpr uint32_t kStageBytes = kATile + kBTile;
+  static constexpr int kEB = 4;
 };
+// real K per stage: one 128-byte swizzle row of packed elements
+template <int P> constexpr int tc_kstage() { return 128 / TcCfg<P>::kEB; }
 template <int P> constexpr size_t tc_smem_bytes() {
   return (size_t)TcCfg<P>::kStages * TcCfg<P>::kStageBytes + 1024;  // + slack for 1024-byte alignment
 }
@@ -77,6 +92,9 @@ template <int P> constexpr size_t tc_smem_bytes() {
 // bits 17-22, M >> 4 at bits 24-28.
 constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kTN >> 3) << 17) |
                             ((uint32_t)(kTM >> 4) << 24);
+// kind::f16 with A and B both BF16 (bits 7-9, 10-12 = 1), F32 accumulator.
+constexpr uint32_t kIdescBf16 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTN >> 3) << 17) |
+                                ((uint32_t)(kTM >> 4) << 24);
 
 // Shared-memory matrix descriptor, K-major with 128-byte swizzle: start
 // address >> 4 (bits 0-13), leading offset unused for this layout (1),
@@ -91,12 +109,20 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 
+template <bool BF>
 __device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accum) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accum)
-      : "memory");
+  if (BF)
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(kIdescBf16), "r"(accum)
+        : "memory");
+  else
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accum)
+        : "memory");
 }
 
 // Arrive on bar once every tcgen05 operation this thread issued so far has completed.
@@ -197,11 +223,12 @@ k_cgemm_tc(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CU
           if (!tc_wait(&empty[s], ph ^ 1, &s_abort)) { ok = false; break; }
           unsigned char* st = smem + (size_t)s * SB;
           mbar_expect_tx(&full[s], SB);
-          tma_load_2d(st, &ta_hi, kt * kTK, ym, &full[s]);
-          tma_load_2d(st + kATile, &tb_hi, kt * kTK, yn, &full[s]);
-          if (P == 3) {
-            tma_load_2d(st + kATile + kBTile, &ta_lo, kt * kTK, ym, &full[s]);
-            tma_load_2d(st + 2 * kATile + kBTile, &tb_lo, kt * kTK, yn, &full[s]);
+          const int kx = kt * tc_kstage<P>();
+          tma_load_2d(st, &ta_hi, kx, ym, &full[s]);
+          tma_load_2d(st + kATile, &tb_hi, kx, yn, &full[s]);
+          if (P != 1) {
+            tma_load_2d(st + kATile + kBTile, &ta_lo, kx, ym, &full[s]);
+            tma_load_2d(st + 2 * kATile + kBTile, &tb_lo, kx, yn, &full[s]);
           }
           issued[s] = 1;
           last_ph[s] = ph;
@@ -235,15 +262,16 @@ k_cgemm_tc(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CU
           tc_fence_after();
           const uint32_t a_hi = smem_addr(smem + (size_t)s * SB), b_hi = a_hi + kATile;
           const uint32_t a_lo = b_hi + kBTile, b_lo = a_lo + kATile;
+          constexpr bool BF = (P == 2);
 #pragma unroll
-          for (int kk = 0; kk < kTK / 8; ++kk) {
-            const uint32_t off = kk * 32;  // 8 tf32 = 32 bytes along K inside the swizzle row
-            if (P == 3) {
-              tc_mma(d, sw128_desc(a_lo + off), sw128_desc(b_hi + off), (kt | kk) != 0);
-              tc_mma(d, sw128_desc(a_hi + off), sw128_desc(b_lo + off), 1u);
-              tc_mma(d, sw128_desc(a_hi + off), sw128_desc(b_hi + off), 1u);
+          for (int kk = 0; kk < 4; ++kk) {
+            const uint32_t off = kk * 32;  // one instruction's K (8 tf32 or 16 bf16) = 32 bytes of the swizzle row
+            if (P != 1) {
+              tc_mma<BF>(d, sw128_desc(a_lo + off), sw128_desc(b_hi + off), (kt | kk) != 0);
+              tc_mma<BF>(d, sw128_desc(a_hi + off), sw128_desc(b_lo + off), 1u);
+              tc_mma<BF>(d, sw128_desc(a_hi + off), sw128_desc(b_hi + off), 1u);
             } else {
-              tc_mma(d, sw128_desc(a_hi + off), sw128_desc(b_hi + off), (kt | kk) != 0);
+              tc_mma<BF>(d, sw128_desc(a_hi + off), sw128_desc(b_hi + off), (kt | kk) != 0);
             }
           }
           tc_commit(&empty[s]);
@@ -305,17 +333,28 @@ __device__ __forceinline__ float tf32_rna(float x) {
 }
 
 template <int P>
-__device__ __forceinline__ void split_store(float* hi, float* lo, long off, float x0, float x1) {
+__device__ __forceinline__ void split_store(void* hi, void* lo, long off, float x0, float x1) {
+  if (P == 2) {
+    const __nv_bfloat16 h0 = __float2bfloat16_rn(x0), h1 = __float2bfloat16_rn(x1);
+    __nv_bfloat162 hv, lv;
+    hv.x = h0; hv.y = h1;
+    lv.x = __float2bfloat16_rn(x0 - __bfloat162float(h0));
+    lv.y = __float2bfloat16_rn(x1 - __bfloat162float(h1));
+    *reinterpret_cast<__nv_bfloat162*>(static_cast<__nv_bfloat16*>(hi) + off) = hv;
+    *reinterpret_cast<__nv_bfloat162*>(static_cast<__nv_bfloat16*>(lo) + off) = lv;
+    return;
+  }
   const float h0 = tf32_rna(x0), h1 = tf32_rna(x1);
-  *reinterpret_cast<float2*>(hi + off) = make_float2(h0, h1);
-  if (P == 3) *reinterpret_cast<float2*>(lo + off) = make_float2(tf32_rna(x0 - h0), tf32_rna(x1 - h1));
+  *reinterpret_cast<float2*>(static_cast<float*>(hi) + off) = make_float2(h0, h1);
+  if (P == 3)
+    *reinterpret_cast<float2*>(static_cast<float*>(lo) + off) = make_float2(tf32_rna(x0 - h0), tf32_rna(x1 - h1));
 }
 
 // A (m x k complex, column-major) -> A_r hi/lo (2m rows x kr floats, row-major),
 // through a 32 x 32 shared-memory transpose so that both sides are coalesced.
 template <int P>
-__global__ void k_pack_a(int m, int k, int kr, const float2* __restrict__ A, long lda, float* __restrict__ hi,
-                         float* __restrict__ lo) {
+__global__ void k_pack_a(int m, int k, int kr, const float2* __restrict__ A, long lda, void* __restrict__ hi,
+                         void* __restrict__ lo) {
   __shared__ float2 t[32][33];
   const int i0 = blockIdx.x * 32, p0 = blockIdx.y * 32, tx = threadIdx.x, ty = threadIdx.y;
   for (int r = ty; r < 32; r += 8) {
@@ -335,8 +374,8 @@ __global__ void k_pack_a(int m, int k, int kr, const float2* __restrict__ A, lon
 // B (k x n complex, column-major) -> B_r hi/lo (n rows x kr floats): column j of B
 // as floats, zero-padded from 2k to kr.
 template <int P>
-__global__ void k_pack_b(int k, int n, int kr, const float2* __restrict__ B, long ldb, float* __restrict__ hi,
-                         float* __restrict__ lo) {
+__global__ void k_pack_b(int k, int n, int kr, const float2* __restrict__ B, long ldb, void* __restrict__ hi,
+                         void* __restrict__ lo) {
   const int kp = kr / 2;
   const long total = (long)kp * n;
   for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
@@ -363,18 +402,19 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 2-D fp32 tensor map over rows x kr (row-major, kr a multiple of 32), box
-// 32 x box_rows, 128-byte swizzle, zero fill beyond the last row.
-bool make_map(CUtensorMap* m, const float* base, int kr, int rows, int box_rows) {
+// 2-D tensor map over rows x kr packed elements (fp32, or bf16 when eb = 2;
+// row-major, kr a multiple of one 128-byte row), box 128 bytes x box_rows,
+// 128-byte swizzle, zero fill beyond the last row.
+bool make_map(CUtensorMap* m, const void* base, int kr, int rows, int box_rows, int eb) {
   auto fn = encode_fn();
   if (!fn) return false;
   const cuuint64_t dims[2] = {(cuuint64_t)kr, (cuuint64_t)rows};
-  const cuuint64_t strides[1] = {(cuuint64_t)kr * 4};
-  const cuuint32_t box[2] = {(cuuint32_t)kTK, (cuuint32_t)box_rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)kr * eb};
+  const cuuint32_t box[2] = {(cuuint32_t)(128 / eb), (cuuint32_t)box_rows};
   const cuuint32_t es[2] = {1, 1};
-  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, es,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  return fn(m, eb == 2 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base),
+            dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 int g_num_sms = 0;
@@ -382,19 +422,22 @@ int g_num_sms = 0;
 template <int P>
 cudaError_t launch_tc(cudaStream_t st, int m, int n, int k, const float2* A, long lda, const float2* B, long ldb,
                       float2* C, long ldc, void* ws, int* status) {
-  const int kr = ((2 * k + kTK - 1) / kTK) * kTK;
-  const size_t abytes = (size_t)2 * m * kr * sizeof(float), bbytes = (size_t)n * kr * sizeof(float);
+  constexpr int EB = TcCfg<P>::kEB, KS = tc_kstage<P>();
+  const int kr = ((2 * k + KS - 1) / KS) * KS;
+  const size_t abytes = (size_t)2 * m * kr * EB, bbytes = (size_t)n * kr * EB;
   char* w = static_cast<char*>(ws);
-  float* a_hi = reinterpret_cast<float*>(w);
-  float* a_lo = reinterpret_cast<float*>(w + abytes);
-  float* b_hi = reinterpret_cast<float*>(w + 2 * abytes);
-  float* b_lo = reinterpret_cast<float*>(w + 2 * abytes + bbytes);
+  void* a_hi = w;
+  void* a_lo = w + abytes;
+  void* b_hi = w + 2 * abytes;
+  void* b_lo = w + 2 * abytes + bbytes;
   k_pack_a<P><<<dim3((m + 31) / 32, (kr / 2 + 31) / 32), dim3(32, 8), 0, st>>>(m, k, kr, A, lda, a_hi, a_lo);
   k_pack_b<P><<<1216, 256, 0, st>>>(k, n, kr, B, ldb, b_hi, b_lo);
   CUtensorMap ma_hi, ma_lo, mb_hi, mb_lo;
-  if (!make_map(&ma_hi, a_hi, kr, 2 * m, kTM) || !make_map(&mb_hi, b_hi, kr, n, kTN)) return cudaErrorNotSupported;
-  if (P == 3) {
-    if (!make_map(&ma_lo, a_lo, kr, 2 * m, kTM) || !make_map(&mb_lo, b_lo, kr, n, kTN)) return cudaErrorNotSupported;
+  if (!make_map(&ma_hi, a_hi, kr, 2 * m, kTM, EB) || !make_map(&mb_hi, b_hi, kr, n, kTN, EB))
+    return cudaErrorNotSupported;
+  if (P != 1) {
+    if (!make_map(&ma_lo, a_lo, kr, 2 * m, kTM, EB) || !make_map(&mb_lo, b_lo, kr, n, kTN, EB))
+      return cudaErrorNotSupported;
   } else {
     ma_lo = ma_hi;
     mb_lo = mb_hi;
@@ -406,7 +449,7 @@ cudaError_t launch_tc(cudaStream_t st, int m, int n, int k, const float2* A, lon
   cudaError_t e = cudaFuncSetAttribute(k_cgemm_tc<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k_cgemm_tc<P><<<grid, kThreads, smem, st>>>(ma_hi, mb_hi, ma_lo, mb_lo, reinterpret_cast<float*>(C), 2 * ldc,
-                                              2 * m, n, kr / kTK, tiles_m, ntiles, status);
+                                              2 * m, n, kr / KS, tiles_m, ntiles, status);
   return cudaGetLastError();
 }
 
@@ -442,6 +485,7 @@ cudaError_t cgemm_tc(cudaStream_t st, int passes, int m, int n, int k, const flo
   if (!cgemm_tc_supported()) return cudaErrorNotSupported;
   if (!ws || ws_bytes < cgemm_tc_work_bytes(m, n, k) || (reinterpret_cast<uintptr_t>(ws) & 255u)) return cudaErrorInvalidValue;
   if (passes == 3) return launch_tc<3>(st, m, n, k, A, lda, B, ldb, C, ldc, ws, status);
+  if (passes == 2) return launch_tc<2>(st, m, n, k, A, lda, B, ldb, C, ldc, ws, status);
   if (passes == 1) return launch_tc<1>(st, m, n, k, A, lda, B, ldb, C, ldc, ws, status);
   return cudaErrorInvalidValue;
 }

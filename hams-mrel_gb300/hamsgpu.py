@@ -184,7 +184,7 @@ class Solver:
 
     def __init__(self, precision: int = HG_PREC_FP64, device: int = 0, grn_kind: int = 8,
                  max_refine: int = 10, refine_tol: float = 1e-10, rho: float = 1000.0, g: float = 9.80665,
-                 lu_tensor: int = 3, refine_method: int = 0, fin_table: int = -1, solver: int = 1):
+                 lu_tensor: int = 2, refine_method: int = 0, fin_table: int = -1, solver: int = 1):
         self.L = load()
         opts = HgOpts()
         self.L.hg_default_opts(ctypes.byref(opts))
@@ -421,7 +421,7 @@ class Solver:
         return list(a)
 
 
-def solve_footprint(precision, n, nl, nbody, nbeta, irsp=0, lu_tensor=3):
+def solve_footprint(precision, n, nl, nbody, nbeta, irsp=0, lu_tensor=2):
     """Device bytes one frequency-solve of this size holds (hg_solve_footprint)."""
     return int(load().hg_solve_footprint(precision, n, nl, nbody, nbeta, irsp, lu_tensor))
 

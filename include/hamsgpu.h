@@ -48,9 +48,11 @@ typedef struct {
     double rho;          /* fluid density for the forces (reference Const_mod: 1000) */
     double g;            /* gravity for VINP (reference Const_mod: 9.80665) */
     int lu_tensor;       /* mixed form, order >= 1024: trailing updates of the complex64 LU on the
-                            tensor cores, 3 = split TF32 (three products, single-precision
-                            quality; default), 1 = TF32 (one product, more refinement sweeps),
-                            0 = FP32 SIMT kernels only */
+                            tensor cores, 2 = split BF16 (three products at the BF16 rate,
+                            ~2^-16 product error, one refinement sweep at the benchmark
+                            configurations; default), 3 = split TF32 (three products,
+                            single-precision quality), 1 = TF32 (one product, more refinement
+                            sweeps), 0 = FP32 SIMT kernels only */
     int refine_method;   /* mixed form: 0 = classical iterative refinement (x += LU^-1 r per
                             sweep; default), 1 = GMRES-based refinement (restarted GMRES of
                             src/IterativeSolvers.f90:324-488 on A d = r, right-preconditioned by
@@ -71,7 +73,7 @@ typedef struct {
                             ZBLOCK_GMRES_SOLVE; hg_fill_factor then factors only those blocks */
 } hg_opts;
 
-/* Fill opts with the defaults above (device 0, FP64, GRN_KIND 8, rho 1000, g 9.80665, lu_tensor 3,
+/* Fill opts with the defaults above (device 0, FP64, GRN_KIND 8, rho 1000, g 9.80665, lu_tensor 2,
  * solver 1). */
 void hg_default_opts(hg_opts *opts);
 
@@ -347,7 +349,8 @@ int hg_elapsed(hg_ctx *ctx, int slot0, int slot1, float *ms);
  * buffers; used to report the roofline of the LU trailing update.
  * precision (kernel variant): 0 complex128 SIMT, 1 complex64 SIMT,
  * 2 complex64 tensor cores split TF32 (3 products), 3 complex64 tensor
- * cores TF32 (1 product); 2 and 3 include their operand packing. */
+ * cores TF32 (1 product), 4 complex64 tensor cores split BF16 (3 products
+ * at the BF16 rate); 2-4 include their operand packing. */
 int hg_bench_gemm(hg_ctx *ctx, int precision, int m, int n, int k, int iters, float *ms_per_launch);
 
 /* Average device time (ms, CUDA events around each launch) of the
@@ -359,7 +362,7 @@ int hg_bench_gemm(hg_ctx *ctx, int precision, int m, int n, int k, int iters, fl
 int hg_bench_panel(hg_ctx *ctx, int m, int iters, float *ms_per_launch);
 
 /* C = C - A B through one of those kernel variants on host arrays (all
- * COMPLEX*16, column-major; variants 1-3 round A, B, C to complex64 on the
+ * COMPLEX*16, column-major; variants 1-4 round A, B, C to complex64 on the
  * device and widen the result back).  A test hook for the LU update
  * kernels; the reference's counterpart is the ZGEMM step inside ZGETRF. */
 int hg_gemm_check(hg_ctx *ctx, int variant, int m, int n, int k, const double *a, int lda, const double *b,

@@ -5,8 +5,9 @@ ZGMRES_SOLVE: restarted GMRES with right preconditioning and Givens
 rotations) is reused as the refinement engine: per outer step an FP64
 residual, then GMRES on A d = r preconditioned by the complex64 LU.  Both
 refinement methods must reach the same solution (they stop on the same 1e-10
-residual), including with the weaker plain-TF32 factorisation, where GMRES
-needs more than one Krylov step per outer step.
+residual), with the default split-BF16 factorisation, the split-TF32 one and
+the weaker plain-TF32 one, where GMRES needs more than one Krylov step per
+outer step.
 """
 import numpy as np
 import pytest
@@ -27,11 +28,11 @@ def _solve(pkg, mesh, h, lu_tensor, refine_method, w=1.1):
     return out
 
 
-@pytest.mark.parametrize("lu_tensor", [3, 1])
+@pytest.mark.parametrize("lu_tensor", [2, 3, 1])
 def test_gmres_refinement_matches_classical(pkg, lu_tensor):
     mesh = pkg.meshgen.three_cylinders(with_lid=False)
     assert mesh.n >= 1024  # the two-level LU with tensor-core updates
-    ref = _solve(pkg, mesh, -1.0, 3, 0)
+    ref = _solve(pkg, mesh, -1.0, 2, 0)
     got = _solve(pkg, mesh, -1.0, lu_tensor, 1)
     (sweeps, resid), its = got[4], got[5]
     assert resid <= 1e-10 and 1 <= sweeps <= 10 and its >= sweeps

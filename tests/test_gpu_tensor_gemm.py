@@ -6,6 +6,7 @@ TF32 parts.  Checked against numpy in complex128 on the complex64-rounded
 operands, at shapes that leave ragged tiles in both output dimensions and
 inner dimensions that are and are not multiples of the 32-wide stage:
   - split TF32 (three products) to single-precision accuracy,
+  - split BF16 (three products, 16 of the 24 bits) to ~2^-16,
   - plain TF32 (one product) to TF32 accuracy,
 and through the LU of hg_gesv (order >= 1024 takes the two-level path whose
 outer trailing updates run on these kernels), every variant refining to the
@@ -39,7 +40,7 @@ def solver(pkg):
 
 
 @pytest.mark.parametrize("m,n,k", SHAPES)
-@pytest.mark.parametrize("variant,tol", [(1, 3e-6), (2, 3e-6), (3, 3e-3)])
+@pytest.mark.parametrize("variant,tol", [(1, 3e-6), (2, 3e-6), (3, 3e-3), (4, 1e-4)])
 def test_complex_gemm_variants(solver, m, n, k, variant, tol):
     a, b, c = _operands(m, n, k, seed=m * 7 + n + k)
     ref = c - a @ b
@@ -58,7 +59,7 @@ def test_split_tf32_beats_plain_tf32(solver):
     assert e3 * 20 < e1
 
 
-@pytest.mark.parametrize("lu_tensor", [0, 1, 3])
+@pytest.mark.parametrize("lu_tensor", [0, 1, 2, 3])
 def test_lu_tensor_variants_refine(pkg, lu_tensor):
     n, nrhs = 1300, 5
     rng = np.random.default_rng(3)
@@ -83,4 +84,4 @@ def test_lu_tensor_variants_refine(pkg, lu_tensor):
         if p != i:
             m[[i, p]] = m[[p, i]]
     rec = float(np.abs(m - a).max() / np.abs(a).max())
-    assert rec < (2e-3 if lu_tensor == 1 else 2e-6)
+    assert rec < {1: 2e-3, 2: 2e-5}.get(lu_tensor, 2e-6)
