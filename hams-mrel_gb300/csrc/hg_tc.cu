@@ -25,9 +25,12 @@
 //               (kind::f16, twice the TF32 rate): hi = rn_bf16(x),
 //               lo = rn_bf16(x - hi) keep 16 of x's 24 bits, so the products
 //               carry ~2^-16 relative error, of the order of the FP32
-//               accumulation's own; 64 real K per 128-byte stage row.
+//               accumulation's own.  Each 128-byte row of a packed operand
+//               holds 32 real K as [32 hi | 32 lo], so one tensor copy per
+//               operand brings both parts and a stage is 48 KB: four stages
+//               in flight instead of two.
 //
-// Kernel: persistent, one CTA per SM, 192 threads in three roles:
+// Kernel: persistent, one CTA per SM, 320 threads in three roles:
 //   warp 0 (one thread)  TMA producer: per stage one 2-D tensor copy per
 //                         operand tile (128 B rows, 128-byte swizzle) into a
 //                         ring of shared-memory stages, completing on the
@@ -36,9 +39,11 @@
 //                         M = 128 real rows, N = 256 columns per instruction,
 //                         tcgen05.commit frees the stage and, after the last
 //                         stage, publishes the accumulator;
-//   warps 2..5           epilogue: tcgen05.ld of the accumulator (warp w
-//                         reads TMEM lanes 32 (w % 4) ..), C -= D with
-//                         coalesced column loads and stores.
+//   warps 2..9           epilogue: tcgen05.ld of the accumulator (warp w
+//                         reads TMEM lanes 32 (w % 4) .., warps 2-5 the
+//                         tile's first 128 columns, 6-9 the others), C -= D
+//                         with coalesced column loads and stores; eight
+//                         warps keep twice the C loads in flight of four.
 // Two accumulators (2 x 256 TMEM columns) let the epilogue of one tile run
 // under the main loop of the next.  Every wait is bounded in time: a wait
 // that runs out raises an abort flag that ends every role, and the kernel
@@ -58,7 +63,8 @@ namespace {
 constexpr int kTM = 128;         // real output rows per tile (64 complex rows)
 constexpr int kTN = 256;         // output columns per tile
 constexpr int kTK = 32;          // real inner extent per stage: one 128-byte swizzle row of fp32
-constexpr int kThreads = 192;
+constexpr int kThreads = 320;
+constexpr int kEpiWarps = 8;  // two per TMEM lane quarter, each half of the tile's columns
 constexpr uint32_t kATile = kTM * kTK * 4;  // 16 KB
 constexpr uint32_t kBTile = kTN * kTK * 4;  // 32 KB
 constexpr uint32_t kTmemCols = 2 * kTN;     // two accumulators
@@ -72,8 +78,8 @@ template <> struct TcCfg<3> {
   static constexpr int kEB = 4;                                    // bytes per packed element
 };
 template <> struct TcCfg<2> {
-  static constexpr int kStages = 2;
-  static constexpr uint32_t kStageBytes = 2 * (kATile + kBTile);
+  static constexpr int kStages = 4;
+  static constexpr uint32_t kStageBytes = kATile + kBTile;  // [hi | lo] rows of A and B
   static constexpr int kEB = 2;
 };
 template <> struct TcCfg<1> {
@@ -81,8 +87,8 @@ template <> struct TcCfg<1> {
   static constexpr uint32_t kStageBytes = kATile + kBTile;
   static constexpr int kEB = 4;
 };
-// real K per stage: one 128-byte swizzle row of packed elements
-template <int P> constexpr int tc_kstage() { return 128 / TcCfg<P>::kEB; }
+// real K per stage: one 128-byte swizzle row of packed elements (BF16: 32 hi + 32 lo)
+template <int P> constexpr int tc_kstage() { return P == 2 ? 32 : 128 / TcCfg<P>::kEB; }
 template <int P> constexpr size_t tc_smem_bytes() {
   return (size_t)TcCfg<P>::kStages * TcCfg<P>::kStageBytes + 1024;  // + slack for 1024-byte alignment
 }
@@ -192,8 +198,8 @@ k_cgemm_tc(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CU
     }
     mbar_init(&tfull[0], 1);
     mbar_init(&tfull[1], 1);
-    mbar_init(&tempty[0], 4);
-    mbar_init(&tempty[1], 4);
+    mbar_init(&tempty[0], kEpiWarps);
+    mbar_init(&tempty[1], kEpiWarps);
     mbar_init(&drain, 1);
     s_abort = 0;
   }
@@ -223,10 +229,10 @@ k_cgemm_tc(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CU
           if (!tc_wait(&empty[s], ph ^ 1, &s_abort)) { ok = false; break; }
           unsigned char* st = smem + (size_t)s * SB;
           mbar_expect_tx(&full[s], SB);
-          const int kx = kt * tc_kstage<P>();
+          const int kx = kt * (P == 2 ? 64 : tc_kstage<P>());  // x in packed elements
           tma_load_2d(st, &ta_hi, kx, ym, &full[s]);
           tma_load_2d(st + kATile, &tb_hi, kx, yn, &full[s]);
-          if (P != 1) {
+          if (P == 3) {
             tma_load_2d(st + kATile + kBTile, &ta_lo, kx, ym, &full[s]);
             tma_load_2d(st + 2 * kATile + kBTile, &tb_lo, kx, yn, &full[s]);
           }
@@ -262,16 +268,26 @@ k_cgemm_tc(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CU
           tc_fence_after();
           const uint32_t a_hi = smem_addr(smem + (size_t)s * SB), b_hi = a_hi + kATile;
           const uint32_t a_lo = b_hi + kBTile, b_lo = a_lo + kATile;
-          constexpr bool BF = (P == 2);
+          if (P == 2) {
+            // [hi | lo] rows: K-steps of 16 bf16 (32 bytes) at 0 and 32, their lo parts 64 bytes on
 #pragma unroll
-          for (int kk = 0; kk < 4; ++kk) {
-            const uint32_t off = kk * 32;  // one instruction's K (8 tf32 or 16 bf16) = 32 bytes of the swizzle row
-            if (P != 1) {
-              tc_mma<BF>(d, sw128_desc(a_lo + off), sw128_desc(b_hi + off), (kt | kk) != 0);
-              tc_mma<BF>(d, sw128_desc(a_hi + off), sw128_desc(b_lo + off), 1u);
-              tc_mma<BF>(d, sw128_desc(a_hi + off), sw128_desc(b_hi + off), 1u);
-            } else {
-              tc_mma<BF>(d, sw128_desc(a_hi + off), sw128_desc(b_hi + off), (kt | kk) != 0);
+            for (int kk = 0; kk < 2; ++kk) {
+              const uint32_t off = kk * 32;
+              tc_mma<true>(d, sw128_desc(a_hi + 64 + off), sw128_desc(b_hi + off), (kt | kk) != 0);
+              tc_mma<true>(d, sw128_desc(a_hi + off), sw128_desc(b_hi + 64 + off), 1u);
+              tc_mma<true>(d, sw128_desc(a_hi + off), sw128_desc(b_hi + off), 1u);
+            }
+          } else {
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+              const uint32_t off = kk * 32;  // one instruction's K (8 tf32) = 32 bytes of the swizzle row
+              if (P == 3) {
+                tc_mma<false>(d, sw128_desc(a_lo + off), sw128_desc(b_hi + off), (kt | kk) != 0);
+                tc_mma<false>(d, sw128_desc(a_hi + off), sw128_desc(b_lo + off), 1u);
+                tc_mma<false>(d, sw128_desc(a_hi + off), sw128_desc(b_hi + off), 1u);
+              } else {
+                tc_mma<false>(d, sw128_desc(a_hi + off), sw128_desc(b_hi + off), (kt | kk) != 0);
+              }
             }
           }
           tc_commit(&empty[s]);
@@ -286,8 +302,8 @@ k_cgemm_tc(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CU
       }
     }
   } else {
-    // ---- epilogue: warps 2..5, TMEM lane quarter q = warp % 4 ----
-    const int q = warp & 3;
+    // ---- epilogue: warps 2..9, TMEM lane quarter q = warp % 4, column half (warp - 2) / 4 ----
+    const int q = warp & 3, half = (warp - 2) >> 2;
     int it = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
       const int acc = it & 1;
@@ -299,7 +315,7 @@ k_cgemm_tc(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CU
       const bool rok = row < mr;
       float* crow = C + row;
       const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * kTN);
-      for (int c0 = 0; c0 < kTN; c0 += 32) {
+      for (int c0 = half * (kTN / 2); c0 < (half + 1) * (kTN / 2); c0 += 32) {
         const int col0 = col_base + c0;
         if (col0 >= n) break;  // uniform over the warp
         float cv[32];
@@ -332,16 +348,22 @@ __device__ __forceinline__ float tf32_rna(float x) {
   return __uint_as_float(r);
 }
 
+// off: the packed element offset row * kr + k of a pair (k even).  BF16 rows
+// hold [32 hi | 32 lo] per 32 values of k, so row r's k lands at
+// r * 2 kr + (k / 32) * 64 + k % 32 (hi) and 32 further on (lo); lo is unused.
 template <int P>
 __device__ __forceinline__ void split_store(void* hi, void* lo, long off, float x0, float x1) {
   if (P == 2) {
+    const long e = 2 * off - (off & 31);  // r * 2 kr + (k / 32) * 64 + k % 32, kr a multiple of 32
     const __nv_bfloat16 h0 = __float2bfloat16_rn(x0), h1 = __float2bfloat16_rn(x1);
     __nv_bfloat162 hv, lv;
     hv.x = h0; hv.y = h1;
     lv.x = __float2bfloat16_rn(x0 - __bfloat162float(h0));
     lv.y = __float2bfloat16_rn(x1 - __bfloat162float(h1));
-    *reinterpret_cast<__nv_bfloat162*>(static_cast<__nv_bfloat16*>(hi) + off) = hv;
-    *reinterpret_cast<__nv_bfloat162*>(static_cast<__nv_bfloat16*>(lo) + off) = lv;
+    __nv_bfloat16* base = static_cast<__nv_bfloat16*>(hi);
+    *reinterpret_cast<__nv_bfloat162*>(base + e) = hv;
+    *reinterpret_cast<__nv_bfloat162*>(base + e + 32) = lv;
+    (void)lo;
     return;
   }
   const float h0 = tf32_rna(x0), h1 = tf32_rna(x1);
@@ -433,9 +455,10 @@ cudaError_t launch_tc(cudaStream_t st, int m, int n, int k, const float2* A, lon
   k_pack_a<P><<<dim3((m + 31) / 32, (kr / 2 + 31) / 32), dim3(32, 8), 0, st>>>(m, k, kr, A, lda, a_hi, a_lo);
   k_pack_b<P><<<1216, 256, 0, st>>>(k, n, kr, B, ldb, b_hi, b_lo);
   CUtensorMap ma_hi, ma_lo, mb_hi, mb_lo;
-  if (!make_map(&ma_hi, a_hi, kr, 2 * m, kTM, EB) || !make_map(&mb_hi, b_hi, kr, n, kTN, EB))
+  const int kx = (P == 2) ? 2 * kr : kr;  // BF16: [hi | lo] rows twice as long, one map per operand
+  if (!make_map(&ma_hi, a_hi, kx, 2 * m, kTM, EB) || !make_map(&mb_hi, b_hi, kx, n, kTN, EB))
     return cudaErrorNotSupported;
-  if (P != 1) {
+  if (P == 3) {
     if (!make_map(&ma_lo, a_lo, kr, 2 * m, kTM, EB) || !make_map(&mb_lo, b_lo, kr, n, kTN, EB))
       return cudaErrorNotSupported;
   } else {
