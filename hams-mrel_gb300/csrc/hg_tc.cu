@@ -30,7 +30,7 @@
 //               operand brings both parts and a stage is 48 KB: four stages
 //               in flight instead of two.
 //
-// Kernel: persistent, one CTA per SM, 320 threads in three roles:
+// Kernel: persistent, one CTA per SM, 576 threads in three roles:
 //   warp 0 (one thread)  TMA producer: per stage one 2-D tensor copy per
 //                         operand tile (128 B rows, 128-byte swizzle) into a
 //                         ring of shared-memory stages, completing on the
@@ -39,11 +39,12 @@
 //                         M = 128 real rows, N = 256 columns per instruction,
 //                         tcgen05.commit frees the stage and, after the last
 //                         stage, publishes the accumulator;
-//   warps 2..9           epilogue: tcgen05.ld of the accumulator (warp w
-//                         reads TMEM lanes 32 (w % 4) .., warps 2-5 the
-//                         tile's first 128 columns, 6-9 the others), C -= D
-//                         with coalesced column loads and stores; eight
-//                         warps keep twice the C loads in flight of four.
+//   warps 2..17          epilogue: tcgen05.ld of the accumulator (warp w
+//                         reads TMEM lanes 32 (w % 4) .., and the (w - 2) / 4-th
+//                         quarter of the tile's columns, 16 at a time), C -= D
+//                         with coalesced column loads and stores: sixteen
+//                         warps keep the C loads of a tile in flight, which
+//                         four could not (the update then waited on them).
 // Two accumulators (2 x 256 TMEM columns) let the epilogue of one tile run
 // under the main loop of the next.  Every wait is bounded in time: a wait
 // that runs out raises an abort flag that ends every role, and the kernel
@@ -63,8 +64,10 @@ namespace {
 constexpr int kTM = 128;         // real output rows per tile (64 complex rows)
 constexpr int kTN = 256;         // output columns per tile
 constexpr int kTK = 32;          // real inner extent per stage: one 128-byte swizzle row of fp32
-constexpr int kThreads = 320;
-constexpr int kEpiWarps = 8;  // two per TMEM lane quarter, each half of the tile's columns
+constexpr int kEpiWarps = 16;                   // four per TMEM lane quarter, each a quarter of the tile's columns
+constexpr int kThreads = 64 + 32 * kEpiWarps;    // + the producer and MMA warps
+constexpr int kEpiCols = kTN / (kEpiWarps / 4);  // columns of one epilogue warp
+constexpr int kEpiChunk = 16;                    // accumulator columns per tcgen05.ld
 constexpr uint32_t kATile = kTM * kTK * 4;  // 16 KB
 constexpr uint32_t kBTile = kTN * kTK * 4;  // 32 KB
 constexpr uint32_t kTmemCols = 2 * kTN;     // two accumulators
@@ -147,6 +150,17 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
           "r"(smem_addr(dst)),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
       : "memory");
+}
+
+// 16 consecutive accumulator columns of this warp's 32 TMEM lanes, one lane per thread.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+        "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
 // 32 consecutive accumulator columns of this warp's 32 TMEM lanes, one lane per thread.
@@ -302,8 +316,8 @@ k_cgemm_tc(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CU
       }
     }
   } else {
-    // ---- epilogue: warps 2..9, TMEM lane quarter q = warp % 4, column half (warp - 2) / 4 ----
-    const int q = warp & 3, half = (warp - 2) >> 2;
+    // ---- epilogue: warps 2..17, TMEM lane quarter q = warp % 4, column quarter (warp - 2) / 4 ----
+    const int q = warp & 3, part = (warp - 2) >> 2;
     int it = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
       const int acc = it & 1;
@@ -315,16 +329,16 @@ k_cgemm_tc(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CU
       const bool rok = row < mr;
       float* crow = C + row;
       const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * kTN);
-      for (int c0 = half * (kTN / 2); c0 < (half + 1) * (kTN / 2); c0 += 32) {
+      for (int c0 = part * kEpiCols; c0 < (part + 1) * kEpiCols; c0 += kEpiChunk) {
         const int col0 = col_base + c0;
         if (col0 >= n) break;  // uniform over the warp
-        float cv[32];
+        float cv[kEpiChunk];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) cv[j] = (rok && col0 + j < n) ? crow[(long)(col0 + j) * ldcf] : 0.f;
-        uint32_t dv[32];
-        tmem_ld32(tbase + (uint32_t)c0, dv);
+        for (int j = 0; j < kEpiChunk; ++j) cv[j] = (rok && col0 + j < n) ? crow[(long)(col0 + j) * ldcf] : 0.f;
+        uint32_t dv[kEpiChunk];
+        tmem_ld16(tbase + (uint32_t)c0, dv);
 #pragma unroll
-        for (int j = 0; j < 32; ++j)
+        for (int j = 0; j < kEpiChunk; ++j)
           if (rok && col0 + j < n) crow[(long)(col0 + j) * ldcf] = cv[j] - __uint_as_float(dv[j]);
       }
       tc_fence_before();
