@@ -878,6 +878,24 @@ int build_rhs(hg_ctx* c, int nbeta, const double* betas_h, bool modes) {
   return 0;
 }
 
+// The mixed deep-water fill's self and adjacent pairs for tn field rows,
+// listed once per mesh: one synchronisation for their number.
+int ensure_mnear(hg_ctx* c, int tn) {
+  if (c->mnear_tn == tn) return 0;
+  const int n = c->n;
+  CK(c->mnear_cnt.ensure(1));
+  if (hg::mixed_near_count(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, c->ox, c->oy, c->mnear_cnt.p))
+    return fail(c, HG_ERR_CUDA, "near-pair count failed: %s", cudaGetErrorString(cudaGetLastError()));
+  int np = 0;
+  CK(cudaMemcpyAsync(&np, c->mnear_cnt.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  CK(c->mnear_list.ensure(np > 0 ? np : 1));
+  CK(hg::mixed_near_build(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, c->ox, c->oy, c->mnear_cnt.p, c->mnear_list.p));
+  c->mnear_np = np;
+  c->mnear_tn = tn;
+  return 0;
+}
+
 // Columns c0 .. c0 + nc - 1 of the potentials to the caller's array (leading
 // dimension ldm): one device copy into a pinned staging buffer of this
 // context, then the columns by this host thread (the solve slots of a sweep
@@ -1227,20 +1245,8 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
       CK(hg::launch_green_fill_fin_fma(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, fs, c->o.grn_kind, c->Af.p, c->Sf.p, tn,
                                        c->status.p, binned ? c->bins.p : nullptr));
     } else if (!special && c->o.grn_kind == 8) {
-      if (c->mnear_tn != tn) {
-        // the self and adjacent pairs, once per mesh: one synchronisation for their number
-        CK(c->mnear_cnt.ensure(1));
-        if (hg::mixed_near_count(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, c->ox, c->oy, c->mnear_cnt.p))
-          return fail(c, HG_ERR_CUDA, "near-pair count failed: %s", cudaGetErrorString(cudaGetLastError()));
-        int np = 0;
-        CK(cudaMemcpyAsync(&np, c->mnear_cnt.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
-        CK(cudaStreamSynchronize(c->st));
-        CK(c->mnear_list.ensure(np > 0 ? np : 1));
-        CK(hg::mixed_near_build(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, c->ox, c->oy, c->mnear_cnt.p,
-                                c->mnear_list.p));
-        c->mnear_np = np;
-        c->mnear_tn = tn;
-      }
+      const int r = ensure_mnear(c, tn);
+      if (r) return r;
       CK(hg::launch_green_fill_mixed(c->st, c->rec.p, c->fx.p, c->tnf, n, tn, c->v, c->ox, c->oy, c->pgauss.p, c->Af.p,
                                      c->Sf.p, tn, c->status.p, -1, c->mnear_list.p, c->mnear_np));
     }
@@ -1495,6 +1501,16 @@ int hg_solve_sweep(hg_ctx* c, int nfreq, const double* v, const double* wk, cons
   }
   const int nd = 6 * c->nbody;
   const size_t mx_cols = (size_t)nd + nbeta;
+  // The mixed deep-water fill's near-pair list depends on the mesh only: listed
+  // once here and copied by every slot that does not hold it, instead of being
+  // listed by each slot (two passes over all N x N pairs per slot)
+  const int sweep_tn = c->n + (irsp == 1 ? c->nl : 0);
+  const bool share_near = mixed(c) && h < 0.0 && c->o.grn_kind == 8 && c->o.solver != 2;
+  if (share_near) {
+    cudaSetDevice(c->o.device);
+    const int r = ensure_mnear(c, sweep_tn);
+    if (r) return r;
+  }
   // Fork/join on the device: the slots' streams wait for the work queued on
   // this context's stream so far, and this stream waits for every slot at the
   // end, so events recorded on it (hg_mark) bracket the whole sweep.
@@ -1518,6 +1534,20 @@ int hg_solve_sweep(hg_ctx* c, int nfreq, const double* v, const double* wk, cons
         return;
       }
       sl->slot_gen = c->mesh_gen;
+    }
+    if (share_near && sl->mnear_tn != sweep_tn) {
+      // the parent's list, queued behind the fork event on this slot's stream
+      if (sl->mnear_list.ensure(c->mnear_np > 0 ? c->mnear_np : 1) != cudaSuccess ||
+          cudaMemcpyAsync(sl->mnear_list.p, c->mnear_list.p, (size_t)(c->mnear_np > 0 ? c->mnear_np : 1) * sizeof(int),
+                          cudaMemcpyDeviceToDevice, sl->st) != cudaSuccess) {
+        sl->err = "copying the near-pair list to the slot failed";
+        slot_rc[k] = HG_ERR_CUDA;
+        mesh_failed[k] = 1;
+        next.store(nfreq);
+        return;
+      }
+      sl->mnear_np = c->mnear_np;
+      sl->mnear_tn = sweep_tn;
     }
     for (;;) {
       const int i = next.fetch_add(1);
