@@ -843,9 +843,13 @@ int solve_cols_once(hg_ctx* c, int c0, int c1) {
     k_colmax<<<nc, 256, 0, c->st>>>(n, Rh, n, nb.p + nc);
     CK(cudaMemcpyAsync(rnorm.data(), nb.p + nc, nc * sizeof(double), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
+    const double prev = worst;
     worst = 0.0;
     for (int k = 0; k < nc; ++k) worst = std::fmax(worst, bnorm[k] > 0 ? rnorm[k] / bnorm[k] : rnorm[k]);
     if (worst <= c->o.refine_tol || sweep >= c->o.max_refine) break;
+    // split-BF16 factors that reduce the residual less than tenfold per sweep
+    // are replaced by split-TF32 ones (solve_cols) rather than swept to max_refine
+    if (c->lu_used == 2 && sweep >= 1 && worst > 0.1 * prev) break;
     // x += M^{-1} r (complex64 correction)
     CK(hg::convert_z2c_2d(c->st, n, nc, Rh, n, Bf, n));
     CK(lu_solve(Bf));
@@ -1753,6 +1757,7 @@ int hg_gesv(hg_ctx* c, int precision, int n, int nrhs, double* a, int lda, int* 
         CK(lu_solve(dBf.p));
         CK(hg::convert_c2z(c->st, (long)nb, dBf.p, dX.p));
         bool ok = false;
+        double worst = 0.0;
         for (int sweep = 0;; ++sweep) {
           CK(cudaMemcpyAsync(dR.p, dB.p, nb * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
           CK(hg::gemm<double>(c->st, false, n, nrhs, n, mone, dA.p, n, dX.p, n, one, dR.p, n, (void*)ws.p,
@@ -1760,10 +1765,12 @@ int hg_gesv(hg_ctx* c, int precision, int n, int nrhs, double* a, int lda, int* 
           k_colmax<<<nrhs, 256, 0, c->st>>>(n, dR.p, n, norms.p + nrhs);
           CK(cudaMemcpyAsync(rn.data(), norms.p + nrhs, nrhs * sizeof(double), cudaMemcpyDeviceToHost, c->st));
           CK(cudaStreamSynchronize(c->st));
-          double worst = 0.0;
+          const double prev = worst;
+          worst = 0.0;
           for (int k = 0; k < nrhs; ++k) worst = std::fmax(worst, bn[k] > 0 ? rn[k] / bn[k] : rn[k]);
           if (worst <= c->o.refine_tol) { ok = true; it = sweep; break; }
           if (sweep >= c->o.max_refine) break;
+          if (tcv == 2 && sweep >= 1 && worst > 0.1 * prev) break;  // stalling split-BF16 factors: redo
           CK(hg::convert_z2c(c->st, (long)nb, dR.p, dBf.p));
           CK(lu_solve(dBf.p));
           CK(hg::add_c2z_2d(c->st, n, nrhs, dBf.p, n, dX.p, n));
