@@ -610,9 +610,13 @@ def _launch_count(n, prec, sweeps=1, nd=30, nbeta=8):
     # mixed: RHS (incident, source columns, S W as a split product: 3 kernels);
     # 1 + sweeps solves, each followed by a residual check (product, split,
     # reduce) and bracketed by conversions; column norms of B and of each residual
-    # (later sweeps update the residual with the correction: one more conversion each)
+    # (later sweeps update the residual with the correction: one more conversion each).
+    # The first residual is the sliced tensor-core product (nd + nbeta <= 40): row maxima,
+    # row exponents, A's digits, their K padding (when 2N is not a multiple of 128), y's
+    # digits, the product, the sum: 4 or 3 kernels more than the split product.
     s1 = 1 + sweeps
-    return fill + lu + 5 + s1 * getrs + 3 * s1 + (1 + s1) + 2 * s1 + sweeps + forces
+    sliced = (4 if (2 * n) % 128 else 3) if nd + nbeta <= 40 else 0
+    return fill + lu + 5 + s1 * getrs + 3 * s1 + sliced + (1 + s1) + 2 * s1 + sweeps + forces
 
 
 # Counted per-pair work of the deep-water fill (oracle/opcount.py on the 6048-panel array): mean

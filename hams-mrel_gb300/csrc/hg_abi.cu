@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <algorithm>
 #include <atomic>
@@ -92,6 +93,7 @@ struct hg_ctx {
   DevBuf<double2> A, S, C, A64, B, X, R, R2, W, Wz, part, exfc, gws;  // gws: split-K GEMM workspace
   DevBuf<float2> Af, Sf, Cf, Bf, Aof;  // Aof: unfactorised copy of Af (mixed form, irsp = 0)
   DevBuf<unsigned char> rws;             // workspace of the double-float residual
+  DevBuf<unsigned char> ozws;            // workspace of the sliced tensor-core residual (digits of A)
   DevBuf<unsigned char> luws;            // packed operands of the tensor-core LU updates
   DevBuf<double> amas, bdmp;
   DevBuf<double> nrm;                    // column norms of the refinement (2 x columns)
@@ -833,7 +835,16 @@ int solve_cols_once(hg_ctx* c, int c0, int c1) {
       CK(hg::resid_df(c->st, false, tn, nc, n, A0, tn, Xc, n, Bc, tn, -1.0, R1, tn, rws, rws_bytes));
       CK(hg::resid_df(c->st, true, n, nc, tn, A0, tn, R1, tn, nullptr, 0, 1.0, Rh, n, rws, rws_bytes));
     } else if (sweep == 0) {
-      CK(hg::resid_df(c->st, false, n, nc, n, A0, tn, Xc, n, Bc, tn, -1.0, Rh, n, rws, rws_bytes));
+      // the first residual, b - A x0 with x0 of the size of x, carries the FP64
+      // accuracy: sliced products on the tensor cores where they apply (up to
+      // 40 columns), else double-float products
+      const size_t ozb = hg::resid_tc_work_bytes(n, nc, n);
+      if (ozb && hg::resid_tc_supported()) {
+        CK(c->ozws.ensure(ozb));
+        CK(hg::resid_tc(c->st, n, nc, n, A0, tn, Xc, n, Bc, tn, -1.0, Rh, n, c->ozws.p, c->ozws.cap, c->status.p));
+      } else {
+        CK(hg::resid_df(c->st, false, n, nc, n, A0, tn, Xc, n, Bc, tn, -1.0, Rh, n, rws, rws_bytes));
+      }
     } else {
       double2* D = c->R.p;  // tn x nc >= n x nc, unused for irsp = 0
       CK(hg::convert_c2z_2d(c->st, n, nc, Bf, n, D, n));
@@ -989,6 +1000,7 @@ void hg_destroy(hg_ctx* c) {
   DevBuf<float2>* cbs[] = {&c->Af, &c->Sf, &c->Cf, &c->Bf, &c->Aof};
   for (auto* b : cbs) b->release();
   c->rws.release();
+  c->ozws.release();
   for (hg_ctx* sl : c->slots) hg_destroy(sl);
   c->slots.clear();
   if (c->pin_out) cudaFreeHost(c->pin_out);
@@ -1669,6 +1681,7 @@ size_t hg_solve_footprint(int precision, int n, int nl, int nbody, int nbeta, in
     b += sizeof(float2) * (tn * nn * (irsp == 1 ? 2 : 3) + (irsp == 1 ? nn * nn : 0) + nn * nc);
     b += sizeof(double2) * (tn * nc + nn * nc);
     b += hg::resid_work_bytes((int)tn, (int)nc, (int)tn);
+    if (irsp != 1) b += hg::resid_tc_work_bytes(n, (int)nc, n);
     b += hg::lu_work_bytes(n, lu_tensor);
   } else {
     b += sizeof(double2) * (2 * tn * nn + (irsp == 1 ? nn * nn + nn * nc : 0));
@@ -1967,6 +1980,40 @@ int hg_gemm_check(hg_ctx* c, int variant, int m, int n, int k, const double* a, 
     CK(hg::convert_c2z(c->st, (long)nc, fc.p, dc.p));
   }
   CK(cudaMemcpyAsync(cm, dc.p, nc * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return check_status(c);
+}
+
+int hg_resid_check(hg_ctx* c, int variant, int m, int nc, int k, const double* a, int lda, const double* y, int ldy,
+                   const double* b, int ldb, double* out, int ldo) {
+  if (!c) return -1;
+  if (variant < 0 || variant > 1) return fail(c, -2, "variant must be 0 (double-float) or 1 (sliced, tensor cores)");
+  if (variant == 1 && !hg::resid_tc_supported()) return fail(c, -2, "the sliced residual needs an sm_103 device");
+  if (m <= 0 || nc <= 0 || k <= 0 || nc > 40) return fail(c, -3, "bad shape (nc <= 40)");
+  if (!a || lda < m || !y || ldy < k || !b || ldb < m || !out || ldo < m) return fail(c, -6, "bad array or leading dimension");
+  CK(cudaSetDevice(c->o.device));
+  DevBuf<double2> da, dy, db, dout;
+  DevBuf<float2> fa;
+  DevBuf<unsigned char> ws;
+  const size_t na = (size_t)lda * k;
+  CK(da.ensure(na));
+  CK(fa.ensure(na));
+  CK(dy.ensure((size_t)ldy * nc));
+  CK(db.ensure((size_t)ldb * nc));
+  CK(dout.ensure((size_t)m * nc));
+  CK(cudaMemcpyAsync(da.p, a, na * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(dy.p, y, (size_t)ldy * nc * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(db.p, b, (size_t)ldb * nc * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+  CK(hg::convert_z2c(c->st, (long)na, da.p, fa.p));
+  if (variant == 0) {
+    CK(ws.ensure(hg::resid_work_bytes(m, nc, k)));
+    CK(hg::resid_df(c->st, false, m, nc, k, fa.p, lda, dy.p, ldy, db.p, ldb, -1.0, dout.p, m, ws.p, ws.cap));
+  } else {
+    CK(ws.ensure(hg::resid_tc_work_bytes(m, nc, k)));
+    CK(hg::resid_tc(c->st, m, nc, k, fa.p, lda, dy.p, ldy, db.p, ldb, -1.0, dout.p, m, ws.p, ws.cap, c->status.p));
+  }
+  CK(cudaMemcpy2DAsync(out, (size_t)ldo * sizeof(double2), dout.p, (size_t)m * sizeof(double2), (size_t)m * sizeof(double2),
+                       nc, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   return check_status(c);
 }

@@ -37,6 +37,16 @@ cudaError_t resid_df(cudaStream_t st, bool transa, int m, int nc, int k, const f
                      long ldy, const double2* Bin, long ldb, double sign, double2* out, long ldo, void* ws,
                      size_t ws_bytes, bool exact = true);
 
+// The same product as resid_df (exact mode, untransposed A) on the tensor
+// cores by exact operand slicing (hg_resid_tc.cu): about 2^-42 of sum |a||y|
+// per entry.  nc <= 40; ws: 256-byte aligned, at least resid_tc_work_bytes;
+// status receives a timeout code if a bounded wait runs out.
+bool resid_tc_supported();
+size_t resid_tc_work_bytes(int m, int nc, int k);
+cudaError_t resid_tc(cudaStream_t st, int m, int nc, int k, const float2* A, long lda, const double2* Y, long ldy,
+                     const double2* Bin, long ldb, double sign, double2* out, long ldo, void* ws, size_t ws_bytes,
+                     int* status);
+
 // Complex64 GEMM for N <= 48 untransposed (hg_gemm32.cu), without split-K.
 cudaError_t cgemm_skinny(cudaStream_t st, int m, int n, int k, float2 alpha, const float2* A, long lda,
                          const float2* B, long ldb, float2 beta, float2* C, long ldc);

@@ -27,7 +27,7 @@ EXPORTS = [
     "hg_solve_sweep", "hg_gmres_iterations", "hg_solve_footprint", "hg_server_create", "hg_server_submit",
     "hg_server_wait", "hg_server_stats", "hg_server_last_error", "hg_server_destroy", "hg_field_points",
     "hg_case_read", "hg_case_free", "hg_case_info", "hg_case_arrays", "hg_case_run", "hg_case_write",
-    "hg_iter_info", "hg_case_options", "hg_server_timeline", "hg_bench_panel",
+    "hg_iter_info", "hg_case_options", "hg_server_timeline", "hg_bench_panel", "hg_resid_check",
 ]
 
 
@@ -118,6 +118,8 @@ def load(build_if_missing: bool = True):
     L.hg_bench_panel.argtypes = [c_void_p, c_int, c_int, P(ctypes.c_float)]
     L.hg_gemm_check.argtypes = [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_void_p,
                                 c_int]
+    L.hg_resid_check.argtypes = [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_void_p,
+                                 c_int, c_void_p, c_int]
     L.hg_mark.argtypes = [c_void_p, c_int]
     L.hg_elapsed.argtypes = [c_void_p, c_int, c_int, P(ctypes.c_float)]
     L.hg_dispersion.argtypes = [c_double, c_double, c_int, c_void_p]
@@ -376,6 +378,18 @@ class Solver:
         m, k = a.shape
         n = b.shape[1]
         self._check(self.L.hg_gemm_check(self.h, variant, m, n, k, _ptr(a), m, _ptr(b), k, _ptr(out), m))
+        return out
+
+    def resid_check(self, variant, a, y, b):
+        """b - A y through the refinement residual's kernel `variant` (hg_resid_check:
+        0 double-float, 1 sliced on the tensor cores); A rounded to complex64 on the device."""
+        a = np.asfortranarray(a, dtype=np.complex128)
+        y = np.asfortranarray(y, dtype=np.complex128)
+        b = np.asfortranarray(b, dtype=np.complex128)
+        m, k = a.shape
+        nc = y.shape[1]
+        out = np.zeros((m, nc), dtype=np.complex128, order="F")
+        self._check(self.L.hg_resid_check(self.h, variant, m, nc, k, _ptr(a), m, _ptr(y), k, _ptr(b), m, _ptr(out), m))
         return out
 
     def bench_gemm(self, variant, m, n, k, iters=3):

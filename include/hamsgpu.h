@@ -368,6 +368,15 @@ int hg_bench_panel(hg_ctx *ctx, int m, int iters, float *ms_per_launch);
 int hg_gemm_check(hg_ctx *ctx, int variant, int m, int n, int k, const double *a, int lda, const double *b,
                   int ldb, double *c, int ldc);
 
+/* out = b - A y (all COMPLEX*16, column-major; A rounded to complex64 on the
+ * device, as the mixed form's matrix is) through the refinement residual's
+ * kernels: variant 0 the double-float products on the FP32 pipes, 1 the
+ * sliced products on the tensor cores (Ozaki et al. 2012: BF16 digits of the
+ * row- and column-scaled operands, exact FP32 partial sums).  nc <= 40.  A
+ * test hook for the residual of the refinement. */
+int hg_resid_check(hg_ctx *ctx, int variant, int m, int nc, int k, const double *a, int lda, const double *y,
+                   int ldy, const double *b, int ldb, double *out, int ldo);
+
 /* Time (milliseconds, CUDA events on the context stream) of the stages of the
  * last hg_solve_frequency: [0] fill, [1] LU, [2] solves and refinement, [3] forces. */
 int hg_stage_times(const hg_ctx *ctx, float *ms4);
