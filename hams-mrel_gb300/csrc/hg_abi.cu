@@ -1226,10 +1226,14 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
       CK(cudaMemsetAsync(c->info.p, 0, sizeof(int), c->st));
       const int r = setup_iter_precond(c);
       if (r) return r;
-    } else if (irsp == 1) {
-      CK(hg::getrf<double>(c->st, n, c->C.p, n, c->ipiv.p, c->info.p, nullptr, 0, 0, &c->lu_aux));
     } else {
-      CK(hg::getrf<double>(c->st, n, c->A.p, tn, c->ipiv.p, c->info.p, nullptr, 0, 0, &c->lu_aux));
+      // U12 and the trailing updates as exact digit products on the tensor cores (lu_tensor != 0)
+      const size_t lwz = (c->o.lu_tensor != 0 && hg::zgemm_tc_supported()) ? hg::lu_work_bytes_z(n) : 0;
+      if (lwz) CK(c->luws.ensure(lwz));
+      if (irsp == 1)
+        CK(hg::getrf<double>(c->st, n, c->C.p, n, c->ipiv.p, c->info.p, c->luws.p, lwz, c->o.lu_tensor, &c->lu_aux));
+      else
+        CK(hg::getrf<double>(c->st, n, c->A.p, tn, c->ipiv.p, c->info.p, c->luws.p, lwz, c->o.lu_tensor, &c->lu_aux));
     }
   } else {
     CK(c->Af.ensure((size_t)tn * n));
@@ -1685,6 +1689,7 @@ size_t hg_solve_footprint(int precision, int n, int nl, int nbody, int nbeta, in
     b += hg::lu_work_bytes(n, lu_tensor);
   } else {
     b += sizeof(double2) * (2 * tn * nn + (irsp == 1 ? nn * nn + nn * nc : 0));
+    if (lu_tensor != 0) b += hg::lu_work_bytes_z(n);
   }
   return b;
 }
@@ -1805,7 +1810,9 @@ int hg_gesv(hg_ctx* c, int precision, int n, int nrhs, double* a, int lda, int* 
   }
   if (fp64) {
     // dA still holds the caller's matrix whenever this branch runs
-    CK(hg::getrf<double>(c->st, n, dA.p, n, dpiv.p, dinfo.p, nullptr));
+    const size_t lwz = (c->o.lu_tensor != 0 && hg::zgemm_tc_supported()) ? hg::lu_work_bytes_z(n) : 0;
+    if (lwz) CK(luws.ensure(lwz));
+    CK(hg::getrf<double>(c->st, n, dA.p, n, dpiv.p, dinfo.p, luws.p, lwz, c->o.lu_tensor));
     CK(cudaMemcpyAsync(&inf, dinfo.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
     if (inf < 0) return fail(c, HG_ERR_DEVICE, "LU panel: a bounded cluster wait ran out (info %d)", inf);
@@ -1843,6 +1850,8 @@ cudaError_t gemm_variant(hg_ctx* c, int variant, int m, int n, int k, void* a, i
     case 4:
       return hg::cgemm_tc(c->st, variant == 2 ? 3 : (variant == 3 ? 1 : 2), m, n, k, (float2*)a, lda, (float2*)b, ldb,
                           (float2*)cc, ldc, ws, ws_bytes, status);
+    case 5:
+      return hg::zgemm_tc(c->st, m, n, k, (double2*)a, lda, (double2*)b, ldb, (double2*)cc, ldc, ws, ws_bytes, status);
   }
   return cudaErrorInvalidValue;
 }
@@ -1851,14 +1860,17 @@ cudaError_t gemm_variant(hg_ctx* c, int variant, int m, int n, int k, void* a, i
 
 int hg_bench_gemm(hg_ctx* c, int precision, int m, int n, int k, int iters, float* ms_per_launch) {
   if (!c) return -1;
-  if (precision < 0 || precision > 4) return fail(c, -2, "precision must be 0..4");
-  if ((precision >= 2) && !hg::cgemm_tc_supported()) return fail(c, -2, "tensor-core GEMM needs an sm_103 device");
+  if (precision < 0 || precision > 5) return fail(c, -2, "precision must be 0..5");
+  if (precision >= 2 && precision <= 4 && !hg::cgemm_tc_supported())
+    return fail(c, -2, "tensor-core GEMM needs an sm_103 device");
+  if (precision == 5 && !hg::zgemm_tc_supported()) return fail(c, -2, "the sliced complex128 GEMM needs an sm_103 device");
   if (m <= 0 || n <= 0 || k <= 0) return fail(c, -3, "bad shape");
   if (iters <= 0) return fail(c, -6, "iters must be positive");
   if (!ms_per_launch) return fail(c, -7, "ms_per_launch is NULL");
   cudaSetDevice(c->o.device);
-  const size_t es = precision ? sizeof(float2) : sizeof(double2);
-  const size_t wsb = precision >= 2 ? hg::cgemm_tc_work_bytes(m, n, k) : 0;
+  const size_t es = (precision == 0 || precision == 5) ? sizeof(double2) : sizeof(float2);
+  const size_t wsb = precision == 5 ? hg::zgemm_tc_work_bytes(m, n, k)
+                                    : (precision >= 2 ? hg::cgemm_tc_work_bytes(m, n, k) : 0);
   void *a = nullptr, *b = nullptr, *cc = nullptr, *ws = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaError_t e = cudaMalloc(&a, (size_t)m * k * es);
@@ -1948,8 +1960,10 @@ int hg_bench_panel(hg_ctx* c, int m, int iters, float* ms_per_launch) {
 int hg_gemm_check(hg_ctx* c, int variant, int m, int n, int k, const double* a, int lda, const double* b, int ldb,
                   double* cm, int ldc) {
   if (!c) return -1;
-  if (variant < 0 || variant > 4) return fail(c, -2, "variant must be 0..4");
-  if (variant >= 2 && !hg::cgemm_tc_supported()) return fail(c, -2, "tensor-core GEMM needs an sm_103 device");
+  if (variant < 0 || variant > 5) return fail(c, -2, "variant must be 0..5");
+  if (variant >= 2 && variant <= 4 && !hg::cgemm_tc_supported())
+    return fail(c, -2, "tensor-core GEMM needs an sm_103 device");
+  if (variant == 5 && !hg::zgemm_tc_supported()) return fail(c, -2, "the sliced complex128 GEMM needs an sm_103 device");
   if (m <= 0 || n <= 0 || k <= 0) return fail(c, -3, "bad shape");
   if (!a || lda < m) return fail(c, -6, "bad a / lda");
   if (!b || ldb < k) return fail(c, -8, "bad b / ldb");
@@ -1967,6 +1981,10 @@ int hg_gemm_check(hg_ctx* c, int variant, int m, int n, int k, const double* a, 
   CK(cudaMemcpyAsync(dc.p, cm, nc * sizeof(double2), cudaMemcpyHostToDevice, c->st));
   if (variant == 0) {
     CK(gemm_variant(c, 0, m, n, k, da.p, lda, db.p, ldb, dc.p, ldc, nullptr, 0, c->status.p));
+  } else if (variant == 5) {
+    const size_t wsb = hg::zgemm_tc_work_bytes(m, n, k);
+    CK(ws.ensure(wsb));
+    CK(gemm_variant(c, 5, m, n, k, da.p, lda, db.p, ldb, dc.p, ldc, ws.p, wsb, c->status.p));
   } else {
     CK(fa.ensure(na));
     CK(fb.ensure(nb));

@@ -476,6 +476,27 @@ size_t lu_work_bytes(int n, int tc_passes) {
   return LuWork(n).total;
 }
 
+// Workspace of the two-level complex128 LU (tensor cores): the sliced GEMM's
+// digits; then for the current outer panel X = L11^-1, M = I - X, Xn = -X and
+// Lf = L11 with its unit diagonal and zeros above (256 x 256 each), and W, a
+// copy of A12 (256 x n) for the refinement of U12.
+struct LuWorkZ {
+  size_t zg, x, m, xn, lf, w, total;
+  explicit LuWorkZ(int n) {
+    auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t blk = up((size_t)kOuterNB * kOuterNB * sizeof(double2));
+    zg = up(zgemm_tc_work_bytes(n, n, kOuterNB));
+    x = zg;
+    m = x + blk;
+    xn = m + blk;
+    lf = xn + blk;
+    w = lf + blk;
+    total = w + up((size_t)kOuterNB * n * sizeof(double2));
+  }
+};
+
+size_t lu_work_bytes_z(int n) { return n < kTcMinN ? 0 : LuWorkZ(n).total; }
+
 namespace {
 
 // LU of the panel rows [k0, n) x columns [k0, k0 + jb) (jb <= 32), pivots
@@ -603,6 +624,70 @@ k_apply_inv(int jb, int nc, const float2* __restrict__ M, const float2* __restri
   if (r0 + rr < jb && c0 + cc < nc) Y[(r0 + rr) + (long)(c0 + cc) * ldy] = acc;
 }
 
+// X <- I (nb x nb, complex128)
+__global__ void k_eye_z(int nb, double2* X, int ldx) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+  if (r < nb) X[r + (long)c * ldx] = make_double2(r == c ? 1.0 : 0.0, 0.0);
+}
+
+// From X = L11^-1: M = I - X, Xn = -X, and Lf = the unit-lower L11 of the
+// factor A11 with zeros above its diagonal (all nb x nb, leading dimension ld).
+__global__ void k_u12_operands(int nb, const double2* __restrict__ X, const double2* __restrict__ A11, long lda,
+                               double2* __restrict__ M, double2* __restrict__ Xn, double2* __restrict__ Lf, int ld) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+  if (r >= nb) return;
+  const long o = r + (long)c * ld;
+  const double2 x = X[o];
+  M[o] = make_double2((r == c ? 1.0 : 0.0) - x.x, -x.y);
+  Xn[o] = make_double2(-x.x, -x.y);
+  Lf[o] = r > c ? A11[r + (long)c * lda] : make_double2(r == c ? 1.0 : 0.0, 0.0);
+}
+
+// Two-level complex128 LU: 256-wide outer panels by the 32-wide loop (FP64
+// pipes), then U12 = L11^-1 A12 and A22 -= L21 U12 as exact BF16 digit
+// products on the tensor cores (zgemm_tc).  U12 from the explicit inverse
+// (X = L11^-1, a column-parallel triangular solve of the identity) with one
+// refinement step, U0 = A12 - (I - X) A12, U12 = U0 + X (A12 - L11 U0): the
+// inverse alone would leave a backward error of cond(L11) eps in U12, the
+// step brings the factorisation's back to that of a triangular solve.
+cudaError_t getrf_z_tc(cudaStream_t st, bool use_cluster, int n, double2* A, long lda, int* ipiv, int* info, void* work,
+                       const LuAux* aux) {
+  const LuWorkZ lw(n);
+  char* wb = static_cast<char*>(work);
+  double2* X = reinterpret_cast<double2*>(wb + lw.x);
+  double2* M = reinterpret_cast<double2*>(wb + lw.m);
+  double2* Xn = reinterpret_cast<double2*>(wb + lw.xn);
+  double2* Lf = reinterpret_cast<double2*>(wb + lw.lf);
+  double2* W = reinterpret_cast<double2*>(wb + lw.w);
+  cudaError_t e = cudaSuccess;
+  for (int K = 0; K < n; K += kOuterNB) {
+    const int jbo = (n - K < kOuterNB) ? n - K : kOuterNB;
+    e = factor_columns<double>(st, use_cluster, n, A, lda, K, K + jbo, ipiv, info, nullptr, aux);
+    if (e != cudaSuccess) return e;
+    k_laswp<double2><<<(n + 127) / 128, 128, 0, st>>>(A, lda, n, ipiv, K, K + jbo, K, K + jbo);
+    const int rest = n - K - jbo;
+    if (rest <= 0) continue;
+    const dim3 eg((jbo + 127) / 128, jbo);
+    double2* A11 = A + K + (long)K * lda;
+    double2* A12 = A + K + (long)(K + jbo) * lda;
+    k_eye_z<<<eg, 128, 0, st>>>(jbo, X, kOuterNB);
+    e = trsm_cols<double>(st, false, A11, lda, jbo, X, kOuterNB, jbo);
+    if (e != cudaSuccess) return e;
+    k_u12_operands<<<eg, 128, 0, st>>>(jbo, X, A11, lda, M, Xn, Lf, kOuterNB);
+    e = cudaMemcpy2DAsync(W, (size_t)kOuterNB * sizeof(double2), A12, (size_t)lda * sizeof(double2),
+                          (size_t)jbo * sizeof(double2), rest, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return e;
+    e = zgemm_tc(st, jbo, rest, jbo, M, kOuterNB, A12, lda, A12, lda, work, lw.zg, info);  // A12 <- U0
+    if (e == cudaSuccess) e = zgemm_tc(st, jbo, rest, jbo, Lf, kOuterNB, A12, lda, W, kOuterNB, work, lw.zg, info);
+    if (e == cudaSuccess) e = zgemm_tc(st, jbo, rest, jbo, Xn, kOuterNB, W, kOuterNB, A12, lda, work, lw.zg, info);
+    if (e != cudaSuccess) return e;
+    e = zgemm_tc(st, rest, rest, jbo, A + (K + jbo) + (long)K * lda, lda, A12, lda, A + (K + jbo) + (long)(K + jbo) * lda,
+                 lda, work, lw.zg, info);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 template <typename R>
@@ -612,6 +697,9 @@ cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* i
   cudaError_t e = cudaMemsetAsync(info, 0, sizeof(int), st);
   if (e != cudaSuccess) return e;
   const bool use_cluster = panel_cluster_supported<R>(n);
+  if (sizeof(R) == 8 && tc_passes != 0 && n >= kTcMinN && work && work_bytes >= lu_work_bytes_z(n) &&
+      zgemm_tc_supported())
+    return getrf_z_tc(st, use_cluster, n, reinterpret_cast<double2*>(A), lda, ipiv, info, work, aux);
   const bool tc = sizeof(R) == 4 && tc_passes != 0 && n >= kTcMinN && work &&
                   work_bytes >= lu_work_bytes(n, tc_passes) && cgemm_tc_supported();
   if (!tc) return factor_columns<R>(st, use_cluster, n, A, lda, 0, n, ipiv, info, nullptr, aux);

@@ -54,11 +54,13 @@ cudaError_t cgemm_skinny(cudaStream_t st, int m, int n, int k, float2 alpha, con
 // In-place LU with partial pivoting of the n x n matrix A (lda).  ipiv is a
 // device array of n 1-based pivot rows, LAPACK style.  info (device int) is
 // set to the first zero pivot (1-based) or left at 0 (a negative value: a
-// bounded device wait ran out).  Complex64 only: tc_passes = 3 or 1 runs the
-// trailing updates of 256-wide outer panels on the tensor cores (cgemm_tc,
-// 3xTF32 or TF32) with work a 256-byte aligned device scratch of at least
-// lu_work_bytes(n, tc_passes) bytes; tc_passes = 0 keeps every update on the
-// SIMT kernels (work unused).
+// bounded device wait ran out).  Complex64: tc_passes = 3, 2 or 1 runs the
+// trailing updates of 256-wide outer panels on the tensor cores (cgemm_tc:
+// 3xTF32, split BF16 or TF32) with work a 256-byte aligned device scratch of
+// at least lu_work_bytes(n, tc_passes) bytes.  Complex128: any tc_passes != 0
+// runs U12 and the trailing updates of 256-wide outer panels as exact BF16
+// digit products (zgemm_tc) with work of at least lu_work_bytes_z(n) bytes.
+// tc_passes = 0 keeps every update on the SIMT kernels (work unused).
 //
 // Look-ahead (aux, optional): a second stream of lower priority and two
 // events.  After each 32-column panel only the next panel's 32 columns are
@@ -80,6 +82,18 @@ cudaError_t getrs(cudaStream_t st, int n, int nrhs, const typename cx<R>::T* LU,
                   typename cx<R>::T* B, long ldb);
 
 size_t lu_work_bytes(int n, int tc_passes);
+size_t lu_work_bytes_z(int n);
+
+// Complex128 C -= A B on the tcgen05 tensor cores, FP64-accurate, by exact
+// BF16 digit slicing of both operands (hg_zgemm_tc.cu): A m x k (lda), B k x n
+// (ldb), C m x n (ldc), column-major; B may alias C (B is sliced before C is
+// written), A may not.  About 2^-48 of each output plus 2^-57 of sum |a||b|.
+// ws: 256-byte aligned device scratch of zgemm_tc_work_bytes(m, n, k) bytes.
+// status (device int) receives -1000 if a bounded wait ran out.
+bool zgemm_tc_supported();
+size_t zgemm_tc_work_bytes(int m, int n, int k);
+cudaError_t zgemm_tc(cudaStream_t st, int m, int n, int k, const double2* A, long lda, const double2* B, long ldb,
+                     double2* C, long ldc, void* ws, size_t ws_bytes, int* status);
 
 // getrs for the complex64 factors of a two-level getrf (tc_passes != 0):
 // uses the inverses of the 256 x 256 diagonal blocks that getrf kept in its

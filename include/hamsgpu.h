@@ -52,7 +52,10 @@ typedef struct {
                             ~2^-16 product error, one refinement sweep at the benchmark
                             configurations; default), 3 = split TF32 (three products,
                             single-precision quality), 1 = TF32 (one product, more refinement
-                            sweeps), 0 = FP32 SIMT kernels only */
+                            sweeps), 0 = FP32 SIMT kernels only.  Plain form, order >= 1024:
+                            any value but 0 runs U12 and the trailing updates of the complex128
+                            LU on the tensor cores as exact BF16 digit products (FP64
+                            accuracy, Ozaki et al. 2012); 0 keeps them on the FP64 pipes */
     int refine_method;   /* mixed form: 0 = classical iterative refinement (x += LU^-1 r per
                             sweep; default), 1 = GMRES-based refinement (restarted GMRES of
                             src/IterativeSolvers.f90:324-488 on A d = r, right-preconditioned by
@@ -350,7 +353,9 @@ int hg_elapsed(hg_ctx *ctx, int slot0, int slot1, float *ms);
  * precision (kernel variant): 0 complex128 SIMT, 1 complex64 SIMT,
  * 2 complex64 tensor cores split TF32 (3 products), 3 complex64 tensor
  * cores TF32 (1 product), 4 complex64 tensor cores split BF16 (3 products
- * at the BF16 rate); 2-4 include their operand packing. */
+ * at the BF16 rate), 5 complex128 tensor cores as exact BF16 digit products
+ * (36 digit pairs, FP64 accuracy); 2-5 include their operand packing or
+ * slicing. */
 int hg_bench_gemm(hg_ctx *ctx, int precision, int m, int n, int k, int iters, float *ms_per_launch);
 
 /* Average device time (ms, CUDA events around each launch) of the
@@ -363,7 +368,7 @@ int hg_bench_panel(hg_ctx *ctx, int m, int iters, float *ms_per_launch);
 
 /* C = C - A B through one of those kernel variants on host arrays (all
  * COMPLEX*16, column-major; variants 1-4 round A, B, C to complex64 on the
- * device and widen the result back).  A test hook for the LU update
+ * device and widen the result back, variants 0 and 5 stay in complex128).  A test hook for the LU update
  * kernels; the reference's counterpart is the ZGEMM step inside ZGETRF. */
 int hg_gemm_check(hg_ctx *ctx, int variant, int m, int n, int k, const double *a, int lda, const double *b,
                   int ldb, double *c, int ldc);
