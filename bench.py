@@ -335,9 +335,21 @@ def ours(args, dist, rank, world, local):
             am, bm, fm, _ = s.solve_frequency(fv, fwk, fw1, -1.0, None, betas)
             e = lambda x, y: float(np.abs(x - y).max() / np.abs(y).max())  # noqa: E731
             errs.append({"A": e(am, a64), "B": e(bm, b64), "F": e(fm, f64)})
+        # the plain form through the sweep's concurrent solve slots, as the mixed form runs
+        nsl = 4
+        v, wk, w1 = inputs(nsl, 0)
+        sp.solve_sweep(v, wk, w1, -1.0, None, betas, nslots=nsl)  # set-up: creates the slots
+        v, wk, w1 = inputs(2 * nsl, nsl)
+        sp.mark(4)
+        sp.solve_sweep(v, wk, w1, -1.0, None, betas, nslots=nsl)
+        sp.mark(5)
+        sweep_ms = sp.elapsed_ms(4, 5)
+        zroof = _gemm_roofline(sp, mesh.n, hg.HG_PREC_FP64, hg, lu_tensor=2)
         sp.close()
         fp64 = {"freq_solves_per_s": 1e3 / statistics.mean(pms), "ms_per_step": statistics.mean(pms),
                 "steps": args.fp64_steps, "slots": 1,
+                "sweep": {"freq_solves_per_s": 2 * nsl / (sweep_ms / 1e3), "frequencies": 2 * nsl, "slots": nsl},
+                "lu_trailing_update": zroof,
                 "mixed_vs_fp64_max_norm_err": {k: max(d[k] for d in errs) for k in ("A", "B", "F")}}
 
     # ---- roofline of the dominant kernel (the LU trailing-update GEMM) ----
@@ -369,7 +381,8 @@ def ours(args, dist, rank, world, local):
             "refine": {"sweeps": sweeps, "residual": resid},
             "e2e": {"value": world * args.steps / t_e2e, "unit": "freq-solves/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
-            "gpu_launches": _launch_count(mesh.n, prec, sweeps) * args.steps if iters is None else None,
+            "gpu_launches": _launch_count(mesh.n, prec, sweeps, lu_tensor=args.lu_tensor) * args.steps
+            if iters is None else None,
             "clocks": clocks, "roofline": roof, "fp64_form": fp64}
     if iters is not None:
         line["iterative"] = {"what": "solver 2 (restarted GMRES(25), tolerance 1e-4), one frequency alone",
@@ -583,10 +596,23 @@ def field_map(args):
     print(json.dumps(line), flush=True)
 
 
-def _launch_count(n, prec, sweeps=1, nd=30, nbeta=8):
+def _launch_count(n, prec, sweeps=1, nd=30, nbeta=8, lu_tensor=2):
     """Kernels the library launches per frequency-solve, from its launch
     sequence (checked against the ncu launch list of one solve)."""
     nb, nbo = 32, 256
+    if prec == 0 and n >= 1024 and lu_tensor != 0:
+        # FP64 form on the tensor cores: each sliced product is 3 kernels (A's digits, B's digits,
+        # the product).  Per outer panel of jbo columns: p = jbo / 32 panels, their interchanges
+        # and L11 solves (when jbo > 32), p - 1 inner products, the other columns' interchanges; where
+        # columns remain: I, L11^-1, the U12 operands, three U12 products and the trailing one.
+        lu = 0
+        for k in range(0, n, nbo):
+            jbo = min(nbo, n - k)
+            p = (jbo + nb - 1) // nb
+            lu += p + (p if jbo > nb else 0) + 3 * (p - 1) + 1 + (15 if n - k - jbo > 0 else 0)
+        blocks = (n + nbo - 1) // nbo
+        getrs = 1 + 2 * blocks + 3 * 2 * (blocks - 1)
+        return 1 + lu + 3 + getrs + 1  # fill, LU, incident / source columns / S W, solves, forces
     def inner(jb, split=False):  # 32-wide panels: panel + fused interchanges / L11 solve, then the update
         p = (jb + nb - 1) // nb   # while columns remain (the FP64 form splits it: next panel's columns, the rest)
         return 2 * p + ((2 * p - 3 if p >= 2 else 0) if split else p - 1)
@@ -672,13 +698,16 @@ def _roofline(s, n, prec, hg, ms_per_step, nd=30, nbeta=8, lu_tensor=2):
 
 def _gemm_roofline(s, n, prec, hg, lu_tensor=2):
     """Roofline of the LU trailing update, the path's dense contraction: the
-    library's tcgen05 GEMM (mixed form, the variant lu_tensor selects) or its
-    complex128 SIMT GEMM (FP64 form), timed with CUDA events on the library's
-    stream at the shape of the first 256-wide outer panel (m = n = N - 256,
-    k = 256)."""
+    library's tcgen05 GEMM (mixed form, the variant lu_tensor selects; FP64
+    form: the exact digit-sliced complex128 product, or the SIMT GEMM with
+    lu_tensor 0), timed with CUDA events on the library's stream at the shape
+    of the first 256-wide outer panel (m = n = N - 256, k = 256)."""
     m, k = n - 256, 256
-    # hg_bench_gemm variants: 2 split TF32, 3 TF32, 4 split BF16
-    variant = {3: 2, 1: 3, 2: 4}.get(lu_tensor, 1) if prec == hg.HG_PREC_MIXED else 0
+    # hg_bench_gemm variants: 2 split TF32, 3 TF32, 4 split BF16, 5 complex128 digit slices
+    if prec == hg.HG_PREC_MIXED:
+        variant = {3: 2, 1: 3, 2: 4}.get(lu_tensor, 1)
+    else:
+        variant = 5 if lu_tensor != 0 else 0
     try:
         ms = s.bench_gemm(variant, m, m, k, iters=10)
     except Exception:
@@ -691,7 +720,8 @@ def _gemm_roofline(s, n, prec, hg, lu_tensor=2):
              3: "k_cgemm_tc<1> (LU trailing update A22 -= L21 U12, complex64, tcgen05 TF32)",
              4: "k_cgemm_tc<2> (LU trailing update A22 -= L21 U12, complex64, tcgen05 split BF16)",
              1: "k_cgemm_wide (LU trailing update, complex64 SIMT)",
-             0: "k_gemm<double> (LU trailing update, complex128 SIMT)"}
+             0: "k_gemm<double> (LU trailing update, complex128 SIMT)",
+             5: "k_zoz_gemm (LU trailing update A22 -= L21 U12, complex128, tcgen05 exact BF16 digit products)"}
     out = {"kernel": names[variant],
            "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
            "peak_source": f"bf16_tflops of {kind} peaks", "flops_per_launch": flops, "ms_per_launch": ms,
@@ -702,6 +732,12 @@ def _gemm_roofline(s, n, prec, hg, lu_tensor=2):
         out["note"] = ("algorithmic complex flops; the hardware does 3 BF16 products per real product at the bf16 "
                        "rate, so the tensor-pipe utilisation is about 3 x frac (ncu: 44.5 % tensor-pipe activity "
                        "at this shape)")
+    if variant == 5:
+        out["note"] = ("algorithmic complex flops of an FP64-accurate product; the hardware does 36 BF16 digit "
+                       "products (the digit pairs s + t <= 9 of eight 7-bit digits per operand) per real product "
+                       "at the bf16 rate, so the tensor-pipe work is 36 x frac of the bf16 peak; includes the "
+                       "two slicing kernels")
+        out["bf16_equivalent_frac"] = 36 * achieved / peak
     if variant == 2:
         # DRAM bytes of one launch of this shape (5792 x 5792 x 256) from the committed ncu capture
         out["traffic"] = (486.998528 + 235.5008) * 1e6 if n == 6048 else None
