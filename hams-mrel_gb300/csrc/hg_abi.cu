@@ -771,11 +771,11 @@ int solve_cols_once(hg_ctx* c, int c0, int c1) {
   if (!mixed(c)) {
     if (c->irsp == 1) {
       CK(hg::gemm<double>(c->st, true, n, nc, tn, one, c->A.p, tn, Bc, tn, zero, Xc, n, WS(c)));
-      CK(hg::getrs<double>(c->st, n, nc, c->C.p, n, c->ipiv.p, Xc, n));
+      CK(hg::getrs<double>(c->st, n, nc, c->C.p, n, c->ipiv.p, Xc, n, c->luws.p, c->luws.cap, c->status.p));
     } else {
       CK(cudaMemcpy2DAsync(Xc, (size_t)n * sizeof(double2), Bc, (size_t)tn * sizeof(double2), (size_t)n * sizeof(double2),
                            nc, cudaMemcpyDeviceToDevice, c->st));
-      CK(hg::getrs<double>(c->st, n, nc, c->A.p, tn, c->ipiv.p, Xc, n));
+      CK(hg::getrs<double>(c->st, n, nc, c->A.p, tn, c->ipiv.p, Xc, n, c->luws.p, c->luws.cap, c->status.p));
     }
     c->sweeps = 0;
     c->resid = 0.0;
@@ -1816,7 +1816,8 @@ int hg_gesv(hg_ctx* c, int precision, int n, int nrhs, double* a, int lda, int* 
     CK(cudaMemcpyAsync(&inf, dinfo.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
     if (inf < 0) return fail(c, HG_ERR_DEVICE, "LU panel: a bounded cluster wait ran out (info %d)", inf);
-    if (inf == 0 && nrhs > 0) CK(hg::getrs<double>(c->st, n, nrhs, dA.p, n, dpiv.p, dB.p, n));
+    if (inf == 0 && nrhs > 0)
+      CK(hg::getrs<double>(c->st, n, nrhs, dA.p, n, dpiv.p, dB.p, n, luws.p, luws.cap, c->status.p));
     result = dB.p;
   }
   CK(cudaMemcpy2DAsync(a, (size_t)lda * sizeof(double2), dA.p, (size_t)n * sizeof(double2), (size_t)n * sizeof(double2),

@@ -512,9 +512,12 @@ cudaError_t panel(cudaStream_t st, bool use_cluster, int n, typename cx<R>::T* A
 // Columns [c0, c1) of A through one level of right-looking blocking with
 // 32-wide panels (pivots applied only inside [c0, c1)).  With aux, the
 // update of the columns beyond the next panel runs on aux->side (see getrf).
+// Complex128 with zws (zgemm_tc_work_bytes of the update): each update is one
+// sliced product on the tensor cores, on st.
 template <typename R>
 cudaError_t factor_columns(cudaStream_t st, bool use_cluster, int n, typename cx<R>::T* A, long lda, int c0, int c1,
-                           int* ipiv, int* info, int* perm = nullptr, const LuAux* aux = nullptr) {
+                           int* ipiv, int* info, int* perm = nullptr, const LuAux* aux = nullptr, void* zws = nullptr,
+                           size_t zws_bytes = 0) {
   typedef typename cx<R>::T T;
   T mone, one;
   mone.x = -1; mone.y = 0; one.x = 1; one.y = 0;
@@ -538,7 +541,11 @@ cudaError_t factor_columns(cudaStream_t st, bool use_cluster, int n, typename cx
     const T* L21 = A + (k + jb) + (long)k * lda;
     const T* U12 = A + k + (long)(k + jb) * lda;
     T* A22 = A + (k + jb) + (long)(k + jb) * lda;
-    if (aux && rest > kNB) {
+    if (sizeof(R) == 8 && zws) {
+      e = zgemm_tc(st, m, rest, jb, reinterpret_cast<const double2*>(L21), lda, reinterpret_cast<const double2*>(U12), lda,
+                   reinterpret_cast<double2*>(A22), lda, zws, zws_bytes, info);
+      if (e != cudaSuccess) return e;
+    } else if (aux && rest > kNB) {
       // the next panel's columns here, the others on the side stream
       e = gemm<R>(st, false, m, kNB, jb, mone, L21, lda, U12, lda, one, A22, lda);
       if (e == cudaSuccess) e = cudaEventRecord(aux->ev_main, st);
@@ -643,9 +650,10 @@ __global__ void k_u12_operands(int nb, const double2* __restrict__ X, const doub
   Lf[o] = r > c ? A11[r + (long)c * lda] : make_double2(r == c ? 1.0 : 0.0, 0.0);
 }
 
-// Two-level complex128 LU: 256-wide outer panels by the 32-wide loop (FP64
-// pipes), then U12 = L11^-1 A12 and A22 -= L21 U12 as exact BF16 digit
-// products on the tensor cores (zgemm_tc).  U12 from the explicit inverse
+// Two-level complex128 LU: 256-wide outer panels by the 32-wide loop (panels
+// on the FP64 pipes, their updates inside the outer panel on the tensor
+// cores), then U12 = L11^-1 A12 and A22 -= L21 U12, all products as exact
+// BF16 digit products (zgemm_tc).  U12 from the explicit inverse
 // (X = L11^-1, a column-parallel triangular solve of the identity) with one
 // refinement step, U0 = A12 - (I - X) A12, U12 = U0 + X (A12 - L11 U0): the
 // inverse alone would leave a backward error of cond(L11) eps in U12, the
@@ -662,7 +670,7 @@ cudaError_t getrf_z_tc(cudaStream_t st, bool use_cluster, int n, double2* A, lon
   cudaError_t e = cudaSuccess;
   for (int K = 0; K < n; K += kOuterNB) {
     const int jbo = (n - K < kOuterNB) ? n - K : kOuterNB;
-    e = factor_columns<double>(st, use_cluster, n, A, lda, K, K + jbo, ipiv, info, nullptr, aux);
+    e = factor_columns<double>(st, use_cluster, n, A, lda, K, K + jbo, ipiv, info, nullptr, aux, work, lw.zg);
     if (e != cudaSuccess) return e;
     k_laswp<double2><<<(n + 127) / 128, 128, 0, st>>>(A, lda, n, ipiv, K, K + jbo, K, K + jbo);
     const int rest = n - K - jbo;
@@ -799,10 +807,19 @@ cudaError_t getrs_inv(cudaStream_t st, int n, int nrhs, const float2* LU, long l
 
 template <typename R>
 cudaError_t getrs(cudaStream_t st, int n, int nrhs, const typename cx<R>::T* LU, long lda, const int* ipiv,
-                  typename cx<R>::T* B, long ldb) {
+                  typename cx<R>::T* B, long ldb, void* work, size_t work_bytes, int* status) {
   typedef typename cx<R>::T T;
   T mone, one;
   mone.x = -1; mone.y = 0; one.x = 1; one.y = 0;
+  // complex128 block updates as exact digit products on the tensor cores
+  const bool ztc = sizeof(R) == 8 && work && status && n > kSolveNB &&
+                   work_bytes >= zgemm_tc_work_bytes(n, nrhs, kSolveNB) && zgemm_tc_supported();
+  auto update = [&](int m, int kk, const T* A_, const T* X_, T* C_) -> cudaError_t {
+    if (ztc)
+      return zgemm_tc(st, m, nrhs, kk, reinterpret_cast<const double2*>(A_), lda, reinterpret_cast<const double2*>(X_),
+                      ldb, reinterpret_cast<double2*>(C_), ldb, work, work_bytes, status);
+    return gemm<R>(st, false, m, nrhs, kk, mone, A_, lda, X_, ldb, one, C_, ldb);
+  };
   k_laswp<T><<<(nrhs + 127) / 128, 128, 0, st>>>(B, ldb, nrhs, ipiv, 0, n, 0, 0);
   for (int k = 0; k < n; k += kSolveNB) {
     const int jb = (n - k < kSolveNB) ? n - k : kSolveNB;
@@ -810,7 +827,7 @@ cudaError_t getrs(cudaStream_t st, int n, int nrhs, const typename cx<R>::T* LU,
     if (e != cudaSuccess) return e;
     const int rest = n - k - jb;
     if (rest > 0) {
-      e = gemm<R>(st, false, rest, nrhs, jb, mone, LU + (k + jb) + (long)k * lda, lda, B + k, ldb, one, B + k + jb, ldb);
+      e = update(rest, jb, LU + (k + jb) + (long)k * lda, B + k, B + k + jb);
       if (e != cudaSuccess) return e;
     }
   }
@@ -820,7 +837,7 @@ cudaError_t getrs(cudaStream_t st, int n, int nrhs, const typename cx<R>::T* LU,
     cudaError_t e = trsm_cols<R>(st, true, LU + k + (long)k * lda, lda, jb, B + k, ldb, nrhs);
     if (e != cudaSuccess) return e;
     if (k > 0) {
-      e = gemm<R>(st, false, k, nrhs, jb, mone, LU + (long)k * lda, lda, B + k, ldb, one, B, ldb);
+      e = update(k, jb, LU + (long)k * lda, B + k, B);
       if (e != cudaSuccess) return e;
     }
   }
@@ -829,8 +846,10 @@ cudaError_t getrs(cudaStream_t st, int n, int nrhs, const typename cx<R>::T* LU,
 
 template cudaError_t getrf<double>(cudaStream_t, int, double2*, long, int*, int*, void*, size_t, int, const LuAux*);
 template cudaError_t getrf<float>(cudaStream_t, int, float2*, long, int*, int*, void*, size_t, int, const LuAux*);
-template cudaError_t getrs<double>(cudaStream_t, int, int, const double2*, long, const int*, double2*, long);
-template cudaError_t getrs<float>(cudaStream_t, int, int, const float2*, long, const int*, float2*, long);
+template cudaError_t getrs<double>(cudaStream_t, int, int, const double2*, long, const int*, double2*, long, void*,
+                                   size_t, int*);
+template cudaError_t getrs<float>(cudaStream_t, int, int, const float2*, long, const int*, float2*, long, void*,
+                                  size_t, int*);
 
 // ------------------------------------------------------------------------
 // conversions

@@ -77,9 +77,12 @@ cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* i
                   size_t work_bytes = 0, int tc_passes = 0, const LuAux* aux = nullptr);
 
 // Solve A X = B with the factors of getrf; B is n x nrhs (ldb), overwritten.
+// Complex128 with work (256-byte aligned, at least zgemm_tc_work_bytes(n,
+// nrhs, 256) bytes) and a device status word: the block updates run as exact
+// digit products on the tensor cores (zgemm_tc); otherwise on the SIMT GEMM.
 template <typename R>
 cudaError_t getrs(cudaStream_t st, int n, int nrhs, const typename cx<R>::T* LU, long lda, const int* ipiv,
-                  typename cx<R>::T* B, long ldb);
+                  typename cx<R>::T* B, long ldb, void* work = nullptr, size_t work_bytes = 0, int* status = nullptr);
 
 size_t lu_work_bytes(int n, int tc_passes);
 size_t lu_work_bytes_z(int n);
