@@ -602,14 +602,14 @@ def _launch_count(n, prec, sweeps=1, nd=30, nbeta=8, lu_tensor=2):
     nb, nbo = 32, 256
     if prec == 0 and n >= 1024 and lu_tensor != 0:
         # FP64 form on the tensor cores: each sliced product is 3 kernels (A's digits, B's digits,
-        # the product).  Per outer panel of jbo columns: p = jbo / 32 panels, their interchanges
-        # and L11 solves (when jbo > 32), p - 1 inner products, the other columns' interchanges; where
+        # the product).  Per outer panel of jbo columns: p = jbo / 16 panels, their interchanges
+        # and L11 solves (when jbo > 16), p - 1 inner products, the other columns' interchanges; where
         # columns remain: I, L11^-1, the U12 operands, three U12 products and the trailing one.
         lu = 0
         for k in range(0, n, nbo):
             jbo = min(nbo, n - k)
-            p = (jbo + nb - 1) // nb
-            lu += p + (p if jbo > nb else 0) + 3 * (p - 1) + 1 + (15 if n - k - jbo > 0 else 0)
+            p = (jbo + 15) // 16
+            lu += p + (p if jbo > 16 else 0) + 3 * (p - 1) + 1 + (15 if n - k - jbo > 0 else 0)
         blocks = (n + nbo - 1) // nbo
         getrs = 1 + 2 * blocks + 3 * 2 * (blocks - 1)
         return 1 + lu + 3 + getrs + 1  # fill, LU, incident / source columns / S W, solves, forces

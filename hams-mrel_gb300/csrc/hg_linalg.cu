@@ -523,8 +523,12 @@ cudaError_t factor_columns(cudaStream_t st, bool use_cluster, int n, typename cx
   mone.x = -1; mone.y = 0; one.x = 1; one.y = 0;
   bool side_pending = false;
   cudaError_t e = cudaSuccess;
-  for (int k = c0; k < c1; k += kNB) {
-    const int jb = (c1 - k < kNB) ? c1 - k : kNB;
+  // complex128 on the tensor cores: 16-wide panels (their FP64 rank-1
+  // updates, the panel's bound, are half those of 32-wide ones; the updates
+  // between panels are tensor-core products either way)
+  const int nbp = (sizeof(R) == 8 && zws) ? kNB / 2 : kNB;
+  for (int k = c0; k < c1; k += nbp) {
+    const int jb = (c1 - k < nbp) ? c1 - k : nbp;
     e = panel<R>(st, use_cluster, n, A, lda, k, jb, ipiv, info);
     if (e != cudaSuccess) return e;
     // the interchanges touch every other column of [c0, c1): the side update must be done

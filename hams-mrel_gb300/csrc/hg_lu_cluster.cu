@@ -85,6 +85,7 @@ k_getf2_cluster(typename cx<R>::T* __restrict__ P, long lda, int m, int jb, int 
   __shared__ int red_i[kWarps];
   __shared__ T s_cand[kClusterCTAs][kClusterNB];
   __shared__ T s_jrow[kClusterNB];
+  __shared__ T s_rp;  // the pivot's reciprocal, computed once per column
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int r0 = rank * rpc;
   const int rl = max(0, min(rpc, m - r0));
@@ -155,8 +156,11 @@ k_getf2_cluster(typename cx<R>::T* __restrict__ P, long lda, int m, int jb, int 
     pmax = __shfl_sync(0xffffffffu, pmax, 0);
     p = __shfl_sync(0xffffffffu, p, 0);
     if (p == INT_MAX) p = jj;
-    __syncthreads();  // s_cand and s_jrow complete
     const int op = p / rpc;
+    // one thread forms the pivot's reciprocal (in double precision three
+    // divisions, each a long FP64-pipe sequence, so not once per thread)
+    if (tid == 0 && pmax > 0) s_rp = c_recip(*cluster.map_shared_rank(&pub_row[q][jj], op));
+    __syncthreads();  // s_cand, s_jrow and s_rp complete
     const bool swap = pmax > 0 && p != jj;
     const T* prow = s_cand[op];
     if (rank == 0 && tid == 0) {
@@ -167,20 +171,32 @@ k_getf2_cluster(typename cx<R>::T* __restrict__ P, long lda, int m, int jb, int 
     if (swap && rank == oj && tid < jb) tile[tid * rpc + lj] = prow[tid];
     // (d) scale below the pivot and update; the owner of row p takes old row jj
     if (pmax > 0) {
-      const T rp = c_recip(prow[jj]);
+      const T rp = s_rp;
       for (int r = tid; r < rl; r += blockDim.x) {
         const int gr = r0 + r;
-        if (gr > jj) {
-          const bool moved = swap && gr == p;
-          T l = moved ? s_jrow[jj] : tile[jj * rpc + r];
-          l = c_mul(l, rp);
-          tile[jj * rpc + r] = l;
-          for (int c = jj + 1; c < jb; ++c) {
-            const T a = moved ? s_jrow[c] : tile[c * rpc + r];
-            tile[c * rpc + r] = c_sub(a, c_mul(l, prow[c]));
+        if (gr <= jj) continue;
+        if (swap && gr == p)
+          for (int c = 0; c < jb; ++c) tile[c * rpc + r] = s_jrow[c];
+        const T l = c_mul(tile[jj * rpc + r], rp);
+        tile[jj * rpc + r] = l;
+        // the rank-1 update in chunks of 8 columns with compile-time indices,
+        // the chunk's loads issued back to back
+#pragma unroll
+        for (int c0 = 0; c0 < kClusterNB; c0 += 8) {
+          if (c0 + 8 <= jj + 1 || c0 >= jb) continue;
+          T u[8], a[8];
+#pragma unroll
+          for (int t = 0; t < 8; ++t) {
+            const int c = c0 + t;
+            if (c > jj && c < jb) {
+              u[t] = prow[c];
+              a[t] = tile[c * rpc + r];
+            }
           }
-          if (moved) {
-            for (int c = 0; c < jj; ++c) tile[c * rpc + r] = s_jrow[c];
+#pragma unroll
+          for (int t = 0; t < 8; ++t) {
+            const int c = c0 + t;
+            if (c > jj && c < jb) tile[c * rpc + r] = c_sub(a[t], c_mul(l, u[t]));
           }
         }
       }

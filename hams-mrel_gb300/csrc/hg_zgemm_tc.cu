@@ -112,6 +112,15 @@ __device__ __forceinline__ void oz_digits_d(double v, int e, uint16_t (&d)[kZD])
   d[0] = oz_bf16_int((int)X);
 }
 
+// v 2^sc for a double v: the exponent field moved by integer addition while
+// the result stays normal (exact), ldexp otherwise.
+__device__ __forceinline__ double oz_scale2(double v, int sc) {
+  const long long b = __double_as_longlong(v);
+  const int ef = (int)((b >> 52) & 0x7FF);
+  if (ef != 0 && ef + sc > 0 && ef + sc < 0x7FF) return __longlong_as_double(b + ((long long)sc << 52));
+  return ldexp(v, sc);
+}
+
 // A's digits: [kZD][mp][kp] BF16 rows (K fastest), row i holding Ar(i, :) at
 // 0..k-1 and Ai(i, :) at k..2k-1, zero beyond (rows m..mp-1, K 2k..kp-1);
 // ex[i] the row's exponent.  One CTA per 32 rows: their largest entries
@@ -359,8 +368,9 @@ k_zoz_gemm(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUten
       oz_fence_before();
       __syncwarp();
       if (lane == 0) oz_arrive(&tempty);  // the next tile's MMAs may start
-      // C -= 2^(e_i + f_j) (T_hi 2^-35 + T_lo 2^-63): the product rounded once
-      // into double precision, then the subtraction
+      // C -= 2^(e_i + f_j - 35) (T_hi + T_lo 2^-28): both words exact in double
+      // precision (|T| < 2^46), one rounding of their sum by an FMA, the power
+      // of two by the exponent field, one rounding of the subtraction
       const int row = row0 + qd * 32 + lane;
       if (row < m) {
         const int e = ex[row];
@@ -369,12 +379,11 @@ k_zoz_gemm(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUten
         for (int c = 0; c < kZEpiCols / 2; ++c) {
           const int jc = jc0 + c;
           if (jc >= n) break;
-          const int sc = e + fx[jc];
-          const double s_hi = ldexp(1.0, sc - 35), s_lo = ldexp(1.0, sc - 63);
+          const int sc = e + fx[jc] - 35;
           double2* p = C + row + (long)jc * ldc;
           double2 cv = *p;
-          cv.x -= fma((double)tl[2 * c], s_lo, (double)th[2 * c] * s_hi);
-          cv.y -= fma((double)tl[2 * c + 1], s_lo, (double)th[2 * c + 1] * s_hi);
+          cv.x -= oz_scale2(fma((double)tl[2 * c], 0x1p-28, (double)th[2 * c]), sc);
+          cv.y -= oz_scale2(fma((double)tl[2 * c + 1], 0x1p-28, (double)th[2 * c + 1]), sc);
           *p = cv;
         }
       }
