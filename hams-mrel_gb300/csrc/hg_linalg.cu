@@ -708,10 +708,11 @@ cudaError_t getrf(cudaStream_t st, int n, typename cx<R>::T* A, long lda, int* i
   if (aux && (!aux->side || !aux->ev_main || !aux->ev_side)) aux = nullptr;
   cudaError_t e = cudaMemsetAsync(info, 0, sizeof(int), st);
   if (e != cudaSuccess) return e;
-  const bool use_cluster = panel_cluster_supported<R>(n);
   if (sizeof(R) == 8 && tc_passes != 0 && n >= kTcMinN && work && work_bytes >= lu_work_bytes_z(n) &&
       zgemm_tc_supported())
-    return getrf_z_tc(st, use_cluster, n, reinterpret_cast<double2*>(A), lda, ipiv, info, work, aux);
+    return getrf_z_tc(st, panel_cluster_supported<R>(n, kNB / 2), n, reinterpret_cast<double2*>(A), lda, ipiv, info,
+                      work, aux);
+  const bool use_cluster = panel_cluster_supported<R>(n);
   const bool tc = sizeof(R) == 4 && tc_passes != 0 && n >= kTcMinN && work &&
                   work_bytes >= lu_work_bytes(n, tc_passes) && cgemm_tc_supported();
   if (!tc) return factor_columns<R>(st, use_cluster, n, A, lda, 0, n, ipiv, info, nullptr, aux);

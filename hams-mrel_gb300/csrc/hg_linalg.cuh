@@ -123,8 +123,9 @@ template <>
 cudaError_t panel_cluster<float>(cudaStream_t st, float2* P, long lda, int m, int jb, int* ipiv, int k0, int* info);
 template <>
 cudaError_t panel_cluster<double>(cudaStream_t st, double2* P, long lda, int m, int jb, int* ipiv, int k0, int* info);
+// Whether the cluster panel runs here for m rows and panels of jb columns.
 template <typename R>
-bool panel_cluster_supported(int m);
+bool panel_cluster_supported(int m, int jb = 32);
 // Column-parallel triangular solve of a jb <= 256 diagonal block for ncols columns.
 template <typename R>
 cudaError_t trsm_cols(cudaStream_t st, bool upper, const typename cx<R>::T* A, long lda, int jb,

@@ -15,9 +15,11 @@
 // the steps unrolled so that every register index is a compile-time
 // constant, and per column one 528-byte message (candidate row, row jj,
 // the candidate's reciprocal) pushed to every CTA by bulk copy.  Taller
-// complex64 panels keep the rows in shared memory (k_getf2_cluster_push),
-// FP64 panels use the loading form (k_getf2_cluster).  The two complex64
-// forms give bitwise-equal factors and pivots.
+// complex64 panels keep the rows in shared memory (k_getf2_cluster_push).
+// FP64 panels of at most 16 columns take the same pushed exchange
+// (k_getf2_cluster_push_z), wider or taller ones the loading form
+// (k_getf2_cluster).  The two complex64 forms give bitwise-equal factors and
+// pivots.
 #include <mutex>
 #include <climits>
 #include <cooperative_groups.h>
@@ -402,6 +404,175 @@ k_getf2_cluster_push(float2* __restrict__ P, long lda, int m, int jb, int rpc, i
   cluster.sync();  // no CTA leaves while a copy into its shared memory could be pending
 }
 
+// Complex128 panel with pushed candidates, at most 16 columns (the width of
+// the complex128 LU's panels when its updates run on the tensor cores): the
+// exchange of k_getf2_cluster_push (per column one message per CTA, sent by
+// 16 bulk copies, a bounded mbarrier wait; no cluster barrier and no remote
+// loads per column) with the arithmetic of k_getf2_cluster<double>.  The
+// message also carries the reciprocal of the candidate's entry in column jj,
+// formed once by its sender (three FP64 divisions).  Reuse of the two message
+// slots is safe for the reasons given above.
+constexpr int kPanelNBZ = 16;
+struct __align__(16) PanelMsgZ {
+  double val;
+  int idx;
+  int pad;
+  double2 rcp;
+  double2 cand[kPanelNBZ];
+  double2 jrow[kPanelNBZ];
+};
+static_assert(sizeof(PanelMsgZ) % 16 == 0, "bulk copies move multiples of 16 bytes");
+
+// warp_best for double values: the non-negative doubles' 64-bit patterns
+// (plus one, 0 = none) reduced as two 32-bit halves, then the smallest row
+// among the lanes holding the largest key.
+__device__ __forceinline__ void warp_best_z(double& v, int& idx) {
+  const unsigned long long key = (v >= 0.0) ? (unsigned long long)__double_as_longlong(v) + 1ull : 0ull;
+  const unsigned hi = (unsigned)(key >> 32), lo = (unsigned)(key & 0xffffffffull);
+  const unsigned hm = __reduce_max_sync(0xffffffffu, hi);
+  const unsigned lm = __reduce_max_sync(0xffffffffu, hi == hm ? lo : 0u);
+  const unsigned im = __reduce_min_sync(0xffffffffu, (hi == hm && lo == lm) ? (unsigned)idx : 0xffffffffu);
+  const unsigned long long km = ((unsigned long long)hm << 32) | lm;
+  idx = (km == 0ull) ? INT_MAX : (int)im;
+  v = (km == 0ull) ? -1.0 : __longlong_as_double((long long)(km - 1ull));
+}
+
+__global__ void __launch_bounds__(kClusterThreads, 1)
+k_getf2_cluster_push_z(double2* __restrict__ P, long lda, int m, int jb, int rpc, int* __restrict__ ipiv, int k0,
+                       int* __restrict__ info) {
+  constexpr int kWarps = kClusterThreads / 32;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* tile = reinterpret_cast<double2*>(smem_raw);  // [jb][rpc], row index fastest
+  __shared__ PanelMsgZ sendbuf[2];
+  __shared__ PanelMsgZ recv[2][kClusterCTAs];
+  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ double red_v[kWarps];
+  __shared__ int red_i[kWarps];
+  __shared__ int s_bad;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int r0 = rank * rpc;
+  const int rl = max(0, min(rpc, m - r0));
+  constexpr uint32_t kMsgBytes = sizeof(PanelMsgZ);
+
+  for (int e = tid; e < rl * jb; e += blockDim.x) {
+    const int r = e % rl, c = e / rl;
+    tile[c * rpc + r] = P[(r0 + r) + (long)c * lda];
+  }
+  if (tid == 0) {
+    s_bad = 0;
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    mbar_expect_tx(&mbar[0], kClusterCTAs * kMsgBytes);
+    if (jb > 1) mbar_expect_tx(&mbar[1], kClusterCTAs * kMsgBytes);
+  }
+  cluster.sync();  // barriers initialised and armed everywhere before any copy
+
+  bool bad = false;
+  for (int jj = 0; jj < jb; ++jj) {
+    const int q = jj & 1;
+    const int oj = jj / rpc, lj = jj - oj * rpc;
+    // (a) this CTA's candidate for column jj (rows >= jj): |re| + |im|, first row on ties
+    double v = -1.0;
+    int idx = INT_MAX;
+    for (int r = tid; r < rl; r += blockDim.x) {
+      if (r0 + r >= jj) {
+        const double2 a = tile[jj * rpc + r];
+        const double av = fabs(a.x) + fabs(a.y);
+        if (av > v || (av == v && r0 + r < idx)) { v = av; idx = r0 + r; }
+      }
+    }
+    warp_best_z(v, idx);
+    if (lane == 0) { red_v[warp] = v; red_i[warp] = idx; }
+    __syncthreads();  // also orders every thread's column jj - 1 updates before the copies below
+    if (warp == 0) {
+      v = (lane < kWarps) ? red_v[lane] : -1.0;
+      idx = (lane < kWarps) ? red_i[lane] : INT_MAX;
+      warp_best_z(v, idx);
+      // (b) pack and push the message
+      PanelMsgZ& msg = sendbuf[q];
+      if (lane == 0) {
+        msg.val = v;
+        msg.idx = idx;
+        if (v > 0.0) msg.rcp = c_recip(tile[jj * rpc + (idx - r0)]);
+      }
+      if (lane < jb) {
+        if (idx != INT_MAX) msg.cand[lane] = tile[lane * rpc + (idx - r0)];
+        if (rank == oj) msg.jrow[lane] = tile[lane * rpc + lj];
+      }
+      fence_proxy_async_smem();
+      __syncwarp();
+      if (lane < kClusterCTAs) {
+        const uint32_t dst = mapa_shared(smem_addr(&recv[q][rank]), lane);
+        const uint32_t bar = mapa_shared(smem_addr(&mbar[q]), lane);
+        bulk_s2s_cluster(dst, smem_addr(&msg), kMsgBytes, bar);
+      }
+    }
+    // (c) wait for the 16 messages of this column
+    if (!mbar_wait_timed(&mbar[q], (jj >> 1) & 1, kPanelWaitNs)) bad = true;
+    if (__syncthreads_or(bad)) {
+      if (tid == 0) s_bad = 1;
+      break;
+    }
+    if (tid == 0 && jj + 2 < jb) mbar_expect_tx(&mbar[q], kClusterCTAs * kMsgBytes);
+    // (d) the pivot: every warp reduces the 16 local messages
+    double pmax = (lane < kClusterCTAs) ? recv[q][lane].val : -1.0;
+    int p = (lane < kClusterCTAs) ? recv[q][lane].idx : INT_MAX;
+    warp_best_z(pmax, p);
+    if (p == INT_MAX) p = jj;
+    const int op = p / rpc;
+    const double2* prow = recv[q][op].cand;
+    const double2* jrow = recv[q][oj].jrow;
+    const bool swap = pmax > 0.0 && p != jj;
+    if (rank == 0 && tid == 0) {
+      ipiv[k0 + jj] = k0 + p + 1;
+      if (!(pmax > 0.0) && *info == 0) *info = k0 + jj + 1;
+    }
+    // (e) row jj becomes the pivot row; the owner of row p takes old row jj
+    if (swap && rank == oj && tid < jb) tile[tid * rpc + lj] = prow[tid];
+    if (pmax > 0.0) {
+      const double2 rp = recv[q][op].rcp;
+      for (int r = tid; r < rl; r += blockDim.x) {
+        const int gr = r0 + r;
+        if (gr <= jj) continue;
+        if (swap && gr == p)
+          for (int c = 0; c < jb; ++c) tile[c * rpc + r] = jrow[c];
+        const double2 l = c_mul(tile[jj * rpc + r], rp);
+        tile[jj * rpc + r] = l;
+#pragma unroll
+        for (int c0 = 0; c0 < kPanelNBZ; c0 += 8) {
+          if (c0 + 8 <= jj + 1 || c0 >= jb) continue;
+          double2 u[8], a[8];
+#pragma unroll
+          for (int t = 0; t < 8; ++t) {
+            const int c = c0 + t;
+            if (c > jj && c < jb) {
+              u[t] = prow[c];
+              a[t] = tile[c * rpc + r];
+            }
+          }
+#pragma unroll
+          for (int t = 0; t < 8; ++t) {
+            const int c = c0 + t;
+            if (c > jj && c < jb) tile[c * rpc + r] = c_sub(a[t], c_mul(l, u[t]));
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (s_bad) {
+    if (rank == 0 && tid == 0) *info = kPanelTimeout;
+  } else {
+    for (int e = tid; e < rl * jb; e += blockDim.x) {
+      const int r = e % rl, c = e / rl;
+      P[(r0 + r) + (long)c * lda] = tile[c * rpc + r];
+    }
+  }
+  cluster.sync();  // no CTA leaves while a copy into its shared memory could be pending
+}
+
 // Register-resident form of the pushed-candidate panel, for panels of at
 // most 512 rows per CTA: each thread keeps its one row of the panel (32
 // complex values) in registers for all 32 column steps.  The shared-memory
@@ -668,23 +839,46 @@ cudaError_t panel_cluster<float>(cudaStream_t st, float2* P, long lda, int m, in
   cfg.numAttrs = 1;
   return cudaLaunchKernelEx(&cfg, k_getf2_cluster_push, P, lda, m, jb, rpc, ipiv, k0, info);
 }
+// Double precision: the pushed-candidate panel for panels of at most 16
+// columns whose tile fits beside its message buffers, else the loading panel.
 template <>
 cudaError_t panel_cluster<double>(cudaStream_t st, double2* P, long lda, int m, int jb, int* ipiv, int k0,
                                   int* info) {
-  return panel_cluster_smem<double>(st, P, lda, m, jb, ipiv, k0, info);
+  const int rpc = (m + kClusterCTAs - 1) / kClusterCTAs;
+  const size_t smem = (size_t)rpc * jb * sizeof(double2);
+  if (jb > kPanelNBZ || smem > (size_t)(kPanelSmemMax - kPushStaticSmem))
+    return panel_cluster_smem<double>(st, P, lda, m, jb, ipiv, k0, info);
+  cudaError_t e = cudaFuncSetAttribute(k_getf2_cluster_push_z, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_getf2_cluster_push_z, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kPanelSmemMax - kPushStaticSmem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kClusterCTAs, 1, 1);
+  cfg.blockDim = dim3(kClusterThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kClusterCTAs;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_getf2_cluster_push_z, P, lda, m, jb, rpc, ipiv, k0, info);
 }
 
 
 // Whether a 16-CTA cluster with the given dynamic shared memory can run here.
 template <typename R>
-bool panel_cluster_supported(int m) {
+bool panel_cluster_supported(int m, int jb) {
   typedef typename cx<R>::T T;
   static int cached[2] = {-1, -1};
   static std::mutex mu;
   std::lock_guard<std::mutex> lock(mu);
   const int idx = sizeof(R) == 8 ? 1 : 0;
   const int rpc = (m + kClusterCTAs - 1) / kClusterCTAs;
-  if ((size_t)rpc * kClusterNB * sizeof(T) > (size_t)kPanelSmemMax) return false;
+  if ((size_t)rpc * jb * sizeof(T) > (size_t)kPanelSmemMax) return false;
   if (cached[idx] < 0) {
     auto kern = k_getf2_cluster<R>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -709,8 +903,8 @@ bool panel_cluster_supported(int m) {
   }
   return cached[idx] == 1;
 }
-template bool panel_cluster_supported<float>(int);
-template bool panel_cluster_supported<double>(int);
+template bool panel_cluster_supported<float>(int, int);
+template bool panel_cluster_supported<double>(int, int);
 
 // ---------------------------------------------------------------------------
 // Triangular solves, one CTA per right-hand-side column (jb <= 256 rows):
