@@ -12,6 +12,7 @@
 #include <atomic>
 #include <chrono>
 #include <complex>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -57,6 +58,7 @@ struct DevBuf {
 struct hg_ctx {
   hg_opts o;
   cudaStream_t st = nullptr;
+  std::unique_ptr<hg::HMatrix> hm;  // solver 2 with hmatrix 1: the H-matrix of the last fill
   std::string err;
   // mesh
   int n = 0, nl = 0, tn = 0, tnf = 0, ntnd = 0, nbody = 0;  // tn: rows of the current solve, tnf: n + nl
@@ -512,6 +514,10 @@ cudaStream_t block_stream(const hg_ctx* c, int b) { return c->pst[b % kBlockStre
 int setup_iter_precond(hg_ctx* c) {
   const int n = c->n;
   const IterMat im = iter_mat(c);
+  if (c->o.hmatrix) {  // HMATRIX_BUILD of the assembled matrix (AssbMatx.f90:284, AssbMatxMulti.f90:288)
+    if (!c->hm) c->hm.reset(new hg::HMatrix());
+    CK(c->hm->build(c->st, n, im.M, im.Mf, im.ld, c->h_xyz.data()));
+  }
   if (c->nbody <= 1) {
     CK(c->pd.ensure(n));
     if (im.Mf) CK(hg::diag_extract(c->st, n, im.Mf, im.ld, c->pd.p));
@@ -579,6 +585,10 @@ int iter_precond(hg_ctx* c, int nc, const double2* V, double2* Z) {
 // (~1e-7 of sum |m||z|, far below the solver's 1e-4).
 int iter_matvec(hg_ctx* c, int nc, const double2* Z, const double2* Bin, double sign, double2* W) {
   const int n = c->n;
+  if (c->o.hmatrix && c->hm) {  // HMATVEC (IterativeSolvers.f90:366, :395)
+    CK(c->hm->matvec(c->st, nc, Z, n, Bin, n, sign, W, n));
+    return 0;
+  }
   const IterMat im = iter_mat(c);
   if (im.Mf) {
     CK(hg::resid_df(c->st, false, n, nc, n, im.Mf, im.ld, Z, n, Bin, n, sign, W, n, c->rws.p, c->rws.cap, false));
@@ -949,6 +959,7 @@ void hg_default_opts(hg_opts* o) {
   o->g = 9.80665;
   o->lu_tensor = 2;
   o->solver = 1;
+  o->hmatrix = 0;
 }
 
 int hg_create(hg_ctx** out, const hg_opts* opts) {
@@ -964,6 +975,7 @@ int hg_create(hg_ctx** out, const hg_opts* opts) {
   if (c->o.refine_method != 0 && c->o.refine_method != 1) { delete c; return -2; }
   if (c->o.fin_table < -1 || c->o.fin_table > 1) { delete c; return -2; }
   if (c->o.solver != 1 && c->o.solver != 2) { delete c; return -2; }
+  if (c->o.hmatrix != 0 && c->o.hmatrix != 1) { delete c; return -2; }
   cudaError_t e = cudaSetDevice(c->o.device);
   // the context's stream carries the LU's critical path (the panels): it gets the higher priority,
   // the look-ahead's side stream the lower one
@@ -1707,6 +1719,46 @@ int hg_iter_info(const hg_ctx* c, int* iterations, int* restarts, int* unconverg
   if (restarts) *restarts = c->sweeps;
   if (unconverged) *unconverged = c->iter_unconv;
   if (residual) *residual = c->resid;
+  return 0;
+}
+
+int hg_hmatrix_info(const hg_ctx* c, int* nblocks, int* ndense, int* nlowrank, double* mean_rank, double* compression) {
+  if (!c) return -1;
+  if (!c->hm || !c->o.hmatrix) return HG_ERR_STATE;
+  const hg::HMatrixStats s = c->hm->stats();
+  if (nblocks) *nblocks = s.nblocks;
+  if (ndense) *ndense = s.ndense;
+  if (nlowrank) *nlowrank = s.nlowrank;
+  if (mean_rank) *mean_rank = s.nlowrank ? (double)s.rank_sum / s.nlowrank : 0.0;
+  if (compression) *compression = s.bytes > 0 ? 16.0 * (double)c->n * (double)c->n / s.bytes : 0.0;
+  return 0;
+}
+
+int hg_hmatrix_check(hg_ctx* c, int n, const double* a, int lda, const double* xyz, int nc, const double* x, double* y,
+                     long long* stats) {
+  if (!c) return -1;
+  if (n <= 0 || nc <= 0) return fail(c, -2, "bad shape");
+  if (!a || lda < n || !xyz || !x || !y) return fail(c, -3, "bad array or leading dimension");
+  CK(cudaSetDevice(c->o.device));
+  DevBuf<double2> da, dx, dy;
+  CK(da.ensure((size_t)n * n));
+  CK(dx.ensure((size_t)n * nc));
+  CK(dy.ensure((size_t)n * nc));
+  CK(cudaMemcpy2DAsync(da.p, (size_t)n * sizeof(double2), a, (size_t)lda * sizeof(double2), (size_t)n * sizeof(double2),
+                       n, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(dx.p, x, (size_t)n * nc * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+  hg::HMatrix h;
+  CK(h.build(c->st, n, da.p, nullptr, n, xyz));
+  CK(h.matvec(c->st, nc, dx.p, n, nullptr, 0, 1.0, dy.p, n));
+  CK(cudaMemcpyAsync(y, dy.p, (size_t)n * nc * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (stats) {
+    const hg::HMatrixStats s = h.stats();
+    stats[0] = s.nblocks;
+    stats[1] = s.ndense;
+    stats[2] = s.nlowrank;
+    stats[3] = s.rank_sum;
+  }
   return 0;
 }
 

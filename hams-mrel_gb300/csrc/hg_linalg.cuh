@@ -87,6 +87,34 @@ cudaError_t getrs(cudaStream_t st, int n, int nrhs, const typename cx<R>::T* LU,
 size_t lu_work_bytes(int n, int tc_passes);
 size_t lu_work_bytes_z(int n);
 
+// H-matrix of the iterative solver's matrix (hg_hmatrix.cu; the reference's
+// src/HMatrix.f90): cluster and block trees of the panel centres xyz
+// (n x 3, column-major), ACA-compressed admissible blocks (1e-4, rank <= 50),
+// dense near-field blocks, all in complex128; M (complex128) or Mf
+// (complex64) is the assembled n x n matrix (leading dimension ld), read
+// only by build.  matvec: W = Bin + sign * H Z for nc columns (Bin may be
+// null; leading dimensions ldz, ldb, ldw).
+struct HMatrixStats {
+  int nblocks = 0, ndense = 0, nlowrank = 0;
+  long long rank_sum = 0;
+  double bytes = 0.0;  // storage of the blocks
+};
+class HMatrix {
+ public:
+  HMatrix();
+  ~HMatrix();
+  HMatrix(const HMatrix&) = delete;
+  HMatrix& operator=(const HMatrix&) = delete;
+  cudaError_t build(cudaStream_t st, int n, const double2* M, const float2* Mf, long ld, const double* xyz);
+  cudaError_t matvec(cudaStream_t st, int nc, const double2* Z, long ldz, const double2* Bin, long ldb, double sign,
+                     double2* W, long ldw);
+  HMatrixStats stats() const;
+  struct Impl;
+
+ private:
+  Impl* p;
+};
+
 // Complex128 C -= A B on the tcgen05 tensor cores, FP64-accurate, by exact
 // BF16 digit slicing of both operands (hg_zgemm_tc.cu): A m x k (lda), B k x n
 // (ldb), C m x n (ldc), column-major; B may alias C (B is sliced before C is

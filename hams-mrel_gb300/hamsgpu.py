@@ -28,6 +28,7 @@ EXPORTS = [
     "hg_server_wait", "hg_server_stats", "hg_server_last_error", "hg_server_destroy", "hg_field_points",
     "hg_case_read", "hg_case_free", "hg_case_info", "hg_case_arrays", "hg_case_run", "hg_case_write",
     "hg_iter_info", "hg_case_options", "hg_server_timeline", "hg_bench_panel", "hg_resid_check",
+    "hg_hmatrix_info", "hg_hmatrix_check",
 ]
 
 
@@ -35,7 +36,7 @@ class HgOpts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("precision", ctypes.c_int), ("grn_kind", ctypes.c_int),
                 ("max_refine", ctypes.c_int), ("refine_tol", ctypes.c_double), ("rho", ctypes.c_double),
                 ("g", ctypes.c_double), ("lu_tensor", ctypes.c_int), ("refine_method", ctypes.c_int),
-                ("fin_table", ctypes.c_int), ("solver", ctypes.c_int)]
+                ("fin_table", ctypes.c_int), ("solver", ctypes.c_int), ("hmatrix", ctypes.c_int)]
 
 
 class HgRequest(ctypes.Structure):
@@ -120,6 +121,8 @@ def load(build_if_missing: bool = True):
                                 c_int]
     L.hg_resid_check.argtypes = [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_void_p,
                                  c_int, c_void_p, c_int]
+    L.hg_hmatrix_info.argtypes = [c_void_p, P(c_int), P(c_int), P(c_int), P(c_double), P(c_double)]
+    L.hg_hmatrix_check.argtypes = [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p, c_void_p]
     L.hg_mark.argtypes = [c_void_p, c_int]
     L.hg_elapsed.argtypes = [c_void_p, c_int, c_int, P(ctypes.c_float)]
     L.hg_dispersion.argtypes = [c_double, c_double, c_int, c_void_p]
@@ -186,7 +189,8 @@ class Solver:
 
     def __init__(self, precision: int = HG_PREC_FP64, device: int = 0, grn_kind: int = 8,
                  max_refine: int = 10, refine_tol: float = 1e-10, rho: float = 1000.0, g: float = 9.80665,
-                 lu_tensor: int = 2, refine_method: int = 0, fin_table: int = -1, solver: int = 1):
+                 lu_tensor: int = 2, refine_method: int = 0, fin_table: int = -1, solver: int = 1,
+                 hmatrix: int = 0):
         self.L = load()
         opts = HgOpts()
         self.L.hg_default_opts(ctypes.byref(opts))
@@ -196,6 +200,7 @@ class Solver:
         opts.refine_method = refine_method
         opts.fin_table = fin_table
         opts.solver = solver
+        opts.hmatrix = hmatrix
         h = ctypes.c_void_p()
         rc = self.L.hg_create(ctypes.byref(h), ctypes.byref(opts))
         if rc != 0:
@@ -415,6 +420,29 @@ class Solver:
         r = ctypes.c_double()
         self._check(self.L.hg_iter_info(self.h, ctypes.byref(it), ctypes.byref(rs), ctypes.byref(un), ctypes.byref(r)))
         return it.value, rs.value, un.value, r.value
+
+    def hmatrix_info(self):
+        """(blocks, dense blocks, low-rank blocks, mean rank, compression) of the
+        H-matrix of the last fill (solver = 2, hmatrix = 1)."""
+        nb, nd, nl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        mr, cr = ctypes.c_double(), ctypes.c_double()
+        self._check(self.L.hg_hmatrix_info(self.h, ctypes.byref(nb), ctypes.byref(nd), ctypes.byref(nl),
+                                           ctypes.byref(mr), ctypes.byref(cr)))
+        return nb.value, nd.value, nl.value, mr.value, cr.value
+
+    def hmatrix_check(self, a, xyz, x):
+        """H x through the device H-matrix of a (hg_hmatrix_check); xyz the n x 3
+        panel centres.  Returns (y, (blocks, dense, low rank, sum of ranks))."""
+        a = np.asfortranarray(a, dtype=np.complex128)
+        n = a.shape[0]
+        xyz = np.asfortranarray(xyz, dtype=np.float64)
+        x = np.asfortranarray(x, dtype=np.complex128)
+        if x.ndim == 1:
+            x = x.reshape(n, 1, order="F")
+        y = np.zeros(x.shape, dtype=np.complex128, order="F")
+        st = np.zeros(4, dtype=np.int64)
+        self._check(self.L.hg_hmatrix_check(self.h, n, _ptr(a), n, _ptr(xyz), x.shape[1], _ptr(x), _ptr(y), _ptr(st)))
+        return y, tuple(int(v) for v in st)
 
     def refine_info(self):
         s = ctypes.c_int(); r = ctypes.c_double()

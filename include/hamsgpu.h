@@ -74,10 +74,17 @@ typedef struct {
                             iterations, right-preconditioned by Jacobi (one body) or by the LU of
                             each body's diagonal block (several bodies), as the reference's
                             ZBLOCK_GMRES_SOLVE; hg_fill_factor then factors only those blocks */
+    int hmatrix;         /* solver 2: 1 = the GMRES products through the reference's H-matrix
+                            (src/HMatrix.f90: cluster tree of the panel centres, at most 32 per
+                            leaf; admissible blocks, centres > 2 x the larger diameter apart,
+                            compressed by ACA to 1e-4 with rank <= 50; dense near field), built
+                            on the device from the assembled matrix after each fill, as the
+                            reference's ISOLV = 2 does; 0 = the dense matrix (default: one
+                            bandwidth-bound pass, no compression error) */
 } hg_opts;
 
 /* Fill opts with the defaults above (device 0, FP64, GRN_KIND 8, rho 1000, g 9.80665, lu_tensor 2,
- * solver 1). */
+ * solver 1, hmatrix 0). */
 void hg_default_opts(hg_opts *opts);
 
 /* Create / destroy a context.  opts may be NULL for the defaults. */
@@ -341,6 +348,12 @@ int hg_gmres_iterations(const hg_ctx *ctx, int *iterations);
  * opts.solver is not 2. */
 int hg_iter_info(const hg_ctx *ctx, int *iterations, int *restarts, int *unconverged, double *residual);
 
+/* The H-matrix of the last fill (opts.solver 2 with opts.hmatrix 1): block count, dense and
+ * low-rank blocks, mean rank of the low-rank blocks, and its storage against the dense matrix's
+ * (n^2 complex128 entries over the blocks' entries).  HG_ERR_STATE without one. */
+int hg_hmatrix_info(const hg_ctx *ctx, int *nblocks, int *ndense, int *nlowrank, double *mean_rank,
+                    double *compression);
+
 /* CUDA events on the context's stream, for callers that time a sequence of
  * calls on the device: hg_mark records event slot (0..15); hg_elapsed waits
  * for the later one and returns the milliseconds between two slots. */
@@ -379,6 +392,14 @@ int hg_gemm_check(hg_ctx *ctx, int variant, int m, int n, int k, const double *a
  * sliced products on the tensor cores (Ozaki et al. 2012: BF16 digits of the
  * row- and column-scaled operands, exact FP32 partial sums).  nc <= 40.  A
  * test hook for the residual of the refinement. */
+/* y = H x for the H-matrix of the COMPLEX*16 n x n matrix a (lda) with panel centres xyz (n x 3,
+ * column-major), for nc columns x (n x nc, leading dimension n; y the same), built on the device as
+ * opts.hmatrix does (src/HMatrix.f90: HMATRIX_BUILD, HMATVEC).  stats (may be NULL) receives the
+ * block count, dense blocks, low-rank blocks and the sum of their ranks.  A test hook for the
+ * H-matrix. */
+int hg_hmatrix_check(hg_ctx *ctx, int n, const double *a, int lda, const double *xyz, int nc, const double *x,
+                     double *y, long long *stats);
+
 int hg_resid_check(hg_ctx *ctx, int variant, int m, int nc, int k, const double *a, int lda, const double *y,
                    int ldy, const double *b, int ldb, double *out, int ldo);
 

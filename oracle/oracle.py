@@ -589,6 +589,195 @@ def gmres_solve(M: np.ndarray, b: np.ndarray, precond, tol=1e-4, maxit=100, rest
     return x, min(it, maxit), info
 
 
+# ---------------------------------------------------------------------------
+# H-matrix compression of the iterative solver (ISOLV = 2): src/HMatrix.f90
+# ---------------------------------------------------------------------------
+HM_NLEAF, HM_ETA, HM_ACA_TOL, HM_RANK_MAX = 32, 2.0, 1.0e-4, 50  # src/HMatrix.f90:58-61
+
+
+@dataclass
+class HMat:
+    """The H-matrix of src/HMatrix.f90: cluster order ``perm`` (cluster
+    position -> original index, 0-based) and blocks in build order, each
+    ``(rs, nr, cs, nc, D)`` (dense) or ``(rs, nr, cs, nc, U, VH)`` (low rank)
+    with rows/columns as 0-based positions in cluster order."""
+    perm: np.ndarray
+    blocks: list
+    tree: list
+
+
+def hmatrix_clusters(xyz: np.ndarray, nleaf: int = HM_NLEAF):
+    """SPLIT_CLUSTER_ITERATIVE (src/HMatrix.f90:236-381): geometric bisection
+    at the middle of the longest bounding-box side, explicit stack, left
+    child first.  xyz is N x 3.  Returns (tree, perm): tree nodes as dicts
+    (start, end inclusive, 0-based; left/right child node indices or -1;
+    center; diameter)."""
+    n = xyz.shape[0]
+    w = np.array(xyz, dtype=np.float64, copy=True)
+    perm = np.arange(n)
+    tree = []
+    stack = [(0, n - 1, -1, 0)]
+    while stack:
+        i0, i1, parent, side = stack.pop()
+        size = i1 - i0 + 1
+        if size <= 0:
+            continue
+        node = len(tree)
+        tree.append({"start": i0, "end": i1, "left": -1, "right": -1})
+        if parent >= 0:
+            tree[parent]["left" if side == 1 else "right"] = node
+        bmin = w[i0].copy()
+        bmax = w[i0].copy()
+        cx = cy = cz = 0.0
+        for j in range(i0, i1 + 1):
+            for d in range(3):
+                if w[j, d] < bmin[d]:
+                    bmin[d] = w[j, d]
+                if w[j, d] > bmax[d]:
+                    bmax[d] = w[j, d]
+            cx += w[j, 0]
+            cy += w[j, 1]
+            cz += w[j, 2]
+        tree[node]["center"] = (cx / size, cy / size, cz / size)
+        blen = bmax - bmin
+        tree[node]["diameter"] = math.sqrt(blen[0] ** 2 + blen[1] ** 2 + blen[2] ** 2)
+        if size <= nleaf:
+            continue
+        dim = 0
+        if blen[1] > blen[dim]:
+            dim = 1
+        if blen[2] > blen[dim]:
+            dim = 2
+        split = 0.5 * (bmin[dim] + bmax[dim])
+        i, j = i0, i1
+        while i <= j:
+            if w[i, dim] <= split:
+                i += 1
+            else:
+                w[[i, j]] = w[[j, i]]
+                perm[[i, j]] = perm[[j, i]]
+                j -= 1
+        left_end = i - 1
+        if left_end < i0:
+            left_end = i0
+        if left_end >= i1:
+            left_end = i1 - 1
+        stack.append((left_end + 1, i1, node, 2))
+        stack.append((i0, left_end, node, 1))
+    return tree, perm
+
+
+def hmatrix_block_list(tree, eta: float = HM_ETA):
+    """BUILD_BLOCK_TREE_ITERATIVE (src/HMatrix.f90:390-497): block pairs in
+    the reference's traversal order, each (row node, col node, admissible)."""
+    out = []
+    stack = [(0, 0)]
+    while stack:
+        r, c = stack.pop()
+        tr, tc = tree[r], tree[c]
+        nr = tr["end"] - tr["start"] + 1
+        nc = tc["end"] - tc["start"] + 1
+        if nr <= 0 or nc <= 0:
+            continue
+        dist = math.sqrt((tr["center"][0] - tc["center"][0]) ** 2 + (tr["center"][1] - tc["center"][1]) ** 2 +
+                         (tr["center"][2] - tc["center"][2]) ** 2)
+        if dist > eta * max(tr["diameter"], tc["diameter"]) and nr > 1 and nc > 1:
+            out.append((r, c, True))
+            continue
+        leaf_r, leaf_c = tr["left"] < 0, tc["left"] < 0
+        if leaf_r and leaf_c:
+            out.append((r, c, False))
+            continue
+        if leaf_r:
+            stack += [(r, tc["right"]), (r, tc["left"])]
+        elif leaf_c:
+            stack += [(tr["right"], c), (tr["left"], c)]
+        else:
+            stack += [(tr["right"], tc["right"]), (tr["right"], tc["left"]), (tr["left"], tc["right"]),
+                      (tr["left"], tc["left"])]
+    return out
+
+
+def hmatrix_aca(Ab: np.ndarray, tol: float = HM_ACA_TOL, rank_max: int = HM_RANK_MAX):
+    """ADD_LOWRANK_BLOCK's partially pivoted ACA (src/HMatrix.f90:560-750) on
+    the block Ab (NR x NC, cluster order).  Returns (U, VH) or None when the
+    block is kept dense.  The stopping test uses the exact
+    ||U V^H||_F^2 update, 2 Re sum_l (u_l^H u_k)(v_k^H v_l): the reference's
+    cross term (:712-719) sums Re(conj(U(j,l)) U(j,k)) Re(conj(VH(k,j))
+    VH(l,j)) over j = 1..NR for both factors, reading past VH's NC columns
+    when NR > NC."""
+    nr, nc = Ab.shape
+    kmax = min(rank_max, nr, nc)
+    if nr <= 4 or nc <= 4:
+        return None
+    U = np.zeros((nr, kmax), dtype=np.complex128)
+    VH = np.zeros((kmax, nc), dtype=np.complex128)
+    used = np.zeros(nr, dtype=bool)
+    frob = 0.0
+    rank = 0
+    for k in range(kmax):
+        if k == 0:
+            pr = 0
+        else:
+            mags = np.abs(U[:, k - 1])
+            mags[used] = -1.0
+            pr = int(np.argmax(mags))
+            if mags[pr] < 0.0:
+                break
+        used[pr] = True
+        row = Ab[pr, :].astype(np.complex128)
+        for l in range(k):
+            row = row - U[pr, l] * VH[l, :]
+        pc = int(np.argmax(np.abs(row)))
+        pe = row[pc]
+        if abs(pe) < 1.0e-30:
+            break
+        col = Ab[:, pc].astype(np.complex128)
+        for l in range(k):
+            col = col - U[:, l] * VH[l, pc]
+        U[:, k] = col / pe
+        VH[k, :] = row
+        rank = k + 1
+        uv = math.sqrt(float(np.sum(np.abs(U[:, k]) ** 2))) * math.sqrt(float(np.sum(np.abs(VH[k, :]) ** 2)))
+        frob += uv * uv
+        for l in range(k):
+            frob += 2.0 * float(np.real(np.vdot(U[:, l], U[:, k]) * np.vdot(VH[l, :], VH[k, :])))
+        if uv < tol * math.sqrt(max(frob, 1.0e-30)):
+            break
+    if rank == 0 or rank * (nr + nc) >= nr * nc:
+        return None
+    return U[:, :rank].copy(), VH[:rank, :].copy()
+
+
+def hmatrix_build(M: np.ndarray, xyz: np.ndarray) -> HMat:
+    """HMATRIX_BUILD (src/HMatrix.f90:135-196) of the assembled matrix M
+    (N x N) with panel centres xyz (N x 3)."""
+    tree, perm = hmatrix_clusters(xyz)
+    blocks = []
+    for r, c, adm in hmatrix_block_list(tree):
+        rs, cs = tree[r]["start"], tree[c]["start"]
+        nr, nc = tree[r]["end"] - rs + 1, tree[c]["end"] - cs + 1
+        Ab = M[np.ix_(perm[rs:rs + nr], perm[cs:cs + nc])]
+        lr = hmatrix_aca(Ab) if adm else None
+        blocks.append((rs, nr, cs, nc, Ab.astype(np.complex128)) if lr is None else (rs, nr, cs, nc) + lr)
+    return HMat(perm=perm, blocks=blocks, tree=tree)
+
+
+def hmatvec(H: HMat, x: np.ndarray) -> np.ndarray:
+    """HMATVEC (src/HMatrix.f90:760-820): y = H x for one or more columns."""
+    xp = x[H.perm]
+    yp = np.zeros(xp.shape, dtype=np.complex128)
+    for b in H.blocks:
+        rs, nr, cs, nc = b[:4]
+        if len(b) == 5:
+            yp[rs:rs + nr] += b[4] @ xp[cs:cs + nc]
+        else:
+            yp[rs:rs + nr] += b[4] @ (b[5] @ xp[cs:cs + nc])
+    y = np.empty_like(yp)
+    y[H.perm] = yp
+    return y
+
+
 def gmres_columns(M: np.ndarray, B: np.ndarray, blocks=None, **kw):
     """ZBLOCK_GMRES_SOLVE (src/IterativeSolvers.f90:535-562): every column
     separately with the same preconditioner.  Returns (X, iterations per

@@ -1,0 +1,67 @@
+"""The oracle's restatement of the reference's H-matrix (src/HMatrix.f90),
+pinned against the dense product it approximates.
+
+1. The block list tiles the matrix exactly once, and every low-rank block is
+   admissible (centres more than 2 x the larger diameter apart).
+2. ACA recovers an exactly low-rank block to rounding, stopping one step
+   after its rank (the stopping test needs an update below 1e-4 of the
+   approximation, which the step after the rank provides).
+3. On an assembled BEM influence matrix (three cylinders, 1536 panels, deep
+   water) H x matches M x within 1e-3 of max |M x| (ACA stops each block at
+   1e-4 of its Frobenius norm), with most of the far field compressed.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from helpers import case_from_mesh
+
+
+@pytest.fixture(scope="module")
+def bem(pkg, oracle):
+    mesh = pkg.meshgen.three_cylinders(with_lid=False)
+    case = case_from_mesh(oracle, mesh, h=-1.0, headings_deg=[0.0])
+    v, wk, w1, wvn = oracle.wave_properties(case.ctl, 1.0)
+    A, _ = oracle.assemble(case, v, wvn, 8, 0)
+    return A, np.asarray(mesh.xyz_p, dtype=np.float64)
+
+
+def test_blocks_tile_the_matrix_once(oracle, bem):
+    A, xyz = bem
+    n = A.shape[0]
+    H = oracle.hmatrix_build(A, xyz)
+    cover = np.zeros((n, n), dtype=np.int32)
+    for b in H.blocks:
+        rs, nr, cs, nc = b[:4]
+        cover[rs:rs + nr, cs:cs + nc] += 1
+    assert (cover == 1).all()
+    assert sorted(H.perm.tolist()) == list(range(n))
+    for r, c, adm in oracle.hmatrix_block_list(H.tree):
+        tr, tc = H.tree[r], H.tree[c]
+        if adm:
+            d = math.dist(tr["center"], tc["center"])
+            assert d > oracle.HM_ETA * max(tr["diameter"], tc["diameter"])
+
+
+def test_aca_recovers_an_exact_low_rank_block(oracle):
+    rng = np.random.default_rng(3)
+    u = rng.standard_normal((60, 3)) + 1j * rng.standard_normal((60, 3))
+    w = rng.standard_normal((3, 45)) + 1j * rng.standard_normal((3, 45))
+    blk = u @ w
+    U, VH = oracle.hmatrix_aca(blk)
+    assert U.shape[1] == 4
+    assert np.abs(U @ VH - blk).max() < 1e-12 * np.abs(blk).max()
+
+
+def test_hmatvec_matches_the_dense_product(oracle, bem):
+    A, xyz = bem
+    H = oracle.hmatrix_build(A, xyz)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((A.shape[0], 3)) + 1j * rng.standard_normal((A.shape[0], 3))
+    y, yd = oracle.hmatvec(H, x), A @ x
+    assert np.abs(y - yd).max() < 1e-3 * np.abs(yd).max()
+    lowrank = [b for b in H.blocks if len(b) == 6]
+    assert len(lowrank) > 100
+    stored = sum(b[4].size if len(b) == 5 else b[4].size + b[5].size for b in H.blocks)
+    assert stored < 0.6 * A.size
