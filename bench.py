@@ -267,7 +267,7 @@ def ours(args, dist, rank, world, local):
         return (np.array([x[0] for x in vals]), np.array([x[1] for x in vals]), np.array([x[2] for x in vals]))
 
     sopts = dict(lu_tensor=args.lu_tensor, refine_method=1 if args.refine == "gmres" else 0,
-                 solver=2 if args.solver == "gmres" else 1)
+                 solver=2 if args.solver == "gmres" else 1, hmatrix=args.hmatrix)
     s = hg.Solver(precision=prec, device=local, **sopts)
     s.set_mesh(mesh.nodes, mesh.ncon, mesh.ncn, mesh.xyz_p, mesh.ds, mesh.pnsz, mesh.dxyz_p, mesh.body_ranges)
     # set-up (not a step): one frequency per slot creates every slot and its device buffers
@@ -372,7 +372,8 @@ def ours(args, dist, rank, world, local):
             "dtype": "complex64+fp64-refine" if prec == hg.HG_PREC_MIXED else "complex128",
             "data": "synthetic",
             "config": dict(CONFIG, precision=args.precision, parallelism=f"replicas{world}", slots=nslots,
-                           refine=args.refine, lu_tensor=args.lu_tensor, solver=args.solver),
+                           refine=args.refine, lu_tensor=args.lu_tensor, solver=args.solver,
+                           **({"hmatrix": args.hmatrix} if args.solver == "gmres" else {})),
             "latency_ms": {"p50": lat_sorted[len(lat) // 2], "p99": lat_sorted[min(len(lat) - 1,
                                                                                   int(0.99 * len(lat)))],
                            "what": f"host wall time per frequency-solve with {nslots} solves in flight"},
@@ -762,6 +763,8 @@ def main():
                     help="mixed-form refinement: classical iterative refinement or GMRES-IR")
     ap.add_argument("--lu-tensor", type=int, default=2, choices=[0, 1, 2, 3],
                     help="LU trailing updates: 2 split-BF16 tensor cores, 3 split-TF32, 1 TF32, 0 FP32 SIMT")
+    ap.add_argument("--hmatrix", type=int, default=0, choices=[0, 1],
+                    help="with --solver gmres: the products through the reference's H-matrix (ACA)")
     ap.add_argument("--solver", default="lu", choices=["lu", "gmres"],
                     help="array workload: linear solver (gmres = the reference's Solver_type 2)")
     ap.add_argument("--workload", default="array", choices=["array", "batch", "serve", "three", "field"],
