@@ -594,6 +594,27 @@ static cudaError_t hm_build(HMatrix::Impl* p, cudaStream_t st, int n, const T* M
   return cudaStreamSynchronize(st);  // the host vectors above are copied before they go
 }
 
+size_t hmatrix_bytes_estimate(int n, const double* xyz, int nc) {
+  if (n <= 0 || !xyz) return 0;
+  std::vector<Node> tree;
+  std::vector<int> perm, br, bc;
+  std::vector<char> adm;
+  hm_trees(n, xyz, tree, perm, br, bc, adm);
+  size_t elems = 0, rows = 0;
+  for (size_t b = 0; b < br.size(); ++b) {
+    const size_t nr = (size_t)(tree[br[b]].end - tree[br[b]].start + 1), ncl = (size_t)(tree[bc[b]].end - tree[bc[b]].start + 1);
+    if (adm[b] && nr > 4 && ncl > 4) {
+      const size_t kmax = std::min<size_t>(kHmRankMax, std::min(nr, ncl));
+      elems += kmax * (nr + ncl) + ncl + (nr + 3) / 4 + 1;  // factors and the ACA scratch
+    } else {
+      elems += nr * ncl;
+    }
+    rows += nr;
+  }
+  elems += rows * (size_t)nc + (size_t)n * nc;  // the product's scratch rows and permuted right-hand sides
+  return elems * sizeof(double2) + br.size() * (sizeof(HmBlock) + 2 * sizeof(int)) + (size_t)4 * n * sizeof(int);
+}
+
 cudaError_t HMatrix::build(cudaStream_t st, int n, const double2* M, const float2* Mf, long ld, const double* xyz) {
   if (n <= 0 || (!M && !Mf) || !xyz) return cudaErrorInvalidValue;
   return M ? hm_build<double2>(p, st, n, M, ld, xyz) : hm_build<float2>(p, st, n, Mf, ld, xyz);

@@ -99,6 +99,11 @@ struct HMatrixStats {
   long long rank_sum = 0;
   double bytes = 0.0;  // storage of the blocks
 };
+// Device bytes of the H-matrix of n panels with centres xyz and of its
+// product with nc columns: the ACA factors at their maximum rank, the dense
+// near-field blocks and the scratch, from the host trees (admissible blocks
+// assumed to compress).
+size_t hmatrix_bytes_estimate(int n, const double* xyz, int nc);
 class HMatrix {
  public:
   HMatrix();

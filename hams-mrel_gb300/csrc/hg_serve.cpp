@@ -36,6 +36,10 @@
 
 #include "../../include/hamsgpu.h"
 
+namespace hg {
+size_t hmatrix_bytes_estimate(int n, const double* xyz, int nc);  // hg_hmatrix.cu
+}
+
 // Milliseconds from ref (an event recorded earlier on the context's device)
 // to the context's hg_mark event in slot (hg_abi.cu).
 int hg_mark_since(const hg_ctx* c, int slot, cudaEvent_t ref, float* ms);
@@ -233,7 +237,8 @@ void copy_in(std::vector<T>& dst, const T* src, size_t count) {
 // for solver 2 the preconditioner (the diagonal, or the per-body diagonal
 // blocks and their pivots), and in the FP64 form without lids the n x nc
 // right-hand-side block of the square system, which hg_solve_footprint
-// counts only for the mixed form and for lids.
+// counts only for the mixed form and for lids; with the H-matrix its blocks
+// and scratch (hmatrix_bytes_estimate, from the request's panel centres).
 static size_t iter_bytes(const hg_opts& o, const hg_request& q) {
   const size_t n = (size_t)q.n, nc = (size_t)6 * q.nbody + (size_t)(q.nbeta > 0 ? q.nbeta : 0);
   size_t b = 0;
@@ -250,6 +255,7 @@ static size_t iter_bytes(const hg_opts& o, const hg_request& q) {
       }
       b += blocks * (o.precision == HG_PREC_MIXED ? 8 : 16) + n * sizeof(int);
     }
+    if (o.hmatrix) b += hg::hmatrix_bytes_estimate(q.n, q.xyz_p, (int)nc);
   } else if (o.refine_method == 1 && o.precision == HG_PREC_MIXED) {
     b += (size_t)(2 * 8 + 2) * n * nc * 16;
   }
