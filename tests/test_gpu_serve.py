@@ -106,3 +106,31 @@ def test_admission_budget(pkg, requests_and_alone):
     with pytest.raises(hg.HamsGpuError):
         srv.submit(big[0], big[1], big[2], big[3], big[4], big[5], big[6])
     srv.close()
+
+
+def test_iterative_hmatrix_requests_equal_alone(pkg):
+    """The iterative solver with the reference's H-matrix (solver 2,
+    hmatrix 1) through the server: results equal to the same request on its
+    own context, and the admission reserves the H-matrix's blocks on top of
+    the dense GMRES's memory."""
+    hg = pkg.hamsgpu
+    mesh = pkg.meshgen.three_cylinders(with_lid=False)
+    vals = [hg.wave_properties(3, w, -1.0) for w in (0.8, 1.3)]
+    v = np.array([x[0] for x in vals]); wk = np.array([x[1] for x in vals]); w1 = np.array([x[2] for x in vals])
+    betas = np.array([0.0, 0.6])
+    s = hg.Solver(precision=hg.HG_PREC_MIXED, solver=2, hmatrix=1)
+    s.set_mesh(mesh.nodes, mesh.ncon, mesh.ncn, mesh.xyz_p, mesh.ds, mesh.pnsz, mesh.dxyz_p, mesh.body_ranges)
+    ref = []
+    for i in range(len(v)):
+        a, b, f, _ = s.solve_frequency(v[i], wk[i], w1[i], -1.0, None, betas, want_potentials=False)
+        ref.append((a.copy(), b.copy(), f.copy()))
+    s.close()
+    reserved = {}
+    for hm in (1, 0):
+        srv = hg.Server(nslots=2, budget_bytes=150e9, solver=2, hmatrix=hm)
+        got = srv.wait(srv.submit(mesh, -1.0, v, wk, w1, None, betas))
+        if hm:
+            _check_same(got, ref)
+        reserved[hm] = srv.stats()["peak_reserved_bytes"]
+        srv.close()
+    assert reserved[1] > reserved[0]
