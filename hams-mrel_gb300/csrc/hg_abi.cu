@@ -1734,6 +1734,11 @@ int hg_hmatrix_info(const hg_ctx* c, int* nblocks, int* ndense, int* nlowrank, d
   return 0;
 }
 
+int hg_hmatrix_partition(int n, const double* xyz, int* perm, int* blocks, int max_blocks) {
+  if (n <= 0 || !xyz || max_blocks < 0) return -1;
+  return hg::hmatrix_partition(n, xyz, perm, blocks, max_blocks);
+}
+
 int hg_hmatrix_check(hg_ctx* c, int n, const double* a, int lda, const double* xyz, int nc, const double* x, double* y,
                      long long* stats) {
   if (!c) return -1;

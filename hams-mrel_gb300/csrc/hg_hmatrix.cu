@@ -594,6 +594,26 @@ static cudaError_t hm_build(HMatrix::Impl* p, cudaStream_t st, int n, const T* M
   return cudaStreamSynchronize(st);  // the host vectors above are copied before they go
 }
 
+int hmatrix_partition(int n, const double* xyz, int* perm, int* blocks, int max_blocks) {
+  if (n <= 0 || !xyz) return -1;
+  std::vector<Node> tree;
+  std::vector<int> pm, br, bc;
+  std::vector<char> adm;
+  hm_trees(n, xyz, tree, pm, br, bc, adm);
+  if (perm) std::copy(pm.begin(), pm.end(), perm);
+  const int nb = (int)br.size();
+  if (blocks)
+    for (int b = 0; b < nb && b < max_blocks; ++b) {
+      int* o = blocks + 5 * (size_t)b;
+      o[0] = tree[br[b]].start;
+      o[1] = tree[br[b]].end - tree[br[b]].start + 1;
+      o[2] = tree[bc[b]].start;
+      o[3] = tree[bc[b]].end - tree[bc[b]].start + 1;
+      o[4] = adm[b];
+    }
+  return nb;
+}
+
 size_t hmatrix_bytes_estimate(int n, const double* xyz, int nc) {
   if (n <= 0 || !xyz) return 0;
   std::vector<Node> tree;

@@ -104,6 +104,10 @@ struct HMatrixStats {
 // near-field blocks and the scratch, from the host trees (admissible blocks
 // assumed to compress).
 size_t hmatrix_bytes_estimate(int n, const double* xyz, int nc);
+// The host trees alone: the cluster permutation (n) and up to max_blocks
+// blocks as (row start, rows, column start, columns, admissible); returns
+// the block count.
+int hmatrix_partition(int n, const double* xyz, int* perm, int* blocks, int max_blocks);
 class HMatrix {
  public:
   HMatrix();

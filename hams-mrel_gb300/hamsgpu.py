@@ -28,7 +28,7 @@ EXPORTS = [
     "hg_server_wait", "hg_server_stats", "hg_server_last_error", "hg_server_destroy", "hg_field_points",
     "hg_case_read", "hg_case_free", "hg_case_info", "hg_case_arrays", "hg_case_run", "hg_case_write",
     "hg_iter_info", "hg_case_options", "hg_server_timeline", "hg_bench_panel", "hg_resid_check",
-    "hg_hmatrix_info", "hg_hmatrix_check",
+    "hg_hmatrix_info", "hg_hmatrix_check", "hg_hmatrix_partition",
 ]
 
 
@@ -123,6 +123,7 @@ def load(build_if_missing: bool = True):
                                  c_int, c_void_p, c_int]
     L.hg_hmatrix_info.argtypes = [c_void_p, P(c_int), P(c_int), P(c_int), P(c_double), P(c_double)]
     L.hg_hmatrix_check.argtypes = [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p, c_void_p]
+    L.hg_hmatrix_partition.argtypes = [c_int, c_void_p, c_void_p, c_void_p, c_int]
     L.hg_mark.argtypes = [c_void_p, c_int]
     L.hg_elapsed.argtypes = [c_void_p, c_int, c_int, P(ctypes.c_float)]
     L.hg_dispersion.argtypes = [c_double, c_double, c_int, c_void_p]
@@ -182,6 +183,22 @@ class HamsGpuError(RuntimeError):
 
 def _ptr(a):
     return None if a is None else a.ctypes.data
+
+
+def hmatrix_partition(xyz):
+    """The H-matrix partition of panel centres xyz (n x 3) on the host
+    (hg_hmatrix_partition): (perm, blocks), blocks an array of rows
+    (row start, rows, column start, columns, admissible)."""
+    L = load()
+    xyz = np.asfortranarray(xyz, dtype=np.float64)
+    n = xyz.shape[0]
+    perm = np.zeros(n, dtype=np.int32)
+    nb = L.hg_hmatrix_partition(n, _ptr(xyz), _ptr(perm), None, 0)
+    if nb < 0:
+        raise HamsGpuError(nb, "hg_hmatrix_partition failed")
+    blocks = np.zeros((nb, 5), dtype=np.int32)
+    L.hg_hmatrix_partition(n, _ptr(xyz), None, _ptr(blocks), nb)
+    return perm, blocks
 
 
 class Solver:

@@ -400,6 +400,14 @@ int hg_gemm_check(hg_ctx *ctx, int variant, int m, int n, int k, const double *a
 int hg_hmatrix_check(hg_ctx *ctx, int n, const double *a, int lda, const double *xyz, int nc, const double *x,
                      double *y, long long *stats);
 
+/* The H-matrix's partition alone, on the host (no device needed): the cluster order perm (n
+ * entries, 0-based original index at each cluster position, SPLIT_CLUSTER_ITERATIVE of
+ * src/HMatrix.f90:236-381) and up to max_blocks blocks in build order (BUILD_BLOCK_TREE_ITERATIVE,
+ * :390-497), five ints each: row start, rows, column start, columns (0-based cluster positions),
+ * admissible (1) or a dense leaf pair (0).  Returns the block count, or a negative value on bad
+ * arguments. */
+int hg_hmatrix_partition(int n, const double *xyz, int *perm, int *blocks, int max_blocks);
+
 int hg_resid_check(hg_ctx *ctx, int variant, int m, int nc, int k, const double *a, int lda, const double *y,
                    int ldy, const double *b, int ldb, double *out, int ldo);
 

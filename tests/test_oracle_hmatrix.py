@@ -9,6 +9,9 @@ pinned against the dense product it approximates.
 3. On an assembled BEM influence matrix (three cylinders, 1536 panels, deep
    water) H x matches M x within 1e-3 of max |M x| (ACA stops each block at
    1e-4 of its Frobenius norm), with most of the far field compressed.
+4. The library's host-side trees (hg_hmatrix_partition, no device needed)
+   equal the oracle's: the same cluster permutation and the same blocks in
+   the same order, on one, three and five bodies.
 """
 import math
 
@@ -65,3 +68,18 @@ def test_hmatvec_matches_the_dense_product(oracle, bem):
     assert len(lowrank) > 100
     stored = sum(b[4].size if len(b) == 5 else b[4].size + b[5].size for b in H.blocks)
     assert stored < 0.6 * A.size
+
+
+@pytest.mark.parametrize("meshname", ["single_cylinder", "three_cylinders", "five_body_array"])
+def test_library_partition_equals_the_oracle(pkg, oracle, meshname):
+    mg = pkg.meshgen
+    mesh = mg.three_cylinders(with_lid=False) if meshname == "three_cylinders" else getattr(mg, meshname)()
+    xyz = np.asarray(mesh.xyz_p, dtype=np.float64)
+    perm, blocks = pkg.hamsgpu.hmatrix_partition(xyz)
+    tree, operm = oracle.hmatrix_clusters(xyz)
+    np.testing.assert_array_equal(perm, operm)
+    ref = []
+    for r, c, adm in oracle.hmatrix_block_list(tree):
+        rs, cs = tree[r]["start"], tree[c]["start"]
+        ref.append((rs, tree[r]["end"] - rs + 1, cs, tree[c]["end"] - cs + 1, int(adm)))
+    np.testing.assert_array_equal(blocks, np.array(ref, dtype=np.int32))
