@@ -734,10 +734,17 @@ def _gemm_roofline(s, n, prec, hg, lu_tensor=2):
                        "rate, so the tensor-pipe utilisation is about 3 x frac (ncu: 44.5 % tensor-pipe activity "
                        "at this shape)")
     if variant == 5:
+        # DRAM bytes of the product kernel: C read and written once, each digit tile read once (eight
+        # digits of A: m x 2k, of B: 2n x 2k, BF16); the 4096 x 4096 x 256 ncu capture measured 0.976 x
+        # these, scaled here to this shape (the traffic grows with them)
+        mp, np2, kp = -(-m // 128) * 128, -(-2 * m // 64) * 64, 2 * k
+        algo = 2.0 * m * m * 16 + 8.0 * (mp + np2) * kp * 2
+        out["traffic"] = 0.976 * algo
         out["note"] = ("algorithmic complex flops of an FP64-accurate product; the hardware does 36 BF16 digit "
                        "products (the digit pairs s + t <= 9 of eight 7-bit digits per operand) per real product "
                        "at the bf16 rate, so the tensor-pipe work is 36 x frac of the bf16 peak; includes the "
-                       "two slicing kernels")
+                       "two slicing kernels; traffic scaled from the 4096 x 4096 x 256 capture "
+                       "(profiles/zgemm_sliced_4096x4096x256.md)")
         out["bf16_equivalent_frac"] = 36 * achieved / peak
     if variant == 2:
         # DRAM bytes of one launch of this shape (5792 x 5792 x 256) from the committed ncu capture
