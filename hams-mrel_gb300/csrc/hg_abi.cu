@@ -113,7 +113,7 @@ struct hg_ctx {
   // field points (hg_field_points): coordinates, on-body flags, DUM2 / DUM1 rows, weights, potentials
   DevBuf<double> fpx;
   DevBuf<int> fonb;
-  DevBuf<double2> fA, fS, fW, fout, fout2;
+  DevBuf<double2> fA, fS, fW, fWn, fout, fout2;  // fWn: -fW, for the tensor-core products
   DevBuf<float2> fAf, fSf;
   int inner_its = 0;                     // GMRES iterations of the last solve
   int irsp = 0;
@@ -254,6 +254,12 @@ int ensure_rhs(hg_ctx* c, int nbeta) {
 
 // Split-K workspace of the context (for the tall-skinny residual products).
 #define WS(c) (void*)(c)->gws.p, (c)->gws.cap * sizeof(double2)
+
+// dst = -src (count complex128 entries).
+__global__ void k_negate(long count, const double2* __restrict__ src, double2* __restrict__ dst) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < count; e += (long)gridDim.x * blockDim.x)
+    dst[e] = make_double2(-src[e].x, -src[e].y);
+}
 
 // Column norms of a complex128 block: out[k] = max over rows |re|+|im|.
 __global__ void k_colmax(int rows, const double2* __restrict__ M, long ld, double* __restrict__ out) {
@@ -1445,6 +1451,16 @@ int hg_field_points(hg_ctx* c, int npts, const double* xyz, int kind, int isol, 
   if (binned) CK(c->bins.ensure(hg::fin_bins_ints(n, chunk)));
   // source weights [radiation modes | -grad phi_I . n of the solved headings]
   CK(hg::launch_rhs_cols(c->st, n, c->dxyz.p, c->body_of.p, c->nbody, nbeta, c->W.p, c->fW.p, n));
+  // plain form: S W - A X as exact digit products on the tensor cores (two products C -= A B, W
+  // negated once) with their digits in the LU's workspace, which the plain form keeps nothing in
+  // after the factorisation (the mixed form keeps its block inverses there)
+  const size_t zb = (!mixed(c) && c->o.lu_tensor != 0 && hg::zgemm_tc_supported())
+                        ? hg::zgemm_tc_work_bytes(chunk, ncol, n) : 0;
+  const bool ztc = zb && c->luws.cap >= zb;
+  if (ztc) {
+    CK(c->fWn.ensure((size_t)n * ncol));
+    k_negate<<<256, 256, 0, c->st>>>((long)n * ncol, c->fW.p, c->fWn.p);
+  }
   std::vector<double> hx((size_t)chunk * 3);
   const double2 one = make_double2(1, 0), mone = make_double2(-1, 0), zero = make_double2(0, 0);
   for (int p0 = 0; p0 < npts; p0 += chunk) {
@@ -1466,8 +1482,16 @@ int hg_field_points(hg_ctx* c, int npts, const double* xyz, int kind, int isol, 
     } else {
       CK(hg::launch_green_fill<double2>(c->st, c->rec.p, c->fpx.p, m, n, m, fs, deep, c->o.grn_kind, c->fA.p, c->fS.p,
                                         m, c->status.p, binned ? c->bins.p : nullptr, 0));
-      CK(hg::gemm<double>(c->st, false, m, ncol, n, one, c->fS.p, m, c->fW.p, n, zero, c->fout.p, m, WS(c)));
-      CK(hg::gemm<double>(c->st, false, m, ncol, n, mone, c->fA.p, m, c->X.p, n, one, c->fout.p, m, WS(c)));
+      if (ztc) {
+        CK(cudaMemsetAsync(c->fout.p, 0, (size_t)m * ncol * sizeof(double2), c->st));
+        CK(hg::zgemm_tc(c->st, m, ncol, n, c->fS.p, m, c->fWn.p, n, c->fout.p, m, c->luws.p, c->luws.cap,
+                        c->status.p));
+        CK(hg::zgemm_tc(c->st, m, ncol, n, c->fA.p, m, c->X.p, n, c->fout.p, m, c->luws.p, c->luws.cap,
+                        c->status.p));
+      } else {
+        CK(hg::gemm<double>(c->st, false, m, ncol, n, one, c->fS.p, m, c->fW.p, n, zero, c->fout.p, m, WS(c)));
+        CK(hg::gemm<double>(c->st, false, m, ncol, n, mone, c->fA.p, m, c->X.p, n, one, c->fout.p, m, WS(c)));
+      }
     }
     CK(hg::launch_field_finish(c->st, m, ncol, nrad, c->fout.p, m, c->fonb.p, c->fpx.p, m, c->betas.p, c->v, c->wk,
                                c->w1, c->h, c->o.g, c->o.rho, isol, kind));

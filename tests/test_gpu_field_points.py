@@ -132,3 +132,23 @@ def test_field_points_need_a_solve(pkg, cyl_case):
     with pytest.raises(RuntimeError):
         s.field_points(np.zeros((1, 3)))
     s.close()
+
+
+def test_field_points_plain_tensor_core_products_match_oracle(pkg, oracle):
+    """Three cylinders (1536 panels, deep water): from order 1024 the plain
+    form's products S W - A X run as exact digit products on the tensor
+    cores (lu_tensor != 0), held to the same 1e-10 against the oracle and
+    within rounding of the FP64-pipe products (lu_tensor 0)."""
+    case = case_from_mesh(oracle, pkg.meshgen.three_cylinders(with_lid=False), h=-1.0, headings_deg=(0.0, 60.0))
+    assert case.n >= 1024
+    w = 1.1
+    pts = _points(case, np.random.default_rng(9), nfluid=16, nsurf=16, ncent=8)
+    got = {}
+    for lu_tensor in (2, 0):
+        s = gpu_solver(pkg, case, 0, lu_tensor=lu_tensor)
+        amas, bdmp, exfc, mx = gpu_frequency(pkg, s, case, w)
+        got[lu_tensor] = (s.field_points(pts, kind=0, isol=1), mx.copy())
+        s.close()
+    ref = _oracle_pot(oracle, case, pts, w, got[2][1])
+    assert max_norm_err(got[2][0], ref) < TOL
+    assert max_norm_err(got[2][0], got[0][0]) < TOL
