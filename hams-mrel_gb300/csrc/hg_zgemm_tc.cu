@@ -1,7 +1,7 @@
 // Complex128 products C -= A B on the tensor cores, FP64-accurate, by exact
 // operand slicing: the plain form's LU updates (U12 = L11^-1 A12 and
-// A22 -= L21 U12 of ZGETRF, AssbMatx.f90:111) and its blocked solves, which
-// otherwise run on GB300's thin FP64 pipes.
+// A22 -= L21 U12 of ZGETRF, AssbMatx.f90:111), its blocked solves and its
+// field-point sums, which otherwise run on GB300's thin FP64 pipes.
 //
 // The scheme (Ozaki, Ogita, Oishi and Rump, Numer. Algorithms 59 (2012)
 // 95-118), as in hg_resid_tc.cu but with both operands in double precision:
@@ -23,8 +23,9 @@
 //    64-bit integers (levels 2..5 and 6..9, by Horner in base 2^7), release
 //    TMEM, and update C with one rounding of the product into double
 //    precision and one of the subtraction.
-// Error: the digits' 2^-57 of sum |a||b| plus the two roundings, the accuracy
-// of a double-precision product.
+// Error: per term the digits' truncation, 2^-57 of the row's and the
+// column's largest entries, plus the two roundings: 2.6e-16 .. 5.7e-16 of
+// |c| + sum |a||b| measured, the accuracy of a double-precision product.
 //
 // Kernel (k_zoz_gemm): persistent, one CTA per SM, output tiles of 128 rows x
 // 64 real columns in M-fastest order (the CTAs working at one time share B's
