@@ -255,8 +255,8 @@ int ensure_rhs(hg_ctx* c, int nbeta) {
 // Split-K workspace of the context (for the tall-skinny residual products).
 #define WS(c) (void*)(c)->gws.p, (c)->gws.cap * sizeof(double2)
 
-// dst = -src (count complex128 entries).
-__global__ void k_negate(long count, const double2* __restrict__ src, double2* __restrict__ dst) {
+// dst = -src (count complex128 entries; dst may be src).
+__global__ void k_negate(long count, const double2* src, double2* dst) {
   for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < count; e += (long)gridDim.x * blockDim.x)
     dst[e] = make_double2(-src[e].x, -src[e].y);
 }
@@ -786,7 +786,14 @@ int solve_cols_once(hg_ctx* c, int c0, int c1) {
   double2* Xc = c->X.p + (size_t)c0 * n;
   if (!mixed(c)) {
     if (c->irsp == 1) {
-      CK(hg::gemm<double>(c->st, true, n, nc, tn, one, c->A.p, tn, Bc, tn, zero, Xc, n, WS(c)));
+      if (c->o.lu_tensor != 0 && hg::zgemm_tc_supported() && c->luws.cap >= hg::zgemm_tc_work_bytes(n, nc, tn)) {
+        // A^T B as -(0 - A^T B), as C = A^T A in hg_fill_factor
+        CK(cudaMemsetAsync(Xc, 0, (size_t)n * nc * sizeof(double2), c->st));
+        CK(hg::zgemm_tc(c->st, n, nc, tn, c->A.p, tn, Bc, tn, Xc, n, c->luws.p, c->luws.cap, c->status.p, true));
+        k_negate<<<256, 256, 0, c->st>>>((long)n * nc, Xc, Xc);
+      } else {
+        CK(hg::gemm<double>(c->st, true, n, nc, tn, one, c->A.p, tn, Bc, tn, zero, Xc, n, WS(c)));
+      }
       CK(hg::getrs<double>(c->st, n, nc, c->C.p, n, c->ipiv.p, Xc, n, c->luws.p, c->luws.cap, c->status.p));
     } else {
       CK(cudaMemcpy2DAsync(Xc, (size_t)n * sizeof(double2), Bc, (size_t)tn * sizeof(double2), (size_t)n * sizeof(double2),
@@ -1235,10 +1242,21 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
       CK(cudaMemcpyAsync(c->A64.p, c->A.p, (size_t)tn * n * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
     }
     CK(cudaEventRecord(c->ev[1], c->st));
+    // the LU's workspace for the digit-sliced tensor-core products (lu_tensor != 0)
+    const size_t lwz =
+        (c->o.solver != 2 && c->o.lu_tensor != 0 && hg::zgemm_tc_supported()) ? hg::lu_work_bytes_z(n) : 0;
+    if (lwz) CK(c->luws.ensure(lwz));
     if (irsp == 1) {
       CK(c->C.ensure((size_t)n * n));
-      CK(hg::gemm<double>(c->st, true, n, n, tn, make_double2(1, 0), c->A.p, tn, c->A.p, tn, make_double2(0, 0), c->C.p,
-                          n));
+      if (lwz && c->luws.cap >= hg::zgemm_tc_work_bytes(n, n, tn)) {
+        // C = A^T A as -(0 - A^T A): one sliced product with the transposed operand, then the sign
+        CK(cudaMemsetAsync(c->C.p, 0, (size_t)n * n * sizeof(double2), c->st));
+        CK(hg::zgemm_tc(c->st, n, n, tn, c->A.p, tn, c->A.p, tn, c->C.p, n, c->luws.p, c->luws.cap, c->status.p, true));
+        k_negate<<<1024, 256, 0, c->st>>>((long)n * n, c->C.p, c->C.p);
+      } else {
+        CK(hg::gemm<double>(c->st, true, n, n, tn, make_double2(1, 0), c->A.p, tn, c->A.p, tn, make_double2(0, 0),
+                            c->C.p, n));
+      }
     }
     if (c->o.solver == 2) {
       CK(cudaMemsetAsync(c->info.p, 0, sizeof(int), c->st));
@@ -1246,8 +1264,6 @@ int hg_fill_factor(hg_ctx* c, int irsp) {
       if (r) return r;
     } else {
       // U12 and the trailing updates as exact digit products on the tensor cores (lu_tensor != 0)
-      const size_t lwz = (c->o.lu_tensor != 0 && hg::zgemm_tc_supported()) ? hg::lu_work_bytes_z(n) : 0;
-      if (lwz) CK(c->luws.ensure(lwz));
       if (irsp == 1)
         CK(hg::getrf<double>(c->st, n, c->C.p, n, c->ipiv.p, c->info.p, c->luws.p, lwz, c->o.lu_tensor, &c->lu_aux));
       else

@@ -124,16 +124,17 @@ class HMatrix {
   Impl* p;
 };
 
-// Complex128 C -= A B on the tcgen05 tensor cores, FP64-accurate, by exact
-// BF16 digit slicing of both operands (hg_zgemm_tc.cu): A m x k (lda), B k x n
-// (ldb), C m x n (ldc), column-major; B may alias C (B is sliced before C is
-// written), A may not.  About 2^-48 of each output plus 2^-57 of sum |a||b|.
+// Complex128 C -= op(A) B on the tcgen05 tensor cores, FP64-accurate, by
+// exact BF16 digit slicing of both operands (hg_zgemm_tc.cu): op(A) = A
+// (m x k, lda) or, with transa, A^T of the k x m matrix A (lda, no
+// conjugation); B k x n (ldb), C m x n (ldc), column-major; B may alias C (B
+// is sliced before C is written), A may not.  About 2^-48 of each output plus 2^-57 of sum |a||b|.
 // ws: 256-byte aligned device scratch of zgemm_tc_work_bytes(m, n, k) bytes.
 // status (device int) receives -1000 if a bounded wait ran out.
 bool zgemm_tc_supported();
 size_t zgemm_tc_work_bytes(int m, int n, int k);
 cudaError_t zgemm_tc(cudaStream_t st, int m, int n, int k, const double2* A, long lda, const double2* B, long ldb,
-                     double2* C, long ldc, void* ws, size_t ws_bytes, int* status);
+                     double2* C, long ldc, void* ws, size_t ws_bytes, int* status, bool transa = false);
 
 // getrs for the complex64 factors of a two-level getrf (tc_passes != 0):
 // uses the inverses of the 256 x 256 diagonal blocks that getrf kept in its

@@ -124,16 +124,37 @@ __device__ __forceinline__ double oz_scale2(double v, int sc) {
 
 // A's digits: [kZD][mp][kp] BF16 rows (K fastest), row i holding Ar(i, :) at
 // 0..k-1 and Ai(i, :) at k..2k-1, zero beyond (rows m..mp-1, K 2k..kp-1);
-// ex[i] the row's exponent.  One CTA per 32 rows: their largest entries
-// first, then 32 x 32 tiles transposed through shared memory, so that the
-// reads of A and the digit writes are both coalesced.
+// ex[i] the row's exponent.  The operand is A (m x k, A[i + p lda]) or, with
+// TRANS, the transpose of the k x m matrix A (A[p + i lda]: its rows are A's
+// columns).  One CTA per 32 rows: their largest entries first, then 32 x 32
+// tiles through shared memory (transposed for A, direct for TRANS), so that
+// the reads of A and the digit writes are both coalesced.
+template <bool TRANS>
 __global__ void __launch_bounds__(256) k_zoz_slice_a(int m, int k, int mp, int kp, const double2* __restrict__ A,
                                                      long lda, int* __restrict__ ex, uint16_t* __restrict__ D) {
   __shared__ double2 t[32][33];
   __shared__ unsigned long long red[8][32];
   __shared__ int es[32];
   const int i0 = blockIdx.x * 32, tx = threadIdx.x, ty = threadIdx.y;
-  {
+  if (TRANS) {  // a warp per row, lanes along its contiguous entries
+    for (int r = ty; r < 32; r += 8) {
+      const int i = i0 + r;
+      unsigned long long amax = 0;
+      if (i < m)
+        for (int p = tx; p < k; p += 32) {
+          const double2 a = A[p + (long)i * lda];
+          amax = max(amax, max(oz_abs_bits(a.x), oz_abs_bits(a.y)));
+        }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) amax = max(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+      if (tx == 0) {
+        const int e = oz_exp_bits(amax);
+        es[r] = e;
+        if (i < mp) ex[i] = e;
+      }
+    }
+    __syncthreads();
+  } else {
     unsigned long long amax = 0;
     const int i = i0 + tx;
     if (i < m)
@@ -154,14 +175,19 @@ __global__ void __launch_bounds__(256) k_zoz_slice_a(int m, int k, int mp, int k
   const size_t slice = (size_t)mp * kp;
   for (int p0 = 0; p0 < k; p0 += 32) {
     for (int r = ty; r < 32; r += 8) {
-      const int i = i0 + tx, p = p0 + r;
-      t[r][tx] = (i < m && p < k) ? A[i + (long)p * lda] : make_double2(0.0, 0.0);
+      if (TRANS) {  // t[r][tx] = op(i0 + r, p0 + tx)
+        const int i = i0 + r, p = p0 + tx;
+        t[r][tx] = (i < m && p < k) ? A[p + (long)i * lda] : make_double2(0.0, 0.0);
+      } else {  // t[r][tx] = op(i0 + tx, p0 + r)
+        const int i = i0 + tx, p = p0 + r;
+        t[r][tx] = (i < m && p < k) ? A[i + (long)p * lda] : make_double2(0.0, 0.0);
+      }
     }
     __syncthreads();
     for (int r = ty; r < 32; r += 8) {
       const int i = i0 + r, p = p0 + tx;
       if (i >= mp || p >= k) continue;
-      const double2 a = t[tx][r];
+      const double2 a = TRANS ? t[r][tx] : t[tx][r];
       uint16_t dr[kZD], di[kZD];
       oz_digits_d(a.x, es[r], dr);
       oz_digits_d(a.y, es[r], di);
@@ -434,7 +460,7 @@ size_t zgemm_tc_work_bytes(int m, int n, int k) {
 }
 
 cudaError_t zgemm_tc(cudaStream_t st, int m, int n, int k, const double2* A, long lda, const double2* B, long ldb,
-                     double2* C, long ldc, void* ws, size_t ws_bytes, int* status) {
+                     double2* C, long ldc, void* ws, size_t ws_bytes, int* status, bool transa) {
   if (m <= 0 || n <= 0 || k <= 0) return cudaSuccess;
   if (!zgemm_tc_supported()) return cudaErrorNotSupported;
   if (!ws || ws_bytes < zgemm_tc_work_bytes(m, n, k) || (reinterpret_cast<uintptr_t>(ws) & 255u))
@@ -451,7 +477,10 @@ cudaError_t zgemm_tc(cudaStream_t st, int m, int n, int k, const double2* A, lon
     uint16_t* Bd = reinterpret_cast<uint16_t*>(w + lw.b_off);
     int* ex = reinterpret_cast<int*>(w + lw.ex_off);
     int* fx = reinterpret_cast<int*>(w + lw.fx_off);
-    k_zoz_slice_a<<<lw.mp / 32, dim3(32, 8), 0, st>>>(m, kc, lw.mp, lw.kp, A + (long)k0 * lda, lda, ex, Ad);
+    if (transa)
+      k_zoz_slice_a<true><<<lw.mp / 32, dim3(32, 8), 0, st>>>(m, kc, lw.mp, lw.kp, A + k0, lda, ex, Ad);
+    else
+      k_zoz_slice_a<false><<<lw.mp / 32, dim3(32, 8), 0, st>>>(m, kc, lw.mp, lw.kp, A + (long)k0 * lda, lda, ex, Ad);
     k_zoz_slice_b<<<(lw.np / 2 + 7) / 8, 256, 0, st>>>(kc, n, lw.np, lw.kp, B + k0, ldb, fx, Bd);
     CUtensorMap ma, mb;
     if (!oz_map(&ma, Ad, lw.kp, kZD * lw.mp, kZTM) || !oz_map(&mb, Bd, lw.kp, kZD * lw.np, kZTN))
