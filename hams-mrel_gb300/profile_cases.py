@@ -8,10 +8,13 @@ repository root, e.g.
     python hams-mrel_gb300/profile_cases.py gemm 6016 6016 32
     python hams-mrel_gb300/profile_cases.py gesv 6048 38 1
 
-  gemm M N K [ITERS] [PREC]  complex GEMM C -= A B (PREC 1 complex64, 0 complex128)
+  gemm M N K [ITERS] [PREC]  complex GEMM C -= A B (PREC: hg_bench_gemm's variant, 0 complex128
+                             SIMT, 1 complex64 SIMT, 2-4 complex64 tensor cores, 5 complex128
+                             digit-sliced tensor cores)
   gesv N NRHS PREC           dense solve (hg_gesv) of a random diagonally
                              dominated system: LU panels, trailing updates,
-                             triangular solves, refinement residuals
+                             triangular solves, refinement residuals (PREC 0
+                             plain, 1 mixed)
   step [PREC]                one frequency-solve of the 6048-panel 5-body
                              benchmark array (fill, LU, solves, forces)
   fill N H PREC              two Green fills + LUs of a cylinder array of about N
